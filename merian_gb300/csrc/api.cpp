@@ -1,0 +1,677 @@
+// C ABI of the GB300 path tracer (declared in include/gbpt.h): context, scene upload, render and
+// traversal queries. Host-only C++ on the CUDA runtime; the kernels live in kernels.cu.
+#include "gbpt.h"
+#include "host_common.h"
+#include "runtime.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace gbpt {
+
+static thread_local std::string g_last_error;
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+struct GeomHost {
+    uint32_t first_vertex, first_triangle, material, flags;
+};
+static_assert(sizeof(GeomHost) == 16, "GeomGPU layout");
+
+} // namespace gbpt
+
+using namespace gbpt;
+
+struct gbpt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::mutex mu;
+    std::map<uint32_t, SceneGPU> scenes;
+    uint32_t next_scene = 1;
+    Work work;
+    unsigned long long* d_misc = nullptr; // [0] nodes, [1] tris, [2] error word
+    gbpt_hit* d_hits = nullptr;
+    uint64_t hits_cap = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+#define GBPT_CUDA_CHECK(call)                                                                      \
+    do {                                                                                           \
+        const cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                                   \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                         \
+            return e_ == cudaErrorMemoryAllocation ? GBPT_ERR_NO_MEMORY : GBPT_ERR_CUDA;           \
+        }                                                                                          \
+    } while (0)
+
+int upload(void** dst, const void* src, size_t bytes, uint64_t& total) {
+    if (bytes == 0) {
+        *dst = nullptr;
+        return GBPT_OK;
+    }
+    GBPT_CUDA_CHECK(cudaMalloc(dst, bytes));
+    total += bytes;
+    const cudaError_t e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(*dst);
+        *dst = nullptr;
+        set_error(std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+        return GBPT_ERR_CUDA;
+    }
+    return GBPT_OK;
+}
+
+void free_scene(SceneGPU& s) {
+    void* ptrs[] = {s.nodes,    s.tris,     s.verts,    s.idx,      s.geoms,      s.mats,
+                    s.env,      s.env_marg, s.env_cond, s.env_func, s.light_tris, s.light_cdf};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    s = SceneGPU{};
+}
+
+int check_ctx(gbpt_ctx* ctx) {
+    if (!ctx) {
+        set_error("null context");
+        return GBPT_ERR_INVALID;
+    }
+    const cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+        return GBPT_ERR_CUDA;
+    }
+    return GBPT_OK;
+}
+
+// Reads and clears the kernels' error word; returns GBPT_ERR_DEVICE when it was set.
+int check_device_error(gbpt_ctx* ctx) {
+    uint32_t flags[2] = {0, 0};
+    if (ctx->work.counters) {
+        GBPT_CUDA_CHECK(cudaMemcpyAsync(&flags[0], ctx->work.counters + 3, 4,
+                                        cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    unsigned long long misc = 0;
+    GBPT_CUDA_CHECK(cudaMemcpyAsync(&misc, ctx->d_misc + 2, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    GBPT_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    flags[1] = (uint32_t)misc;
+    if (flags[0] | flags[1]) {
+        if (ctx->work.counters) cudaMemsetAsync(ctx->work.counters + 3, 0, 4, ctx->stream);
+        cudaMemsetAsync(ctx->d_misc + 2, 0, 8, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+        set_error("kernel error flag raised (traversal stack overflow)");
+        return GBPT_ERR_DEVICE;
+    }
+    return GBPT_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+GBPT_API uint32_t gbpt_abi_version(void) { return GBPT_ABI_VERSION; }
+
+GBPT_API const char* gbpt_last_error(void) { return g_last_error.c_str(); }
+
+GBPT_API int gbpt_create(int device, uint64_t stream, gbpt_ctx** out_ctx) {
+    if (!out_ctx) {
+        set_error("gbpt_create: null out_ctx");
+        return GBPT_ERR_INVALID;
+    }
+    *out_ctx = nullptr;
+    int n = 0;
+    GBPT_CUDA_CHECK(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) {
+        set_error("gbpt_create: no such CUDA device");
+        return GBPT_ERR_INVALID;
+    }
+    GBPT_CUDA_CHECK(cudaSetDevice(device));
+    auto ctx = std::make_unique<gbpt_ctx>();
+    ctx->device = device;
+    if (stream) {
+        ctx->stream = (cudaStream_t)stream;
+    } else {
+        GBPT_CUDA_CHECK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        ctx->own_stream = true;
+    }
+    GBPT_CUDA_CHECK(cudaMalloc((void**)&ctx->d_misc, 4 * sizeof(unsigned long long)));
+    GBPT_CUDA_CHECK(cudaMemset(ctx->d_misc, 0, 4 * sizeof(unsigned long long)));
+    GBPT_CUDA_CHECK(cudaEventCreate(&ctx->ev0));
+    GBPT_CUDA_CHECK(cudaEventCreate(&ctx->ev1));
+    const int rc = work_reserve(ctx->work, 0, 0);
+    if (rc != GBPT_OK) {
+        set_error("gbpt_create: work buffer allocation failed");
+        return rc;
+    }
+    *out_ctx = ctx.release();
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_destroy(gbpt_ctx* ctx) {
+    if (!ctx) return GBPT_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& kv : ctx->scenes) free_scene(kv.second);
+    work_free(ctx->work);
+    if (ctx->d_misc) cudaFree(ctx->d_misc);
+    if (ctx->d_hits) cudaFree(ctx->d_hits);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_synchronize(gbpt_ctx* ctx) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    GBPT_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    return check_device_error(ctx);
+}
+
+GBPT_API int gbpt_memory_info(gbpt_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes,
+                              uint64_t* ctx_bytes) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    size_t f = 0, t = 0;
+    GBPT_CUDA_CHECK(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+    if (ctx_bytes) {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        uint64_t b = ctx->work.bytes;
+        for (auto& kv : ctx->scenes) b += kv.second.bytes;
+        *ctx_bytes = b;
+    }
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t* out_scene) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!d || !out_scene || (d->triangle_count && (!d->vertices || !d->indices)) ||
+        (d->geometry_count && !d->geometries) || (d->material_count && !d->materials)) {
+        set_error("gbpt_scene_create: null pointer in scene description");
+        return GBPT_ERR_INVALID;
+    }
+    if (d->instance_count != 0) {
+        set_error("gbpt_scene_create: two-level (instanced) scenes are not supported yet");
+        return GBPT_ERR_INVALID;
+    }
+    // validate geometry ranges and gather world-space triangles
+    BuildInput bi;
+    uint64_t total_tris = 0;
+    for (uint32_t g = 0; g < d->geometry_count; ++g) {
+        const gbpt_geometry& geo = d->geometries[g];
+        if ((uint64_t)geo.first_triangle + geo.triangle_count > d->triangle_count) {
+            set_error("gbpt_scene_create: geometry " + std::to_string(g) + " triangle range out of bounds");
+            return GBPT_ERR_INVALID;
+        }
+        if (geo.material_id >= d->material_count) {
+            set_error("gbpt_scene_create: geometry " + std::to_string(g) + " material out of range");
+            return GBPT_ERR_INVALID;
+        }
+        total_tris += geo.triangle_count;
+    }
+    if (total_tris >= (1ull << 31)) {
+        set_error("gbpt_scene_create: too many triangles");
+        return GBPT_ERR_INVALID;
+    }
+    for (uint32_t m = 0; m < d->material_count; ++m) {
+        if (d->materials[m].model > GBPT_MATERIAL_OPENPBR_TRANSMISSION) {
+            set_error("gbpt_scene_create: material " + std::to_string(m) + " has an unknown model");
+            return GBPT_ERR_INVALID;
+        }
+    }
+    bi.v.reserve(9 * total_tris);
+    bi.prim.reserve(total_tris);
+    bi.geom.reserve(total_tris);
+    bi.flags.reserve(total_tris);
+    for (uint32_t g = 0; g < d->geometry_count; ++g) {
+        const gbpt_geometry& geo = d->geometries[g];
+        const uint32_t tf = (geo.instance_mask & 0xFFu) |
+                            ((geo.flags & GBPT_MESH_TWO_SIDED) ? (1u << 8) : 0u) |
+                            ((geo.flags & GBPT_MESH_FLIP_FACING) ? (1u << 9) : 0u);
+        for (uint32_t k = 0; k < geo.triangle_count; ++k) {
+            const uint64_t tri = (uint64_t)geo.first_triangle + k;
+            for (int c = 0; c < 3; ++c) {
+                const uint64_t vi = (uint64_t)geo.first_vertex + d->indices[3 * tri + c];
+                if (vi >= d->vertex_count) {
+                    set_error("gbpt_scene_create: vertex index out of bounds in geometry " +
+                              std::to_string(g));
+                    return GBPT_ERR_INVALID;
+                }
+                const float* p = d->vertices[vi].position;
+                if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(p[2])) {
+                    set_error("gbpt_scene_create: non-finite vertex position");
+                    return GBPT_ERR_INVALID;
+                }
+                bi.v.insert(bi.v.end(), p, p + 3);
+            }
+            bi.prim.push_back(k);
+            bi.geom.push_back(g);
+            bi.flags.push_back(tf);
+        }
+    }
+    CwBvh bvh;
+    if (!build_cwbvh(bi, bvh, 48)) return GBPT_ERR_INVALID;
+
+    SceneGPU s;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    uint64_t bytes = 0;
+    auto fail = [&](int code) {
+        free_scene(s);
+        return code;
+    };
+    if ((rc = upload(&s.nodes, bvh.nodes.data(), bvh.nodes.size() * sizeof(CwNode), bytes))) return fail(rc);
+    if ((rc = upload(&s.tris, bvh.tris.data(), bvh.tris.size() * sizeof(TriRecord), bytes))) return fail(rc);
+    if ((rc = upload(&s.verts, d->vertices, d->vertex_count * sizeof(gbpt_packed_vertex), bytes))) return fail(rc);
+    if ((rc = upload(&s.idx, d->indices, d->triangle_count * 3 * sizeof(uint32_t), bytes))) return fail(rc);
+    std::vector<GeomHost> gh(d->geometry_count);
+    for (uint32_t g = 0; g < d->geometry_count; ++g)
+        gh[g] = {d->geometries[g].first_vertex, d->geometries[g].first_triangle,
+                 d->geometries[g].material_id, d->geometries[g].flags};
+    if ((rc = upload(&s.geoms, gh.data(), gh.size() * sizeof(GeomHost), bytes))) return fail(rc);
+    if ((rc = upload(&s.mats, d->materials, d->material_count * sizeof(gbpt_material), bytes))) return fail(rc);
+    s.n_nodes = bvh.nodes.size();
+    s.n_tris = bvh.tris.size();
+    s.n_verts = d->vertex_count;
+    s.geom_count = d->geometry_count;
+    s.mat_count = d->material_count;
+    s.depth = bvh.depth;
+
+    // emissive triangles, power = area x luminance (next-event estimation)
+    {
+        std::vector<float> lt;
+        std::vector<double> pw;
+        for (uint32_t g = 0; g < d->geometry_count; ++g) {
+            const gbpt_geometry& geo = d->geometries[g];
+            const gbpt_material& m = d->materials[geo.material_id];
+            if (m.model == GBPT_MATERIAL_DIFFUSE) continue;
+            const double lum = 0.299 * m.emission[0] + 0.587 * m.emission[1] + 0.114 * m.emission[2];
+            if (!(lum > 0.0)) continue;
+            for (uint32_t k = 0; k < geo.triangle_count; ++k) {
+                const uint64_t tri = (uint64_t)geo.first_triangle + k;
+                const float* p[3];
+                for (int c = 0; c < 3; ++c)
+                    p[c] = d->vertices[geo.first_vertex + d->indices[3 * tri + c]].position;
+                const double e1[3] = {(double)p[1][0] - p[0][0], (double)p[1][1] - p[0][1], (double)p[1][2] - p[0][2]};
+                const double e2[3] = {(double)p[2][0] - p[0][0], (double)p[2][1] - p[0][1], (double)p[2][2] - p[0][2]};
+                const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                             cz = e1[0] * e2[1] - e1[1] * e2[0];
+                const double area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+                if (!(area > 0.0)) continue;
+                pw.push_back(area * lum);
+                uint32_t gw = g, fw = (geo.flags & GBPT_MESH_FLIP_FACING) ? 1u : 0u, zw = 0;
+                float f[12];
+                for (int c = 0; c < 3; ++c) {
+                    f[4 * c + 0] = p[c][0];
+                    f[4 * c + 1] = p[c][1];
+                    f[4 * c + 2] = p[c][2];
+                }
+                std::memcpy(&f[3], &gw, 4);
+                std::memcpy(&f[7], &fw, 4);
+                std::memcpy(&f[11], &zw, 4);
+                lt.insert(lt.end(), f, f + 12);
+            }
+        }
+        if (!pw.empty()) {
+            double acc = 0.0;
+            for (double x : pw) acc += x;
+            std::vector<float> cdf(pw.size());
+            double run = 0.0;
+            for (size_t i = 0; i < pw.size(); ++i) {
+                run += pw[i];
+                cdf[i] = (float)(run / acc);
+            }
+            cdf.back() = 1.0f;
+            if ((rc = upload(&s.light_tris, lt.data(), lt.size() * sizeof(float), bytes))) return fail(rc);
+            if ((rc = upload(&s.light_cdf, cdf.data(), cdf.size() * sizeof(float), bytes))) return fail(rc);
+            s.n_lights = (uint32_t)pw.size();
+            s.light_total = (float)acc;
+        }
+    }
+    // environment and its importance-sampling tables (luminance x sin(theta), floored)
+    if (d->env && d->env->texels && d->env->width && d->env->height) {
+        const gbpt_env_map& e = *d->env;
+        const uint32_t w = e.width, h = e.height;
+        if ((rc = upload(&s.env, e.texels, (size_t)w * h * 4 * sizeof(float), bytes))) return fail(rc);
+        s.ew = w;
+        s.eh = h;
+        std::memcpy(s.env_m, e.to_local, sizeof(s.env_m));
+        s.env_intensity = e.intensity;
+        std::vector<double> func((size_t)w * h);
+        double mean = 0.0;
+        for (uint32_t y = 0; y < h; ++y) {
+            const double st = std::sin(3.14159265358979323846 * (y + 0.5) / h);
+            for (uint32_t x = 0; x < w; ++x) {
+                const float* t = &e.texels[4 * ((size_t)y * w + x)];
+                const double l = std::max(0.0, 0.299 * t[0] + 0.587 * t[1] + 0.114 * t[2]);
+                func[(size_t)y * w + x] = l * st;
+                mean += l * st;
+            }
+        }
+        mean /= (double)w * h;
+        for (double& f : func) f += 1e-3 * mean + 1e-30;
+        std::vector<float> ffunc(func.size()), cond((size_t)h * (w + 1)), marg(h + 1);
+        std::vector<double> rows(h);
+        double tot = 0.0;
+        for (uint32_t y = 0; y < h; ++y) {
+            double r = 0.0;
+            cond[(size_t)y * (w + 1)] = 0.0f;
+            for (uint32_t x = 0; x < w; ++x) r += func[(size_t)y * w + x];
+            double run = 0.0;
+            for (uint32_t x = 0; x < w; ++x) {
+                run += func[(size_t)y * w + x];
+                cond[(size_t)y * (w + 1) + x + 1] = (float)(run / r);
+            }
+            cond[(size_t)y * (w + 1) + w] = 1.0f;
+            rows[y] = r;
+            tot += r;
+        }
+        double run = 0.0;
+        marg[0] = 0.0f;
+        for (uint32_t y = 0; y < h; ++y) {
+            run += rows[y];
+            marg[y + 1] = (float)(run / tot);
+        }
+        marg[h] = 1.0f;
+        for (size_t i = 0; i < func.size(); ++i) ffunc[i] = (float)func[i];
+        s.env_func_int = (float)(tot / ((double)w * h));
+        if ((rc = upload(&s.env_func, ffunc.data(), ffunc.size() * sizeof(float), bytes))) return fail(rc);
+        if ((rc = upload(&s.env_cond, cond.data(), cond.size() * sizeof(float), bytes))) return fail(rc);
+        if ((rc = upload(&s.env_marg, marg.data(), marg.size() * sizeof(float), bytes))) return fail(rc);
+    }
+    s.bytes = bytes;
+    const uint32_t id = ctx->next_scene++;
+    ctx->scenes[id] = s;
+    *out_scene = id;
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_scene_destroy(gbpt_ctx* ctx, uint32_t scene) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) {
+        set_error("gbpt_scene_destroy: unknown scene id");
+        return GBPT_ERR_NOT_FOUND;
+    }
+    GBPT_CUDA_CHECK(cudaStreamSynchronize(ctx->stream)); // work in flight may still read it
+    free_scene(it->second);
+    ctx->scenes.erase(it);
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_scene_stats(gbpt_ctx* ctx, uint32_t scene, uint64_t* nodes, uint64_t* tris,
+                              uint64_t* bytes, uint32_t* depth) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) {
+        set_error("gbpt_scene_stats: unknown scene id");
+        return GBPT_ERR_NOT_FOUND;
+    }
+    if (nodes) *nodes = it->second.n_nodes;
+    if (tris) *tris = it->second.n_tris;
+    if (bytes) *bytes = it->second.bytes;
+    if (depth) *depth = it->second.depth;
+    return GBPT_OK;
+}
+
+static int validate_params(const gbpt_camera* cam, const gbpt_render_params* p) {
+    if (!cam || !p) {
+        set_error("null camera or params");
+        return GBPT_ERR_INVALID;
+    }
+    if (p->width == 0 || p->height == 0 || (uint64_t)p->width * p->height > (1ull << 31)) {
+        set_error("render: width/height out of range");
+        return GBPT_ERR_INVALID;
+    }
+    if (p->spp < 0 || p->spp > (1 << 24) || p->max_path_length < 1 || p->max_path_length > 64) {
+        set_error("render: spp must be in [0, 2^24] and max path length in [1, 64]");
+        return GBPT_ERR_INVALID;
+    }
+    if (p->pixel_count && !p->pixels) {
+        set_error("render: pixel_count without a pixel list");
+        return GBPT_ERR_INVALID;
+    }
+    for (uint32_t i = 0; i < p->pixel_count; ++i) {
+        if (p->pixels[i] >= p->width * p->height) {
+            set_error("render: pixel id out of range");
+            return GBPT_ERR_INVALID;
+        }
+    }
+    return GBPT_OK;
+}
+
+static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
+                       const gbpt_render_params* p, float* out_dev, float* out_host,
+                       gbpt_render_stats* stats) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if ((rc = validate_params(cam, p))) return rc;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) {
+        set_error("render: unknown scene id");
+        return GBPT_ERR_NOT_FOUND;
+    }
+    Work& w = ctx->work;
+    const uint32_t n_pix = p->pixel_count ? p->pixel_count : p->width * p->height;
+    RenderArgs a;
+    a.camera = *cam;
+    a.params = *p;
+    a.pixel_count = n_pix;
+    a.pixels_device = nullptr;
+    if (p->pixel_count) {
+        if (p->pixel_count > w.pix_id_cap) {
+            if (w.pix_id) cudaFree(w.pix_id);
+            w.pix_id = nullptr;
+            w.pix_id_cap = 0;
+            GBPT_CUDA_CHECK(cudaMalloc((void**)&w.pix_id, (size_t)p->pixel_count * 4));
+            w.pix_id_cap = p->pixel_count;
+        }
+        GBPT_CUDA_CHECK(cudaMemcpyAsync(w.pix_id, p->pixels, (size_t)p->pixel_count * 4,
+                                        cudaMemcpyHostToDevice, ctx->stream));
+        a.pixels_device = w.pix_id;
+    }
+    if (!out_dev) {
+        if (n_pix > w.out_cap) {
+            if (w.out) cudaFree(w.out);
+            w.out = nullptr;
+            w.out_cap = 0;
+            GBPT_CUDA_CHECK(cudaMalloc((void**)&w.out, (size_t)n_pix * sizeof(float4)));
+            w.out_cap = n_pix;
+        }
+        a.out_device = w.out;
+    } else {
+        a.out_device = (float4*)out_dev;
+    }
+    if (p->spp == 0) {
+        GBPT_CUDA_CHECK(cudaMemsetAsync(a.out_device, 0, (size_t)n_pix * sizeof(float4), ctx->stream));
+    }
+    uint64_t launches = 0;
+    if (stats) {
+        GBPT_CUDA_CHECK(cudaMemsetAsync(w.stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
+        GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev0, ctx->stream));
+    }
+    rc = render_frame(it->second, w, a, ctx->stream, &launches);
+    if (rc != GBPT_OK) {
+        set_error(rc == GBPT_ERR_NO_MEMORY ? "render: work buffer allocation failed"
+                                           : "render: kernel launch failed: " +
+                                                 cuda_error_string(cudaGetLastError()));
+        return rc;
+    }
+    if (stats) GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (out_host) {
+        GBPT_CUDA_CHECK(cudaMemcpyAsync(out_host, a.out_device, (size_t)n_pix * sizeof(float4),
+                                        cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (stats || out_host) {
+        if ((rc = check_device_error(ctx))) return rc;
+    }
+    if (stats) {
+        unsigned long long st[2] = {0, 0};
+        GBPT_CUDA_CHECK(cudaMemcpy(st, w.stats, sizeof(st), cudaMemcpyDeviceToHost));
+        float ms = 0.f;
+        GBPT_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        stats->samples = (uint64_t)n_pix * (uint64_t)p->spp;
+        stats->rays = st[0];
+        stats->shadow_rays = st[1];
+        stats->kernel_launches = launches;
+        stats->device_ms = ms;
+    }
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_render(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
+                         const gbpt_render_params* params, float* out_rgba_host,
+                         gbpt_render_stats* stats) {
+    if (!out_rgba_host) {
+        set_error("gbpt_render: null output");
+        return GBPT_ERR_INVALID;
+    }
+    return render_impl(ctx, scene, camera, params, nullptr, out_rgba_host, stats);
+}
+
+GBPT_API int gbpt_render_device(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
+                                const gbpt_render_params* params, float* out_rgba_device,
+                                gbpt_render_stats* stats) {
+    if (!out_rgba_device) {
+        set_error("gbpt_render_device: null output");
+        return GBPT_ERR_INVALID;
+    }
+    return render_impl(ctx, scene, camera, params, out_rgba_device, nullptr, stats);
+}
+
+GBPT_API int gbpt_trace_primary(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
+                                uint32_t width, uint32_t height, uint32_t instance_mask,
+                                gbpt_hit* out_hits_host) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!camera || !out_hits_host || width == 0 || height == 0 ||
+        (uint64_t)width * height > (1ull << 28)) {
+        set_error("gbpt_trace_primary: invalid arguments");
+        return GBPT_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) {
+        set_error("gbpt_trace_primary: unknown scene id");
+        return GBPT_ERR_NOT_FOUND;
+    }
+    const uint64_t n = (uint64_t)width * height;
+    if (n > ctx->hits_cap) {
+        if (ctx->d_hits) cudaFree(ctx->d_hits);
+        ctx->d_hits = nullptr;
+        ctx->hits_cap = 0;
+        GBPT_CUDA_CHECK(cudaMalloc((void**)&ctx->d_hits, n * sizeof(gbpt_hit)));
+        ctx->hits_cap = n;
+    }
+    rc = trace_primary(it->second, *camera, width, height, instance_mask, ctx->d_hits,
+                       reinterpret_cast<uint32_t*>(ctx->d_misc + 2), ctx->stream);
+    if (rc) {
+        set_error("gbpt_trace_primary: launch failed");
+        return rc;
+    }
+    GBPT_CUDA_CHECK(cudaMemcpyAsync(out_hits_host, ctx->d_hits, n * sizeof(gbpt_hit),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+    return check_device_error(ctx);
+}
+
+static int trace_common(gbpt_ctx* ctx, uint32_t scene, const gbpt_ray* rays, uint32_t n,
+                        uint32_t mask, int any_hit, gbpt_hit* hits, double* npr, double* tpr) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if ((n && (!rays || !hits))) {
+        set_error("gbpt_trace: null rays or hits");
+        return GBPT_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) {
+        set_error("gbpt_trace: unknown scene id");
+        return GBPT_ERR_NOT_FOUND;
+    }
+    if (npr || tpr) GBPT_CUDA_CHECK(cudaMemsetAsync(ctx->d_misc, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    rc = trace_rays(it->second, rays, n, mask, any_hit, hits, ctx->d_misc, ctx->stream);
+    if (rc) {
+        set_error("gbpt_trace: launch failed");
+        return rc;
+    }
+    if (npr || tpr) {
+        unsigned long long c[2] = {0, 0};
+        GBPT_CUDA_CHECK(cudaMemcpyAsync(c, ctx->d_misc, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
+        if ((rc = check_device_error(ctx))) return rc;
+        if (npr) *npr = n ? (double)c[0] / n : 0.0;
+        if (tpr) *tpr = n ? (double)c[1] / n : 0.0;
+    }
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_trace(gbpt_ctx* ctx, uint32_t scene, const gbpt_ray* rays_device, uint32_t n,
+                        uint32_t instance_mask, int any_hit, gbpt_hit* hits_device) {
+    return trace_common(ctx, scene, rays_device, n, instance_mask, any_hit, hits_device, nullptr,
+                        nullptr);
+}
+
+GBPT_API int gbpt_trace_counted(gbpt_ctx* ctx, uint32_t scene, const gbpt_ray* rays_device,
+                                uint32_t n, uint32_t instance_mask, int any_hit,
+                                gbpt_hit* hits_device, double* nodes_per_ray,
+                                double* tris_per_ray) {
+    double a = 0, b = 0;
+    const int rc = trace_common(ctx, scene, rays_device, n, instance_mask, any_hit, hits_device, &a, &b);
+    if (nodes_per_ray) *nodes_per_ray = a;
+    if (tris_per_ray) *tris_per_ray = b;
+    return rc;
+}
+
+// Camera::recompute_ray_basis + Camera::write_to (camera.cpp:263-266,349-367), focus on target
+GBPT_API int gbpt_camera_look_at(const float position[3], const float target[3], const float up[3],
+                                 float vfov, float aspect, float near_plane, float far_plane,
+                                 gbpt_camera* out) {
+    if (!position || !target || !up || !out) {
+        set_error("gbpt_camera_look_at: null argument");
+        return GBPT_ERR_INVALID;
+    }
+    const V3 pos = v3(position[0], position[1], position[2]);
+    const V3 tgt = v3(target[0], target[1], target[2]);
+    const V3 upv = v3(up[0], up[1], up[2]);
+    const V3 fwd = normalize(tgt - pos);
+    const V3 rgt = normalize(cross(fwd, upv));
+    const V3 d = tgt - pos;
+    const float focus = std::sqrt(dot(d, d));
+    const float ht = std::tan(vfov * 0.5f);
+    const V3 U = (ht * aspect * focus) * rgt;
+    const V3 V = (ht * focus) * cross(rgt, fwd);
+    const V3 W = focus * fwd;
+    std::memset(out, 0, sizeof(*out));
+    const float* src[4] = {&pos.x, &U.x, &V.x, &W.x};
+    float* dst[4] = {out->position, out->U, out->V, out->W};
+    for (int k = 0; k < 4; ++k) {
+        dst[k][0] = src[k][0];
+        dst[k][1] = src[k][1];
+        dst[k][2] = src[k][2];
+    }
+    out->near_plane = near_plane;
+    out->far_plane = far_plane;
+    return GBPT_OK;
+}
+
+GBPT_API uint32_t gbpt_encode_normal(const float n[3]) { return encode_normal(v3(n[0], n[1], n[2])); }
+
+GBPT_API uint32_t gbpt_pack_half2(float x, float y) { return pack_half2(x, y); }
+
+} // extern "C"

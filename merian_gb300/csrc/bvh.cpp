@@ -1,0 +1,435 @@
+// Host BVH builder: binned-SAH binary BVH, greedily collapsed to an 8-wide tree and written in
+// the compressed-wide layout of Ylitie, Karras and Laine, "Efficient Incoherent Ray Traversal on
+// GPUs Through Compressed Wide BVHs" (HPG 2017): 80-byte nodes with 8-bit child boxes relative to
+// a per-node origin and power-of-two scale, octant-ordered child slots, and up to three
+// triangles per leaf child.
+//
+// merian itself hands its triangles to the Vulkan driver (BLAS/TLAS build with
+// ePreferFastTrace, scene.cpp:1117-1120,1836-1882), so there is no reference builder to mirror;
+// the traversal semantics that matter for parity (closest hit, culling) live in the kernels.
+#include "host_common.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <thread>
+
+namespace gbpt {
+namespace {
+
+struct Box {
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+    float hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    void grow(const Box& b) {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], b.lo[a]);
+            hi[a] = std::max(hi[a], b.hi[a]);
+        }
+    }
+    void grow(const float* p) {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], p[a]);
+            hi[a] = std::max(hi[a], p[a]);
+        }
+    }
+    bool empty() const { return lo[0] > hi[0]; }
+    float area() const {
+        if (empty()) return 0.0f;
+        const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        return 2.0f * (dx * dy + dy * dz + dz * dx);
+    }
+};
+
+struct B2Node {
+    Box box;
+    uint32_t left = 0, right = 0; // children (internal)
+    uint32_t first = 0, count = 0;
+    bool leaf = true;
+};
+
+constexpr int kBins = 32;
+constexpr float kCostTraverse = 0.5f; // relative to one triangle test
+constexpr uint32_t kMaxLeaf = 3;      // CWBVH leaf children hold up to three triangles
+
+struct Builder {
+    const std::vector<Box>& pbox;
+    const std::vector<float>& cent; // 3 per primitive
+    std::vector<uint32_t>& idx;
+    std::vector<B2Node> nodes;
+
+    Builder(const std::vector<Box>& b, const std::vector<float>& c, std::vector<uint32_t>& i)
+        : pbox(b), cent(c), idx(i) {}
+
+    // Builds the subtree over idx[begin, end) into `out` (root at out[root_index]).
+    void build_range(std::vector<B2Node>& out, uint32_t root_index, uint32_t begin, uint32_t end) {
+        struct Task {
+            uint32_t node, begin, end;
+        };
+        std::vector<Task> stack{{root_index, begin, end}};
+        while (!stack.empty()) {
+            const Task t = stack.back();
+            stack.pop_back();
+            const uint32_t n = t.end - t.begin;
+            Box box, cbox;
+            for (uint32_t i = t.begin; i < t.end; ++i) {
+                box.grow(pbox[idx[i]]);
+                cbox.grow(&cent[3 * idx[i]]);
+            }
+            out[t.node].box = box;
+            out[t.node].first = t.begin;
+            out[t.node].count = n;
+            out[t.node].leaf = true;
+            if (n <= 1) continue;
+
+            // binned SAH over the three axes
+            float best_cost = FLT_MAX;
+            int best_axis = -1, best_split = 0;
+            const float parent_area = std::max(box.area(), 1e-30f);
+            for (int a = 0; a < 3; ++a) {
+                const float ext = cbox.hi[a] - cbox.lo[a];
+                if (!(ext > 0.0f)) continue;
+                const float k = (float)kBins / ext;
+                Box bb[kBins];
+                uint32_t bn[kBins] = {};
+                for (uint32_t i = t.begin; i < t.end; ++i) {
+                    const uint32_t p = idx[i];
+                    int b = (int)((cent[3 * p + a] - cbox.lo[a]) * k);
+                    b = std::min(std::max(b, 0), kBins - 1);
+                    bb[b].grow(pbox[p]);
+                    bn[b]++;
+                }
+                float right_area[kBins];
+                uint32_t right_n[kBins];
+                Box acc;
+                uint32_t accn = 0;
+                for (int b = kBins - 1; b > 0; --b) {
+                    acc.grow(bb[b]);
+                    accn += bn[b];
+                    right_area[b] = acc.area();
+                    right_n[b] = accn;
+                }
+                Box lacc;
+                uint32_t lacn = 0;
+                for (int b = 0; b < kBins - 1; ++b) {
+                    lacc.grow(bb[b]);
+                    lacn += bn[b];
+                    if (lacn == 0 || right_n[b + 1] == 0) continue;
+                    const float c = kCostTraverse + (lacc.area() * (float)lacn +
+                                                     right_area[b + 1] * (float)right_n[b + 1]) /
+                                                        parent_area;
+                    if (c < best_cost) {
+                        best_cost = c;
+                        best_axis = a;
+                        best_split = b + 1;
+                    }
+                }
+            }
+            const float leaf_cost = (float)n;
+            if (n <= kMaxLeaf && (best_axis < 0 || leaf_cost <= best_cost)) continue;
+
+            uint32_t mid;
+            if (best_axis < 0) {
+                // all centroids coincide: split by count
+                mid = t.begin + n / 2;
+            } else {
+                const float k = (float)kBins / (cbox.hi[best_axis] - cbox.lo[best_axis]);
+                const auto it = std::partition(
+                    idx.begin() + t.begin, idx.begin() + t.end, [&](uint32_t p) {
+                        int b = (int)((cent[3 * p + best_axis] - cbox.lo[best_axis]) * k);
+                        b = std::min(std::max(b, 0), kBins - 1);
+                        return b < best_split;
+                    });
+                mid = (uint32_t)(it - idx.begin());
+                if (mid == t.begin || mid == t.end) mid = t.begin + n / 2;
+            }
+            const uint32_t l = (uint32_t)out.size();
+            out.emplace_back();
+            out.emplace_back();
+            out[t.node].leaf = false;
+            out[t.node].left = l;
+            out[t.node].right = l + 1;
+            stack.push_back({l + 1, mid, t.end});
+            stack.push_back({l, t.begin, mid});
+        }
+    }
+};
+
+// Smallest power-of-two scale with 255 * scale >= ext, as a biased exponent in [1, 254].
+int quant_exponent(double ext) {
+    if (!(ext > 0.0)) return 1;
+    int e;
+    std::frexp(ext / 255.0, &e); // ext/255 = f * 2^e, f in [0.5, 1)
+    // 2^e >= ext/255 always holds; try one smaller in case ext/255 is an exact power of two
+    if (std::ldexp(255.0, e - 1) >= ext) e -= 1;
+    int biased = e + 127;
+    return std::min(std::max(biased, 1), 254);
+}
+
+} // namespace
+
+bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
+    const size_t n = in.prim.size();
+    out.nodes.clear();
+    out.tris.clear();
+    out.depth = 1;
+    if (n == 0) {
+        CwNode root{};
+        root.w[3] = 127u | (127u << 8) | (127u << 16); // unit scale, no children
+        out.nodes.push_back(root);
+        return true;
+    }
+    std::vector<Box> pbox(n);
+    std::vector<float> cent(3 * n);
+    std::vector<uint32_t> idx(n);
+    Box scene;
+    for (size_t i = 0; i < n; ++i) {
+        Box b;
+        b.grow(&in.v[9 * i + 0]);
+        b.grow(&in.v[9 * i + 3]);
+        b.grow(&in.v[9 * i + 6]);
+        pbox[i] = b;
+        for (int a = 0; a < 3; ++a) cent[3 * i + a] = 0.5f * (b.lo[a] + b.hi[a]);
+        idx[i] = (uint32_t)i;
+        scene.grow(b);
+    }
+    for (int a = 0; a < 3; ++a) {
+        out.lo[a] = scene.lo[a];
+        out.hi[a] = scene.hi[a];
+    }
+
+    Builder bld(pbox, cent, idx);
+    std::vector<B2Node>& b2 = bld.nodes;
+    b2.reserve(2 * n);
+    b2.emplace_back();
+    // Top levels serially until there are enough independent subtrees, then the subtrees in
+    // parallel into private node arrays that are appended afterwards.
+    {
+        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        if (n < 200000 || hw == 1) {
+            bld.build_range(b2, 0, 0, (uint32_t)n);
+        } else {
+            // split the root range into up to 2*hw pieces by a coarse serial build (depth-limited)
+            struct Part {
+                uint32_t node, begin, end;
+            };
+            std::vector<Part> parts{{0, 0, (uint32_t)n}};
+            // expand the largest part with one SAH split at a time
+            while (parts.size() < 2 * hw) {
+                size_t bi = 0;
+                for (size_t i = 1; i < parts.size(); ++i)
+                    if (parts[i].end - parts[i].begin > parts[bi].end - parts[bi].begin) bi = i;
+                const Part p = parts[bi];
+                if (p.end - p.begin < 1024) break;
+                {
+                    Box box, cbox;
+                    for (uint32_t i = p.begin; i < p.end; ++i) {
+                        box.grow(pbox[idx[i]]);
+                        cbox.grow(&cent[3 * idx[i]]);
+                    }
+                    int axis = 0;
+                    for (int a = 1; a < 3; ++a)
+                        if (cbox.hi[a] - cbox.lo[a] > cbox.hi[axis] - cbox.lo[axis]) axis = a;
+                    // median split on the widest centroid axis keeps the parts balanced
+                    const uint32_t mid = p.begin + (p.end - p.begin) / 2;
+                    std::nth_element(idx.begin() + p.begin, idx.begin() + mid,
+                                     idx.begin() + p.end, [&](uint32_t x, uint32_t y) {
+                                         return cent[3 * x + axis] < cent[3 * y + axis];
+                                     });
+                    b2[p.node].box = box;
+                    b2[p.node].first = p.begin;
+                    b2[p.node].count = p.end - p.begin;
+                    b2[p.node].leaf = false;
+                    const uint32_t l = (uint32_t)b2.size();
+                    b2.emplace_back();
+                    b2.emplace_back();
+                    b2[p.node].left = l;
+                    b2[p.node].right = l + 1;
+                    parts[bi] = {l, p.begin, mid};
+                    parts.push_back({l + 1, mid, p.end});
+                }
+            }
+            std::vector<std::vector<B2Node>> sub(parts.size());
+            std::vector<std::thread> threads;
+            for (size_t i = 0; i < parts.size(); ++i) {
+                threads.emplace_back([&, i]() {
+                    Builder local(pbox, cent, idx);
+                    sub[i].reserve(2 * (parts[i].end - parts[i].begin));
+                    sub[i].emplace_back();
+                    local.build_range(sub[i], 0, parts[i].begin, parts[i].end);
+                });
+            }
+            for (auto& t : threads) t.join();
+            for (size_t i = 0; i < parts.size(); ++i) {
+                const uint32_t base = (uint32_t)b2.size() - 1; // sub root replaces parts[i].node
+                // sub[i][0] goes to parts[i].node; sub[i][k>0] to base + k
+                auto remap = [&](uint32_t k) { return k == 0 ? parts[i].node : base + k; };
+                for (size_t k = 1; k < sub[i].size(); ++k) {
+                    B2Node nd = sub[i][k];
+                    if (!nd.leaf) {
+                        nd.left = remap(nd.left);
+                        nd.right = remap(nd.right);
+                    }
+                    b2.push_back(nd);
+                }
+                B2Node root = sub[i][0];
+                if (!root.leaf) {
+                    root.left = remap(root.left);
+                    root.right = remap(root.right);
+                }
+                b2[parts[i].node] = root;
+            }
+        }
+    }
+
+    // ---- collapse to 8-wide and emit ----------------------------------------------------------
+    struct Task {
+        uint32_t b2node, cw, depth;
+    };
+    out.nodes.reserve(b2.size() / 4 + 1);
+    out.tris.reserve(n);
+    out.nodes.emplace_back();
+    std::vector<Task> stack{{0, 0, 1}};
+    auto is_inner = [&](uint32_t k) { return !b2[k].leaf && b2[k].count > kMaxLeaf; };
+    while (!stack.empty()) {
+        const Task t = stack.back();
+        stack.pop_back();
+        out.depth = std::max(out.depth, t.depth);
+        if (t.depth > max_depth) {
+            set_error("BVH deeper than the traversal stack (" + std::to_string(max_depth) + ")");
+            return false;
+        }
+        std::vector<uint32_t> ch;
+        if (is_inner(t.b2node)) {
+            ch = {b2[t.b2node].left, b2[t.b2node].right};
+            while (ch.size() < 8) {
+                int best = -1;
+                float best_area = -1.0f;
+                for (size_t i = 0; i < ch.size(); ++i) {
+                    if (is_inner(ch[i]) && b2[ch[i]].box.area() > best_area) {
+                        best_area = b2[ch[i]].box.area();
+                        best = (int)i;
+                    }
+                }
+                if (best < 0) break;
+                const uint32_t k = ch[best];
+                ch[best] = b2[k].left;
+                ch.push_back(b2[k].right);
+            }
+        } else {
+            ch = {t.b2node}; // the whole tree is one leaf
+        }
+        // node box and centroid
+        Box nbox;
+        for (uint32_t c : ch) nbox.grow(b2[c].box);
+        float pc[3];
+        for (int a = 0; a < 3; ++a) pc[a] = 0.5f * (nbox.lo[a] + nbox.hi[a]);
+        // octant slot assignment: slot s has the diagonal (+-1,+-1,+-1), sign bit a set = negative;
+        // a child goes where it lies furthest back along that diagonal (first visited by rays
+        // whose direction octant is s)
+        const size_t m = ch.size();
+        int slot_of[8];
+        {
+            struct Cand {
+                float cost;
+                int child, slot;
+            };
+            std::vector<Cand> cands;
+            for (size_t i = 0; i < m; ++i) {
+                float off[3];
+                for (int a = 0; a < 3; ++a)
+                    off[a] = 0.5f * (b2[ch[i]].box.lo[a] + b2[ch[i]].box.hi[a]) - pc[a];
+                for (int s = 0; s < 8; ++s) {
+                    float c = 0.0f;
+                    for (int a = 0; a < 3; ++a) c += ((s >> a) & 1) ? -off[a] : off[a];
+                    cands.push_back({c, (int)i, s});
+                }
+            }
+            std::sort(cands.begin(), cands.end(), [](const Cand& x, const Cand& y) {
+                if (x.cost != y.cost) return x.cost < y.cost;
+                if (x.child != y.child) return x.child < y.child;
+                return x.slot < y.slot;
+            });
+            bool used_slot[8] = {};
+            for (size_t i = 0; i < m; ++i) slot_of[i] = -1;
+            for (const Cand& c : cands) {
+                if (slot_of[c.child] >= 0 || used_slot[c.slot]) continue;
+                slot_of[c.child] = c.slot;
+                used_slot[c.slot] = true;
+            }
+        }
+        int child_at[8];
+        for (int s = 0; s < 8; ++s) child_at[s] = -1;
+        for (size_t i = 0; i < m; ++i) child_at[slot_of[i]] = (int)i;
+
+        CwNode node{};
+        // quantisation frame
+        int ebias[3];
+        for (int a = 0; a < 3; ++a) {
+            const double ext = (double)nbox.hi[a] - (double)nbox.lo[a];
+            ebias[a] = quant_exponent(ext);
+            while (std::ldexp(255.0, ebias[a] - 127) < ext && ebias[a] < 254) ebias[a]++;
+        }
+        std::memcpy(&node.w[0], &nbox.lo[0], 4);
+        std::memcpy(&node.w[1], &nbox.lo[1], 4);
+        std::memcpy(&node.w[2], &nbox.lo[2], 4);
+        uint32_t imask = 0;
+        const uint32_t child_base = (uint32_t)out.nodes.size();
+        const uint32_t tri_base = (uint32_t)out.tris.size();
+        uint32_t n_inner = 0;
+        uint8_t meta[8] = {}, qlo[3][8] = {}, qhi[3][8] = {};
+        std::vector<Task> push;
+        for (int s = 0; s < 8; ++s) {
+            const int i = child_at[s];
+            if (i < 0) continue;
+            const B2Node& c = b2[ch[i]];
+            for (int a = 0; a < 3; ++a) {
+                const double scale = std::ldexp(1.0, ebias[a] - 127);
+                double lo = std::floor(((double)c.box.lo[a] - (double)nbox.lo[a]) / scale);
+                double hi = std::ceil(((double)c.box.hi[a] - (double)nbox.lo[a]) / scale);
+                lo = std::min(std::max(lo, 0.0), 255.0);
+                hi = std::min(std::max(hi, 0.0), 255.0);
+                qlo[a][s] = (uint8_t)lo;
+                qhi[a][s] = (uint8_t)hi;
+            }
+            if (is_inner(ch[i])) {
+                imask |= 1u << s;
+                meta[s] = (uint8_t)((1u << 5) | (24u + (uint32_t)s));
+                push.push_back({ch[i], child_base + n_inner, t.depth + 1});
+                n_inner++;
+            } else {
+                const uint32_t off = (uint32_t)out.tris.size() - tri_base;
+                const uint32_t cnt = c.count;
+                for (uint32_t k = 0; k < cnt; ++k) {
+                    const uint32_t p = idx[c.first + k];
+                    TriRecord tr{};
+                    std::memcpy(tr.v0, &in.v[9 * p + 0], 12);
+                    std::memcpy(tr.v1, &in.v[9 * p + 3], 12);
+                    std::memcpy(tr.v2, &in.v[9 * p + 6], 12);
+                    tr.prim = in.prim[p];
+                    tr.geom = in.geom[p];
+                    tr.pad = in.flags.empty() ? 0xFFu : in.flags[p];
+                    out.tris.push_back(tr);
+                }
+                static const uint8_t unary[4] = {0, 1, 3, 7};
+                meta[s] = (uint8_t)((unary[cnt] << 5) | off);
+            }
+        }
+        node.w[3] = (uint32_t)ebias[0] | ((uint32_t)ebias[1] << 8) | ((uint32_t)ebias[2] << 16) |
+                    (imask << 24);
+        node.w[4] = child_base;
+        node.w[5] = tri_base;
+        std::memcpy(&node.w[6], meta, 8);
+        std::memcpy(&node.w[8], qlo[0], 8);
+        std::memcpy(&node.w[10], qlo[1], 8);
+        std::memcpy(&node.w[12], qlo[2], 8);
+        std::memcpy(&node.w[14], qhi[0], 8);
+        std::memcpy(&node.w[16], qhi[1], 8);
+        std::memcpy(&node.w[18], qhi[2], 8);
+        out.nodes.resize(out.nodes.size() + n_inner);
+        out.nodes[t.cw] = node;
+        for (auto it = push.rbegin(); it != push.rend(); ++it) stack.push_back(*it);
+    }
+    return true;
+}
+
+} // namespace gbpt

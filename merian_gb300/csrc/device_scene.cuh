@@ -1,0 +1,337 @@
+// Device view of a scene in HBM and the CWBVH traversal.
+//
+// Traversal replaces the hardware ray query merian issues through TraceRayInline with
+// RAY_FLAG_CULL_BACK_FACING_TRIANGLES (acceleration-structure.slang:59-72) on ForceOpaque
+// instances (scene.cpp:1849-1850). Closest hit over triangles whose instance mask intersects the
+// ray mask, back faces culled unless the geometry is TwoSided, the front face swapped by
+// FlipFacing (scene.cpp:1841-1848). Ties at equal t go to the smallest (geometry, primitive), so
+// the result does not depend on the BVH layout.
+#pragma once
+
+#include "device_math.cuh"
+#include "gbpt.h"
+
+namespace gbpt {
+
+struct GeomGPU {
+    uint32_t first_vertex, first_triangle, material, flags;
+};
+
+// per-triangle flag word (third float4 of a triangle record)
+constexpr uint32_t kTriTwoSided = 1u << 8;
+constexpr uint32_t kTriFlip = 1u << 9;
+
+struct DevScene {
+    const uint4* __restrict__ nodes;  // 5 per CWBVH node
+    const float4* __restrict__ tris;  // 3 per triangle record
+    const uint32_t* __restrict__ verts; // gbpt_packed_vertex as 6 words
+    const uint32_t* __restrict__ idx;
+    const GeomGPU* __restrict__ geoms;
+    const float4* __restrict__ mats;  // gbpt_material as 5 float4
+    uint32_t geom_count;
+    // environment
+    const float4* __restrict__ env;
+    uint32_t ew, eh;
+    float env_m[9];
+    float env_intensity;
+    const float* __restrict__ env_marg; // eh + 1, normalised
+    const float* __restrict__ env_cond; // eh * (ew + 1), normalised per row
+    const float* __restrict__ env_func; // eh * ew
+    float env_func_int;
+    // emissive triangles
+    const float4* __restrict__ light_tris; // 3 per light: v0 (w = geometry), v1, v2
+    const float* __restrict__ light_cdf;   // n_lights, inclusive, normalised
+    uint32_t n_lights;
+    float light_total; // sum of area x luminance
+    float p_env;       // probability of choosing the environment in NEE
+};
+
+struct Hit {
+    float t, u, v;
+    uint32_t prim, geom; // geom = 0xFFFFFFFF on miss
+};
+
+// ---- watertight test (Woop, Benthin, Wald 2013) -------------------------------------------------
+// Explicit round-to-nearest intrinsics (no FMA contraction) so the float result equals the
+// host oracle's bit for bit.
+struct RayPre {
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+    float ox, oy, oz; // origin permuted to (kx, ky, kz)
+};
+GBPT_DI float pick(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+GBPT_DI RayPre ray_pre(float3 o, float3 d) {
+    RayPre p;
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    p.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    p.kx = p.kz == 2 ? 0 : p.kz + 1;
+    p.ky = p.kx == 2 ? 0 : p.kx + 1;
+    const float dkz = pick(d.x, d.y, d.z, p.kz);
+    if (dkz < 0.0f) {
+        const int t = p.kx;
+        p.kx = p.ky;
+        p.ky = t;
+    }
+    p.Sx = __fdiv_rn(pick(d.x, d.y, d.z, p.kx), dkz);
+    p.Sy = __fdiv_rn(pick(d.x, d.y, d.z, p.ky), dkz);
+    p.Sz = __fdiv_rn(1.0f, dkz);
+    p.ox = pick(o.x, o.y, o.z, p.kx);
+    p.oy = pick(o.x, o.y, o.z, p.ky);
+    p.oz = pick(o.x, o.y, o.z, p.kz);
+    return p;
+}
+
+// Returns true with t, u, v when hit within [tmin, tmax] on an accepted face.
+GBPT_DI bool intersect_tri(const RayPre& p, float4 a4, float4 b4, float4 c4, uint32_t tflags,
+                           float tmin, float tmax, float& t_out, float& u_out, float& v_out) {
+    const float Akx = __fsub_rn(pick(a4.x, a4.y, a4.z, p.kx), p.ox);
+    const float Aky = __fsub_rn(pick(a4.x, a4.y, a4.z, p.ky), p.oy);
+    const float Akz = __fsub_rn(pick(a4.x, a4.y, a4.z, p.kz), p.oz);
+    const float Bkx = __fsub_rn(pick(b4.x, b4.y, b4.z, p.kx), p.ox);
+    const float Bky = __fsub_rn(pick(b4.x, b4.y, b4.z, p.ky), p.oy);
+    const float Bkz = __fsub_rn(pick(b4.x, b4.y, b4.z, p.kz), p.oz);
+    const float Ckx = __fsub_rn(pick(c4.x, c4.y, c4.z, p.kx), p.ox);
+    const float Cky = __fsub_rn(pick(c4.x, c4.y, c4.z, p.ky), p.oy);
+    const float Ckz = __fsub_rn(pick(c4.x, c4.y, c4.z, p.kz), p.oz);
+    const float Ax = __fsub_rn(Akx, __fmul_rn(p.Sx, Akz));
+    const float Ay = __fsub_rn(Aky, __fmul_rn(p.Sy, Akz));
+    const float Bx = __fsub_rn(Bkx, __fmul_rn(p.Sx, Bkz));
+    const float By = __fsub_rn(Bky, __fmul_rn(p.Sy, Bkz));
+    const float Cx = __fsub_rn(Ckx, __fmul_rn(p.Sx, Ckz));
+    const float Cy = __fsub_rn(Cky, __fmul_rn(p.Sy, Ckz));
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = __double2float_rn(__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx)));
+        V = __double2float_rn(__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx)));
+        W = __double2float_rn(__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax)));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f) return false;
+    if (!(tflags & kTriTwoSided)) {
+        const bool front = det > 0.0f;
+        if (front == ((tflags & kTriFlip) != 0)) return false;
+    }
+    const float Az = __fmul_rn(p.Sz, Akz);
+    const float Bz = __fmul_rn(p.Sz, Bkz);
+    const float Cz = __fmul_rn(p.Sz, Ckz);
+    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    const float t = __fdiv_rn(T, det);
+    if (!(t >= tmin && t <= tmax)) return false;
+    t_out = t;
+    u_out = __fdiv_rn(V, det);
+    v_out = __fdiv_rn(W, det);
+    return true;
+}
+
+// ---- CWBVH traversal ----------------------------------------------------------------------------
+constexpr int kStackSize = 48;
+
+struct TraceCounters {
+    uint32_t nodes, tris;
+};
+
+GBPT_DI float safe_rcp(float d) {
+    const float m = 1e-20f;
+    return __fdiv_rn(1.0f, fabsf(d) > m ? d : copysignf(m, d));
+}
+
+// Closest hit (ANY = false) or first hit (ANY = true) of a ray against the scene. Sets *err when
+// the traversal stack would overflow (the builder bounds the depth, so this does not happen for
+// trees it accepted).
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ Hit trace_ray(const DevScene& sc, float3 o, float3 d, float tmin,
+                                         float tmax, uint32_t ray_mask, TraceCounters* ctr,
+                                         uint32_t* err) {
+    Hit best;
+    best.t = tmax;
+    best.u = best.v = 0.0f;
+    best.prim = 0xFFFFFFFFu;
+    best.geom = 0xFFFFFFFFu;
+    uint32_t best_geom_key = 0xFFFFFFFFu, best_prim_key = 0xFFFFFFFFu;
+    const RayPre pre = ray_pre(o, d);
+    const float3 inv = f3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+    const uint32_t oct = (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) |
+                         ((__float_as_uint(d.z) >> 31) << 2);
+    const uint32_t oct_inv = 7u - oct;
+    const uint32_t oct_inv4 = oct_inv * 0x01010101u;
+    const bool negx = d.x < 0.0f || (d.x == 0.0f && signbit(d.x));
+    const bool negy = d.y < 0.0f || (d.y == 0.0f && signbit(d.y));
+    const bool negz = d.z < 0.0f || (d.z == 0.0f && signbit(d.z));
+    const float kErr = 1.0f / 1048576.0f; // 2^-20 relative slack on dequantised plane distances
+
+    uint2 stack[kStackSize];
+    int sp = 0;
+    uint2 ngroup = make_uint2(0u, 0x80000000u);
+    bool found = false;
+    while (true) {
+        uint2 tgroup = make_uint2(0u, 0u);
+        {
+            // descend into the nearest remaining child of the current node group
+            const uint32_t hits = ngroup.y;
+            const uint32_t bit = 31u - __clz(hits & 0xFF000000u);
+            ngroup.y &= ~(1u << bit);
+            if (ngroup.y > 0x00FFFFFFu) {
+                if (sp >= kStackSize) {
+                    atomicOr(err, 1u);
+                    break;
+                }
+                stack[sp++] = ngroup;
+            }
+            const uint32_t slot = (bit - 24u) ^ oct_inv;
+            const uint32_t imask_parent = hits & 0xFFu;
+            const uint32_t rel = __popc(imask_parent & ((1u << slot) - 1u));
+            const uint32_t ni = ngroup.x + rel;
+            if (COUNT) ctr->nodes++;
+            const uint4 n0 = __ldg(&sc.nodes[5 * ni + 0]);
+            const uint4 n1 = __ldg(&sc.nodes[5 * ni + 1]);
+            const uint4 n2 = __ldg(&sc.nodes[5 * ni + 2]);
+            const uint4 n3 = __ldg(&sc.nodes[5 * ni + 3]);
+            const uint4 n4 = __ldg(&sc.nodes[5 * ni + 4]);
+            const float px = __uint_as_float(n0.x), py = __uint_as_float(n0.y),
+                        pz = __uint_as_float(n0.z);
+            const float sx = __uint_as_float((n0.w & 0xFFu) << 23);
+            const float sy = __uint_as_float(((n0.w >> 8) & 0xFFu) << 23);
+            const float sz = __uint_as_float(((n0.w >> 16) & 0xFFu) << 23);
+            const uint32_t imask = n0.w >> 24;
+            const float aix = sx * inv.x, aiy = sy * inv.y, aiz = sz * inv.z;
+            const float aox = (px - o.x) * inv.x, aoy = (py - o.y) * inv.y, aoz = (pz - o.z) * inv.z;
+            const float ex = (fabsf(aox) + 255.0f * fabsf(aix)) * kErr;
+            const float ey = (fabsf(aoy) + 255.0f * fabsf(aiy)) * kErr;
+            const float ez = (fabsf(aoz) + 255.0f * fabsf(aiz)) * kErr;
+            const float nox = aox - ex, fox = aox + ex;
+            const float noy = aoy - ey, foy = aoy + ey;
+            const float noz = aoz - ez, foz = aoz + ez;
+            uint32_t hitmask = 0;
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                const uint32_t meta4 = half ? n1.w : n1.z;
+                const uint32_t is_inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
+                const uint32_t inner_mask4 = (is_inner4 >> 4) * 0xFFu;
+                const uint32_t bit_index4 = (meta4 ^ (oct_inv4 & inner_mask4)) & 0x1F1F1F1Fu;
+                const uint32_t child_bits4 = (meta4 >> 5) & 0x07070707u;
+                const uint32_t qlx = half ? n2.y : n2.x, qly = half ? n2.w : n2.z;
+                const uint32_t qlz = half ? n3.y : n3.x, qhx = half ? n3.w : n3.z;
+                const uint32_t qhy = half ? n4.y : n4.x, qhz = half ? n4.w : n4.z;
+                const uint32_t nqx = negx ? qhx : qlx, fqx = negx ? qlx : qhx;
+                const uint32_t nqy = negy ? qhy : qly, fqy = negy ? qly : qhy;
+                const uint32_t nqz = negz ? qhz : qlz, fqz = negz ? qlz : qhz;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const uint32_t sh = 8u * j;
+                    const float tnx = fmaf((float)((nqx >> sh) & 0xFFu), aix, nox);
+                    const float tny = fmaf((float)((nqy >> sh) & 0xFFu), aiy, noy);
+                    const float tnz = fmaf((float)((nqz >> sh) & 0xFFu), aiz, noz);
+                    const float tfx = fmaf((float)((fqx >> sh) & 0xFFu), aix, fox);
+                    const float tfy = fmaf((float)((fqy >> sh) & 0xFFu), aiy, foy);
+                    const float tfz = fmaf((float)((fqz >> sh) & 0xFFu), aiz, foz);
+                    const float cmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+                    const float cmax = fminf(fminf(tfx, tfy), fminf(tfz, best.t));
+                    if (cmin <= cmax) {
+                        const uint32_t cb = (child_bits4 >> sh) & 7u;
+                        const uint32_t bi = (bit_index4 >> sh) & 31u;
+                        hitmask |= cb << bi;
+                    }
+                }
+            }
+            ngroup = make_uint2(n1.x, (hitmask & 0xFF000000u) | imask);
+            tgroup = make_uint2(n1.y, hitmask & 0x00FFFFFFu);
+        }
+        while (tgroup.y != 0u) {
+            const uint32_t b = __ffs(tgroup.y) - 1u;
+            tgroup.y &= tgroup.y - 1u;
+            const uint32_t ti = tgroup.x + b;
+            const float4 r0 = __ldg(&sc.tris[3 * ti + 0]);
+            const float4 r1 = __ldg(&sc.tris[3 * ti + 1]);
+            const float4 r2 = __ldg(&sc.tris[3 * ti + 2]);
+            const uint32_t tfl = __float_as_uint(r2.w);
+            if (((tfl & 0xFFu) & ray_mask) == 0u) continue;
+            if (COUNT) ctr->tris++;
+            float t, u, v;
+            if (!intersect_tri(pre, r0, r1, r2, tfl, tmin, best.t, t, u, v)) continue;
+            const uint32_t prim = __float_as_uint(r0.w), geom = __float_as_uint(r1.w);
+            if (t < best.t || geom < best_geom_key ||
+                (geom == best_geom_key && prim < best_prim_key)) {
+                best.t = t;
+                best.u = u;
+                best.v = v;
+                best.prim = prim;
+                best.geom = geom;
+                best_geom_key = geom;
+                best_prim_key = prim;
+                found = true;
+                if (ANY) return best;
+            }
+        }
+        if (ngroup.y <= 0x00FFFFFFu) {
+            if (sp == 0) break;
+            ngroup = stack[--sp];
+        }
+    }
+    if (!found) {
+        best.geom = 0xFFFFFFFFu;
+        best.prim = 0xFFFFFFFFu;
+    }
+    return best;
+}
+
+// ---- camera (camera.slang:29-56), bit-identical to the oracle's FP32 build ---------------------------
+struct CamGPU {
+    float3 pos, U, V, W;
+    float near_plane, far_plane, jx, jy;
+};
+GBPT_DI void camera_ray(const CamGPU& c, uint32_t px, uint32_t py, uint32_t w, uint32_t h,
+                        float3& o, float3& d, float& tmin, float& tmax) {
+    const float x = __fdiv_rn(__fadd_rn(__fadd_rn((float)px, 0.5f), c.jx), (float)w);
+    const float y = __fdiv_rn(__fadd_rn(__fadd_rn((float)py, 0.5f), c.jy), (float)h);
+    const float nx = __fadd_rn(__fmul_rn(2.0f, x), -1.0f);
+    const float ny = __fadd_rn(__fmul_rn(-2.0f, y), 1.0f);
+    const float dx = __fadd_rn(__fadd_rn(__fmul_rn(nx, c.U.x), __fmul_rn(ny, c.V.x)), c.W.x);
+    const float dy = __fadd_rn(__fadd_rn(__fmul_rn(nx, c.U.y), __fmul_rn(ny, c.V.y)), c.W.y);
+    const float dz = __fadd_rn(__fadd_rn(__fmul_rn(nx, c.U.z), __fmul_rn(ny, c.V.z)), c.W.z);
+    const float l = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+    d = f3(__fdiv_rn(dx, l), __fdiv_rn(dy, l), __fdiv_rn(dz, l));
+    const float lw = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(c.W.x, c.W.x), __fmul_rn(c.W.y, c.W.y)),
+                                          __fmul_rn(c.W.z, c.W.z)));
+    const float wx = __fdiv_rn(c.W.x, lw), wy = __fdiv_rn(c.W.y, lw), wz = __fdiv_rn(c.W.z, lw);
+    const float cosv = __fadd_rn(__fadd_rn(__fmul_rn(wx, d.x), __fmul_rn(wy, d.y)), __fmul_rn(wz, d.z));
+    const float inv_cos = __fdiv_rn(1.0f, cosv);
+    o = c.pos;
+    tmin = __fmul_rn(c.near_plane, inv_cos);
+    tmax = __fmul_rn(c.far_plane, inv_cos);
+}
+
+// ---- environment (environment-map.slang:23-35, utils/math.slang:243-250) -------------------------------
+GBPT_DI float3 env_to_local(const DevScene& s, float3 d) {
+    const float* M = s.env_m;
+    return f3(M[0] * d.x + M[1] * d.y + M[2] * d.z, M[3] * d.x + M[4] * d.y + M[5] * d.z,
+              M[6] * d.x + M[7] * d.y + M[8] * d.z);
+}
+GBPT_DI int wrapi(int i, int n) {
+    const int r = i % n;
+    return r < 0 ? r + n : r;
+}
+GBPT_DI float3 env_eval(const DevScene& s, float3 dir) {
+    if (s.ew == 0u) return f3(0.f, 0.f, 0.f);
+    const float3 p = normalize(env_to_local(s, dir));
+    const float u = atan2f(p.x, -p.z) * kInv2Pi + 0.5f;
+    const float v = acosf(fminf(fmaxf(p.y, -1.0f), 1.0f)) * kInvPi;
+    if (!(u == u) || !(v == v)) return f3(0.f, 0.f, 0.f);
+    const float x = u * (float)s.ew - 0.5f, y = v * (float)s.eh - 0.5f;
+    const float fx = floorf(x), fy = floorf(y);
+    const float a = x - fx, b = y - fy;
+    const int ix = (int)fx, iy = (int)fy;
+    const int x0 = wrapi(ix, (int)s.ew), x1 = wrapi(ix + 1, (int)s.ew);
+    const int y0 = wrapi(iy, (int)s.eh), y1 = wrapi(iy + 1, (int)s.eh);
+    const float4 t00 = __ldg(&s.env[(size_t)y0 * s.ew + x0]);
+    const float4 t10 = __ldg(&s.env[(size_t)y0 * s.ew + x1]);
+    const float4 t01 = __ldg(&s.env[(size_t)y1 * s.ew + x0]);
+    const float4 t11 = __ldg(&s.env[(size_t)y1 * s.ew + x1]);
+    const float3 top = f3(t00.x, t00.y, t00.z) * (1.0f - a) + f3(t10.x, t10.y, t10.z) * a;
+    const float3 bot = f3(t01.x, t01.y, t01.z) * (1.0f - a) + f3(t11.x, t11.y, t11.z) * a;
+    return (top * (1.0f - b) + bot * b) * s.env_intensity;
+}
+
+} // namespace gbpt

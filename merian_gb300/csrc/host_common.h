@@ -1,0 +1,153 @@
+// Host-side helpers shared by the scene generators, the BVH builder and the C ABI.
+#pragma once
+
+#include "gbpt.h"
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace gbpt {
+
+struct V3 {
+    float x, y, z;
+};
+inline V3 v3(float x, float y, float z) { return {x, y, z}; }
+inline V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 operator*(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline V3 normalize(V3 a) {
+    const float l = std::sqrt(dot(a, a));
+    return {a.x / l, a.y / l, a.z / l};
+}
+
+// Octahedral projection + packSnorm2x16 (merian encoding.slang:14-30). packSnorm2x16 rounds
+// clamp(v,-1,1)*32767 to nearest (ties away from zero) and stores x in the low 16 bits.
+inline uint32_t encode_normal(V3 n) {
+    const float inv_l1 = 1.0f / ((std::fabs(n.x) + std::fabs(n.y)) + std::fabs(n.z));
+    float px, py;
+    if (n.z < 0.0f) {
+        px = std::copysign(1.0f - std::fabs(n.y * inv_l1), n.x);
+        py = std::copysign(1.0f - std::fabs(n.x * inv_l1), n.y);
+    } else {
+        px = n.x * inv_l1;
+        py = n.y * inv_l1;
+    }
+    auto pack = [](float v) -> uint32_t {
+        v = v < -1.0f ? -1.0f : (v > 1.0f ? 1.0f : v);
+        const int32_t i = (int32_t)std::round(v * 32767.0f);
+        return (uint32_t)(uint16_t)(int16_t)i;
+    };
+    return pack(px) | (pack(py) << 16);
+}
+
+// float -> IEEE binary16, round to nearest even (Slang half(x) conversion).
+inline uint16_t float_to_half(float f) {
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u;
+    uint32_t mag = x & 0x7fffffffu;
+    if (mag >= 0x7f800000u) { // inf / nan
+        return (uint16_t)(sign | 0x7c00u | (mag > 0x7f800000u ? 0x200u : 0u));
+    }
+    if (mag >= 0x477ff000u) { // rounds to >= 65520 -> inf
+        return (uint16_t)(sign | 0x7c00u);
+    }
+    if (mag < 0x38800000u) { // half subnormal (or zero): value = q * 2^-24
+        float a;
+        std::memcpy(&a, &mag, 4);
+        // exact power-of-two scaling, then round half to even; q = 1024 is the smallest normal
+        const uint32_t q = (uint32_t)std::nearbyint(a * 16777216.0f);
+        return (uint16_t)(sign | q);
+    }
+    // normal: rebias exponent 127 -> 15, keep 10 mantissa bits
+    uint32_t h = ((mag - 0x38000000u) >> 13);
+    const uint32_t rem = mag & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h++;
+    return (uint16_t)(sign | h);
+}
+
+inline uint32_t pack_half2(float a, float b) {
+    return (uint32_t)float_to_half(a) | ((uint32_t)float_to_half(b) << 16);
+}
+
+// PCG32 (O'Neill, pcg-random.org): 64-bit LCG state, XSH-RR output. Integer-only, so a seed
+// gives the same stream on every host.
+struct Pcg32 {
+    uint64_t state = 0, inc = 1;
+    Pcg32(uint64_t seed, uint64_t stream) {
+        inc = (stream << 1u) | 1u;
+        next();
+        state += seed;
+        next();
+    }
+    uint32_t next() {
+        const uint64_t old = state;
+        state = old * 6364136223846793005ULL + inc;
+        const uint32_t xorshifted = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        const uint32_t rot = (uint32_t)(old >> 59u);
+        return (xorshifted >> rot) | (xorshifted << ((32u - rot) & 31u));
+    }
+    // [0, 1) with 24 random bits
+    float uniform() { return (float)(next() >> 8) * (1.0f / 16777216.0f); }
+    double uniform_d() {
+        const uint64_t hi = next() >> 5, lo = next() >> 6;
+        return ((double)hi * 67108864.0 + (double)lo) * (1.0 / 9007199254740992.0);
+    }
+};
+
+void set_error(const std::string& msg);
+
+// ---- CWBVH (compressed 8-wide BVH, Ylitie/Karras/Laine HPG 2017 layout) -------------------
+// Node = 5 x 16 bytes:
+//   w0: p.x p.y p.z (float), e.x | e.y<<8 | e.z<<16 | imask<<24
+//   w1: child_base, tri_base, meta[0..3], meta[4..7]
+//   w2: q_lo.x[0..7], q_lo.y[0..7]   (bytes)
+//   w3: q_lo.z[0..7], q_hi.x[0..7]
+//   w4: q_hi.y[0..7], q_hi.z[0..7]
+// meta: inner child = 0b001_11sss (24 + slot); leaf = unary triangle count in bits 5..7, triangle
+// offset from tri_base in bits 0..4; empty = 0.
+struct CwNode {
+    uint32_t w[20];
+};
+static_assert(sizeof(CwNode) == 80, "CWBVH node must be 80 bytes");
+
+// Triangle record used by the traversal: 3 x float4 = 48 bytes
+//   (v0.xyz, primitive id bits), (v1.xyz, geometry id bits), (v2.xyz, 0)
+struct TriRecord {
+    float v0[3];
+    uint32_t prim;
+    float v1[3];
+    uint32_t geom;
+    float v2[3];
+    uint32_t pad;
+};
+static_assert(sizeof(TriRecord) == 48, "triangle record must be 48 bytes");
+
+struct BuildInput {
+    // world-space triangles
+    std::vector<float> v; // 9 floats per triangle
+    std::vector<uint32_t> prim;
+    std::vector<uint32_t> geom;
+    std::vector<uint32_t> flags; // instance mask (bits 0-7), two-sided (bit 8), flip (bit 9)
+};
+
+struct CwBvh {
+    std::vector<CwNode> nodes;
+    std::vector<TriRecord> tris;
+    uint32_t depth = 0;
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+};
+
+// Binned-SAH BVH2 build, greedy surface-area collapse to 8-wide, octant slot ordering and 8-bit
+// conservative quantisation. Returns false (and sets the error) when the tree is deeper than
+// max_depth.
+bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth);
+
+} // namespace gbpt

@@ -1,0 +1,90 @@
+// Internal interface between the C ABI (api.cpp, host only) and the kernels (kernels.cu).
+#pragma once
+
+#include "gbpt.h"
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+namespace gbpt {
+
+struct DevScene; // device_scene.cuh
+
+// A scene resident in HBM. All pointers are device pointers owned by the context.
+struct SceneGPU {
+    void* nodes = nullptr;      // CWBVH, 80 B per node
+    void* tris = nullptr;       // 48 B per triangle record
+    void* verts = nullptr;      // gbpt_packed_vertex
+    void* idx = nullptr;        // uint32 x 3 per triangle
+    void* geoms = nullptr;      // GeomGPU
+    void* mats = nullptr;       // gbpt_material
+    void* env = nullptr;        // float4 texels
+    void* env_marg = nullptr;
+    void* env_cond = nullptr;
+    void* env_func = nullptr;
+    void* light_tris = nullptr; // 3 float4 per emissive triangle
+    void* light_cdf = nullptr;
+    uint64_t n_nodes = 0, n_tris = 0, n_verts = 0;
+    uint32_t geom_count = 0, mat_count = 0;
+    uint32_t ew = 0, eh = 0;
+    float env_m[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    float env_intensity = 1.0f;
+    float env_func_int = 0.0f;
+    uint32_t n_lights = 0;
+    float light_total = 0.0f;
+    uint32_t depth = 0;
+    uint64_t bytes = 0;
+};
+
+// Work buffers of the wavefront, grown on demand and kept for the context's lifetime.
+struct Work {
+    uint64_t path_cap = 0;  // paths per wave
+    uint64_t pixel_cap = 0; // pixels per wave
+    // path state (SoA, indexed by wave-local path id)
+    float4* thr = nullptr;  // throughput rgb, current IOR
+    float4* rad = nullptr;  // radiance rgb, pdf of the last BSDF sample
+    uint32_t* rng = nullptr;
+    // ray queues (two, ping-pong) and hits
+    float4* q_od[2] = {nullptr, nullptr}; // 2 float4 per entry: (o, tmin), (d, tmax)
+    uint32_t* q_path[2] = {nullptr, nullptr};
+    float4* hit_tuv = nullptr; // t, u, v, primitive bits
+    uint32_t* hit_geom = nullptr;
+    // shadow queue
+    float4* s_od = nullptr;     // 2 float4 per entry: (o, tmax), (d, 0)
+    float4* s_contrib = nullptr;
+    uint32_t* s_path = nullptr;
+    // per-pixel primary shading point cache (5 float4 per pixel)
+    float4* pix = nullptr;
+    uint32_t* pix_id = nullptr; // pixel ids of the current request (device)
+    uint64_t pix_id_cap = 0;
+    float4* out = nullptr;      // device output staging for host-output renders
+    uint64_t out_cap = 0;
+    // counters: [0],[1] queue counts, [2] shadow count, [3] error flags, [4..7] scratch
+    uint32_t* counters = nullptr;
+    unsigned long long* stats = nullptr; // [0] rays, [1] shadow rays
+    uint64_t bytes = 0;
+};
+
+struct RenderArgs {
+    gbpt_camera camera;
+    gbpt_render_params params;
+    const uint32_t* pixels_device; // nullptr: all pixels
+    uint32_t pixel_count;
+    float4* out_device;
+};
+
+// kernels.cu
+int render_frame(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
+                 uint64_t* launches);
+int trace_rays(const SceneGPU& scene, const gbpt_ray* rays, uint32_t n, uint32_t mask, int any_hit,
+               gbpt_hit* hits, unsigned long long* counters_device, cudaStream_t stream);
+int trace_primary(const SceneGPU& scene, const gbpt_camera& cam, uint32_t w, uint32_t h,
+                  uint32_t mask, gbpt_hit* hits_device, uint32_t* err_device, cudaStream_t stream);
+int work_reserve(Work& work, uint64_t paths, uint64_t pixels);
+void work_free(Work& work);
+
+std::string cuda_error_string(cudaError_t e);
+
+} // namespace gbpt

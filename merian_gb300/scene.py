@@ -1,0 +1,232 @@
+"""Scene data, the device context and the benchmark workloads.
+
+``SceneData`` holds the host arrays of one scene in the layouts of ``include/gbpt.h`` (merian's
+PackedVertexData / GeometryData / material records). ``Context`` owns a ``gbpt_ctx``: scenes
+uploaded to HBM and the render / traversal entry points.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+
+BASE_SEED = 0x1234567
+
+
+@dataclass
+class SceneData:
+    vertices: np.ndarray
+    indices: np.ndarray
+    geometries: np.ndarray
+    materials: np.ndarray
+    env: np.ndarray | None = None          # (h, w, 4) float32
+    env_to_local: np.ndarray = field(default_factory=lambda: np.eye(3, dtype=np.float32))
+    env_intensity: float = 1.0
+
+    @property
+    def triangle_count(self) -> int:
+        return int(self.indices.shape[0])
+
+    def desc(self):
+        """(SceneDesc, keep-alive objects) for gbpt_scene_create / the oracle."""
+        keep = []
+        env_p = None
+        if self.env is not None:
+            env = np.ascontiguousarray(self.env, dtype=np.float32)
+            keep.append(env)
+            e = N.EnvMap()
+            e.texels = env.ctypes.data_as(C.POINTER(C.c_float))
+            e.height, e.width = int(env.shape[0]), int(env.shape[1])
+            e.to_local[:] = [float(x) for x in np.asarray(self.env_to_local, np.float32).reshape(9)]
+            e.intensity = float(self.env_intensity)
+            keep.append(e)
+            env_p = C.pointer(e)
+        d = N.SceneDesc()
+        d.vertices = N.ptr(self.vertices)
+        d.vertex_count = len(self.vertices)
+        d.indices = N.ptr(self.indices)
+        d.triangle_count = self.triangle_count
+        d.geometries = N.ptr(self.geometries)
+        d.geometry_count = len(self.geometries)
+        d.materials = N.ptr(self.materials)
+        d.material_count = len(self.materials)
+        d.env = env_p
+        return d, keep
+
+
+def cornell(seed: int = BASE_SEED) -> SceneData:
+    """The 1,024-triangle Cornell box (gbpt_gen_cornell)."""
+    lib = N.load()
+    v = np.zeros(3072, N.VERTEX_DTYPE)
+    i = np.zeros((1024, 3), np.uint32)
+    g = np.zeros(8, N.GEOMETRY_DTYPE)
+    m = np.zeros(8, N.MATERIAL_DTYPE)
+    N.check(lib.gbpt_gen_cornell(seed, N.ptr(v), N.ptr(i), N.ptr(g), N.ptr(m)))
+    return SceneData(v, i, g, m)
+
+
+def env_lobes(seed: int, width: int = 2048, height: int = 1024) -> np.ndarray:
+    lib = N.load()
+    t = np.zeros((height, width, 4), np.float32)
+    N.check(lib.gbpt_gen_env(seed, width, height, N.ptr(t)))
+    return t
+
+
+def soup(seed: int = BASE_SEED, n_triangles: int = 1_000_000, n_geometries: int = 4096,
+         env_size: tuple[int, int] | None = (2048, 1024)) -> SceneData:
+    """Triangle soup with an optional Gaussian-lobe lat-long environment (gbpt_gen_soup)."""
+    lib = N.load()
+    n_geometries = max(1, min(n_geometries, n_triangles))
+    v = np.zeros(3 * n_triangles, N.VERTEX_DTYPE)
+    i = np.zeros((n_triangles, 3), np.uint32)
+    g = np.zeros(n_geometries, N.GEOMETRY_DTYPE)
+    m = np.zeros(n_geometries, N.MATERIAL_DTYPE)
+    N.check(lib.gbpt_gen_soup(seed, n_triangles, n_geometries, N.ptr(v), N.ptr(i), N.ptr(g),
+                              N.ptr(m)))
+    env = env_lobes(seed ^ 0xE27, *env_size) if env_size else None
+    return SceneData(v, i, g, m, env)
+
+
+def look_at(position, target, up=(0.0, 1.0, 0.0), vfov_deg: float = 40.0, aspect: float = 1.0,
+            near: float = 0.1, far: float = 1000.0) -> N.Camera:
+    """merian Camera basis (camera.cpp:263-266,349-367); near/far are merian's defaults."""
+    lib = N.load()
+    cam = N.Camera()
+    f3 = C.c_float * 3
+    N.check(lib.gbpt_camera_look_at(f3(*position), f3(*target), f3(*up),
+                                    math.radians(vfov_deg), aspect, near, far, C.byref(cam)))
+    return cam
+
+
+def render_params(width: int, height: int, spp: int, max_path_length: int, *,
+                  emission_on_primary: bool = True, instance_mask: int = 0xFF,
+                  frame: int = 0, nee: bool = False, rr_depth: int = 0,
+                  sort_materials: bool = False, pixels: np.ndarray | None = None):
+    p = N.RenderParams()
+    p.width, p.height, p.spp, p.max_path_length = width, height, spp, max_path_length
+    p.emission_on_primary = int(emission_on_primary)
+    p.instance_mask = instance_mask
+    p.frame = frame
+    p.nee = int(nee)
+    p.rr_depth = rr_depth
+    p.sort_materials = int(sort_materials)
+    keep = None
+    if pixels is not None and len(pixels):
+        keep = np.ascontiguousarray(pixels, dtype=np.uint32)
+        p.pixels = keep.ctypes.data_as(C.POINTER(C.c_uint32))
+        p.pixel_count = len(keep)
+    return p, keep
+
+
+# ---- the benchmark workloads -------------------------------------------------------------------
+WORKLOADS = {
+    # strict-parity configuration: the reference's BSDF-only estimator
+    "cornell-256-16spp": dict(scene="cornell", width=256, height=256, spp=16, max_path_length=5,
+                              nee=False, rr_depth=0,
+                              camera=dict(position=(0.5, 0.5, -1.4), target=(0.5, 0.5, 0.0),
+                                          vfov_deg=40.0)),
+    # the headline: 1M-triangle soup, 1080p, 64 spp, path length 8, NEE + roulette from depth 3
+    "soup-1m-1080p-64spp": dict(scene="soup", n_triangles=1_000_000, width=1920, height=1080,
+                                spp=64, max_path_length=8, nee=True, rr_depth=3,
+                                camera=dict(position=(0.5, 0.5, -1.2), target=(0.5, 0.5, 0.5),
+                                            vfov_deg=45.0)),
+}
+
+
+def workload_scene(name: str, seed: int = BASE_SEED, **overrides) -> SceneData:
+    w = dict(WORKLOADS[name], **overrides)
+    if w["scene"] == "cornell":
+        return cornell(seed)
+    return soup(seed, w.get("n_triangles", 1_000_000), w.get("n_geometries", 4096),
+                w.get("env_size", (2048, 1024)))
+
+
+def workload_camera(name: str, width: int | None = None, height: int | None = None) -> N.Camera:
+    w = WORKLOADS[name]
+    width = width or w["width"]
+    height = height or w["height"]
+    c = w["camera"]
+    return look_at(c["position"], c["target"], (0.0, 1.0, 0.0), c["vfov_deg"], width / height)
+
+
+class Context:
+    """One gbpt_ctx on one CUDA device; scenes stay resident in HBM until destroyed."""
+
+    def __init__(self, device: int = 0, stream: int = 0):
+        self.lib = N.load()
+        h = C.c_void_p()
+        N.check(self.lib.gbpt_create(device, stream, C.byref(h)))
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.gbpt_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def upload(self, scene: SceneData) -> int:
+        d, keep = scene.desc()
+        sid = C.c_uint32()
+        N.check(self.lib.gbpt_scene_create(self.handle, C.byref(d), C.byref(sid)))
+        del keep
+        return sid.value
+
+    def destroy_scene(self, sid: int) -> None:
+        N.check(self.lib.gbpt_scene_destroy(self.handle, sid))
+
+    def scene_stats(self, sid: int) -> dict:
+        n, t, b = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        dp = C.c_uint32()
+        N.check(self.lib.gbpt_scene_stats(self.handle, sid, C.byref(n), C.byref(t), C.byref(b),
+                                          C.byref(dp)))
+        return dict(nodes=n.value, tris=t.value, bytes=b.value, depth=dp.value)
+
+    def render(self, sid: int, camera: N.Camera, params: N.RenderParams,
+               stats: bool = False):
+        n = params.pixel_count or params.width * params.height
+        out = np.empty((n, 4), np.float32)
+        st = N.RenderStats()
+        N.check(self.lib.gbpt_render(self.handle, sid, C.byref(camera), C.byref(params),
+                                     N.ptr(out), C.byref(st) if stats else None))
+        return (out, st) if stats else out
+
+    def render_device(self, sid: int, camera: N.Camera, params: N.RenderParams, out_ptr: int,
+                      stats: bool = False):
+        st = N.RenderStats()
+        N.check(self.lib.gbpt_render_device(self.handle, sid, C.byref(camera), C.byref(params),
+                                            out_ptr, C.byref(st) if stats else None))
+        return st if stats else None
+
+    def trace_primary(self, sid: int, camera: N.Camera, width: int, height: int,
+                      mask: int = 0xFF) -> np.ndarray:
+        hits = np.zeros(width * height, N.HIT_DTYPE)
+        N.check(self.lib.gbpt_trace_primary(self.handle, sid, C.byref(camera), width, height, mask,
+                                            N.ptr(hits)))
+        return hits
+
+    def trace(self, sid: int, rays_dev: int, n: int, hits_dev: int, mask: int = 0xFF,
+              any_hit: bool = False, counted: bool = False):
+        if counted:
+            a, b = C.c_double(), C.c_double()
+            N.check(self.lib.gbpt_trace_counted(self.handle, sid, rays_dev, n, mask, int(any_hit),
+                                                hits_dev, C.byref(a), C.byref(b)))
+            return a.value, b.value
+        N.check(self.lib.gbpt_trace(self.handle, sid, rays_dev, n, mask, int(any_hit), hits_dev))
+        return None
+
+    def synchronize(self) -> None:
+        N.check(self.lib.gbpt_synchronize(self.handle))
+
+    def memory_info(self) -> dict:
+        f, t, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        N.check(self.lib.gbpt_memory_info(self.handle, C.byref(f), C.byref(t), C.byref(c)))
+        return dict(free=f.value, total=t.value, ctx=c.value)

@@ -1,0 +1,131 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+Only the tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg load this module; the
+product path never does. ``load()`` builds ``oracle/_build/liboracle.so`` with the Makefile
+beside this file when it is missing or older than its sources.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+SOURCES = [HERE / "oracle.cpp", HERE / "oracle_math.h", HERE.parent / "include" / "gbpt.h"]
+
+_lib = None
+
+
+def build() -> Path:
+    stale = not LIB.exists() or any(s.stat().st_mtime > LIB.stat().st_mtime for s in SOURCES)
+    if stale:
+        subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB))
+        vp, u32, u64, i32, f32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_float
+        lib.oracle_scene_create.restype = vp
+        lib.oracle_scene_create.argtypes = [vp, u64, vp, u64, vp, u32, vp, u32, vp, u32, u32, vp,
+                                            f32]
+        lib.oracle_scene_destroy.argtypes = [vp]
+        lib.oracle_trace_primary.argtypes = [vp, vp, u32, u32, u32, i32, vp, vp]
+        lib.oracle_trace_rays.argtypes = [vp, vp, u32, u32, i32, i32, vp, vp, vp]
+        lib.oracle_render.argtypes = [vp, vp, vp, i32, i32, vp, vp, vp]
+        lib.oracle_num_threads.restype = i32
+        lib.oracle_bsdf_check.argtypes = [i32, vp, vp, f32, f32, vp, f32, u32, u32, vp]
+        _lib = lib
+    return _lib
+
+
+def _p(a) -> int:
+    return a.ctypes.data if a is not None and a.size else 0
+
+
+class OracleScene:
+    """The oracle's own copy of a scene (same host arrays the GPU receives)."""
+
+    def __init__(self, scene):
+        lib = load()
+        self._keep = scene
+        env = None if scene.env is None else np.ascontiguousarray(scene.env, np.float32)
+        self._env = env
+        m = np.ascontiguousarray(np.asarray(scene.env_to_local, np.float32).reshape(9))
+        self._m = m
+        self.h = lib.oracle_scene_create(
+            _p(scene.vertices), len(scene.vertices), _p(scene.indices), scene.triangle_count,
+            _p(scene.geometries), len(scene.geometries), _p(scene.materials),
+            len(scene.materials), _p(env), 0 if env is None else env.shape[1],
+            0 if env is None else env.shape[0], _p(m), float(scene.env_intensity))
+
+    def close(self):
+        if self.h:
+            load().oracle_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def trace_primary(self, camera, width: int, height: int, mask: int = 0xFF,
+                      fp64: bool = True, hit_dtype=None):
+        hits = np.zeros(width * height, hit_dtype)
+        t64 = np.zeros(width * height, np.float64)
+        load().oracle_trace_primary(self.h, C.addressof(camera), width, height, mask, int(fp64),
+                                    _p(hits), _p(t64))
+        return hits, t64
+
+    def trace_rays(self, rays: np.ndarray, mask: int = 0xFF, fp64: bool = False,
+                   any_hit: bool = False, hit_dtype=None):
+        hits = np.zeros(len(rays), hit_dtype)
+        nn, nt = C.c_uint64(), C.c_uint64()
+        load().oracle_trace_rays(self.h, _p(rays), len(rays), mask, int(fp64), int(any_hit),
+                                 _p(hits), C.addressof(nn), C.addressof(nt))
+        return hits, nn.value, nt.value
+
+    def render(self, camera, params, fp64: bool = True, threads: int = 0):
+        """(rgba (n,4) float64, mean of squared per-sample rgb (n,3), traced rays)."""
+        n = params.pixel_count or params.width * params.height
+        rgba = np.zeros((n, 4), np.float64)
+        sq = np.zeros((n, 3), np.float64)
+        rays = C.c_uint64()
+        load().oracle_render(self.h, C.addressof(camera), C.addressof(params), int(fp64), threads,
+                             _p(rgba), _p(sq), C.addressof(rays))
+        return rgba, sq, rays.value
+
+
+def num_threads() -> int:
+    return load().oracle_num_threads()
+
+
+BSDF_KINDS = {"lambert": 0, "ggx": 1, "conductor": 2, "rough_dielectric": 3, "fresnel_mix": 4}
+
+
+def bsdf_check(kind: str, wi, albedo=(0.8, 0.5, 0.2), alpha: float = 0.3,
+               alpha_y: float | None = None, f0=(0.95, 0.64, 0.54), ior_f0: float = 0.04,
+               n_samples: int = 1 << 18, seed: int = 0x1234567) -> dict:
+    """The reference's BSDF property checks (tests/bsdf/bsdf-checks.slang) on the oracle BSDFs."""
+    out = np.zeros(16, np.float32)
+    wi = np.asarray(wi, np.float32)
+    al = np.asarray(albedo, np.float32)
+    f0a = np.asarray(f0, np.float32)
+    load().oracle_bsdf_check(BSDF_KINDS[kind], _p(wi), _p(al), alpha,
+                             alpha if alpha_y is None else alpha_y, _p(f0a), ior_f0, n_samples,
+                             seed, _p(out))
+    return unpack_check(out, n_samples)
+
+
+def unpack_check(out: np.ndarray, n_samples: int) -> dict:
+    return dict(furnace=out[0:3].astype(np.float64), furnace_stderr=out[3:6].astype(np.float64),
+                mean_cos=float(out[6]), stderr_cos=float(out[7]), valid=int(out[8]),
+                max_weight_err=float(out[9]), max_pdf_err=float(out[10]),
+                pdf_integral=float(out[11]), max_recip_err=float(out[12]), n=n_samples)

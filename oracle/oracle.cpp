@@ -1,0 +1,1036 @@
+// ORACLE (test infrastructure only; the product never links or calls this file). CPU restatement
+// of merian's `pt` renderer (include/merian-graph/nodes/render_pt/render_pt.slang:24-130) and of
+// the scene functions it calls (include/merian-shaders/scene/scene.slang:62-102,312-498,
+// hit.slang:7-147), templated on float (the timed CPU baseline) and double (the parity
+// estimator). Hardware ray queries have no source in the reference; they are restated as a
+// binary binned-SAH BVH with the watertight ray/triangle test of Woop, Benthin and Wald (JCGT
+// 2013), back-face culling per merian's MeshFlags (scene.cpp:1841-1848) and a deterministic tie
+// rule (smallest geometry, then primitive id, at equal t). Also restates the BSDF property checks
+// of tests/bsdf/bsdf-checks.slang and the next-event-estimation estimator that the GPU adds
+// (not in the reference; unbiased against it).
+#include "oracle_math.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <chrono>
+#include <thread>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORACLE_API extern "C" __attribute__((visibility("default")))
+
+namespace oracle {
+
+struct Scene {
+    std::vector<gbpt_packed_vertex> verts;
+    std::vector<uint32_t> idx;
+    std::vector<gbpt_geometry> geoms;
+    std::vector<gbpt_material> mats;
+    std::vector<float> env;
+    uint32_t ew = 0, eh = 0;
+    float env_to_local[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    float env_intensity = 1.0f;
+    // flattened triangles (in the order of `idx`)
+    std::vector<float> tv;        // 9 per triangle
+    std::vector<uint32_t> tgeom;  // geometry of each triangle
+    std::vector<uint32_t> tprim;  // primitive id within the geometry
+    std::vector<uint32_t> geom_tri_base; // first flattened triangle of each geometry
+    // BVH2
+    struct Node {
+        float lo[3], hi[3];
+        uint32_t left_or_first, count; // count > 0: leaf over perm[first, first+count)
+    };
+    std::vector<Node> nodes;
+    std::vector<uint32_t> perm;
+    // emissive triangles for next-event estimation
+    std::vector<uint32_t> light_tri;
+    std::vector<double> light_cdf; // inclusive prefix of power, normalised to 1
+    double light_total = 0.0;
+    // environment importance sampling
+    std::vector<double> env_marg;  // eh + 1, prefix of row sums
+    std::vector<double> env_cond;  // eh * (ew + 1) per-row prefix
+    std::vector<double> env_func;  // eh * ew
+    double env_func_int = 0.0;     // sum / (ew*eh)
+};
+
+// ---- BVH2 build (binned SAH, 16 bins) ---------------------------------------------------------
+static void build_bvh(Scene& s) {
+    const size_t n = s.tgeom.size();
+    s.perm.resize(n);
+    for (size_t i = 0; i < n; ++i) s.perm[i] = (uint32_t)i;
+    std::vector<float> blo(3 * n), bhi(3 * n), cen(3 * n);
+    for (size_t i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            const float x = s.tv[9 * i + a], y = s.tv[9 * i + 3 + a], z = s.tv[9 * i + 6 + a];
+            blo[3 * i + a] = std::min(x, std::min(y, z));
+            bhi[3 * i + a] = std::max(x, std::max(y, z));
+            cen[3 * i + a] = 0.5f * (blo[3 * i + a] + bhi[3 * i + a]);
+        }
+    s.nodes.clear();
+    s.nodes.push_back({});
+    struct T {
+        uint32_t node, b, e;
+    };
+    std::vector<T> st{{0, 0, (uint32_t)n}};
+    auto area = [](const float* lo, const float* hi) {
+        const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        return 2.0f * (dx * dy + dy * dz + dz * dx);
+    };
+    while (!st.empty()) {
+        const T t = st.back();
+        st.pop_back();
+        float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        float clo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, chi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (uint32_t i = t.b; i < t.e; ++i) {
+            const uint32_t p = s.perm[i];
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], blo[3 * p + a]);
+                hi[a] = std::max(hi[a], bhi[3 * p + a]);
+                clo[a] = std::min(clo[a], cen[3 * p + a]);
+                chi[a] = std::max(chi[a], cen[3 * p + a]);
+            }
+        }
+        Scene::Node& nd = s.nodes[t.node];
+        std::memcpy(nd.lo, lo, 12);
+        std::memcpy(nd.hi, hi, 12);
+        const uint32_t cnt = t.e - t.b;
+        nd.left_or_first = t.b;
+        nd.count = cnt;
+        if (cnt <= 2) continue;
+        constexpr int NB = 16;
+        float best = FLT_MAX;
+        int best_axis = -1, best_bin = 0;
+        for (int a = 0; a < 3; ++a) {
+            const float ext = chi[a] - clo[a];
+            if (!(ext > 0.0f)) continue;
+            float bl[NB][3], bh[NB][3];
+            uint32_t bn[NB] = {};
+            for (int b = 0; b < NB; ++b)
+                for (int k = 0; k < 3; ++k) bl[b][k] = FLT_MAX, bh[b][k] = -FLT_MAX;
+            for (uint32_t i = t.b; i < t.e; ++i) {
+                const uint32_t p = s.perm[i];
+                int b = (int)((cen[3 * p + a] - clo[a]) / ext * NB);
+                b = std::min(std::max(b, 0), NB - 1);
+                bn[b]++;
+                for (int k = 0; k < 3; ++k) {
+                    bl[b][k] = std::min(bl[b][k], blo[3 * p + k]);
+                    bh[b][k] = std::max(bh[b][k], bhi[3 * p + k]);
+                }
+            }
+            for (int split = 1; split < NB; ++split) {
+                float l0[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, l1[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+                float r0[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, r1[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+                uint32_t nl = 0, nr = 0;
+                for (int b = 0; b < NB; ++b) {
+                    float* x0 = b < split ? l0 : r0;
+                    float* x1 = b < split ? l1 : r1;
+                    (b < split ? nl : nr) += bn[b];
+                    for (int k = 0; k < 3; ++k) {
+                        x0[k] = std::min(x0[k], bl[b][k]);
+                        x1[k] = std::max(x1[k], bh[b][k]);
+                    }
+                }
+                if (nl == 0 || nr == 0) continue;
+                const float c = area(l0, l1) * nl + area(r0, r1) * nr;
+                if (c < best) {
+                    best = c;
+                    best_axis = a;
+                    best_bin = split;
+                }
+            }
+        }
+        uint32_t mid;
+        if (best_axis < 0) {
+            mid = t.b + cnt / 2;
+        } else {
+            const float ext = chi[best_axis] - clo[best_axis];
+            auto it = std::partition(s.perm.begin() + t.b, s.perm.begin() + t.e, [&](uint32_t p) {
+                int b = (int)((cen[3 * p + best_axis] - clo[best_axis]) / ext * NB);
+                b = std::min(std::max(b, 0), NB - 1);
+                return b < best_bin;
+            });
+            mid = (uint32_t)(it - s.perm.begin());
+            if (mid == t.b || mid == t.e) mid = t.b + cnt / 2;
+        }
+        const uint32_t l = (uint32_t)s.nodes.size();
+        s.nodes.push_back({});
+        s.nodes.push_back({});
+        s.nodes[t.node].left_or_first = l;
+        s.nodes[t.node].count = 0;
+        st.push_back({l, t.b, mid});
+        st.push_back({l + 1, mid, t.e});
+    }
+}
+
+// ---- watertight ray/triangle test (Woop, Benthin, Wald 2013) ----------------------------------
+// Front face = counter-clockwise (face normal cross(e01, e02) towards the ray origin): U, V, W
+// and det all positive. FlipFacing swaps the accepted side, TwoSided accepts both (merian
+// MeshFlags, scene.hpp:39-58, mapped to the TLAS instance flags at scene.cpp:1841-1848).
+template <class R> struct RayPre {
+    int kx, ky, kz;
+    R Sx, Sy, Sz;
+    V3<R> o;
+};
+template <class R> inline R comp(V3<R> v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+template <class R> inline RayPre<R> ray_pre(const Ray<R>& r) {
+    RayPre<R> p;
+    const R ax = std::fabs(r.d.x), ay = std::fabs(r.d.y), az = std::fabs(r.d.z);
+    p.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    p.kx = (p.kz + 1) % 3;
+    p.ky = (p.kx + 1) % 3;
+    if (comp(r.d, p.kz) < R(0)) std::swap(p.kx, p.ky);
+    p.Sx = comp(r.d, p.kx) / comp(r.d, p.kz);
+    p.Sy = comp(r.d, p.ky) / comp(r.d, p.kz);
+    p.Sz = R(1) / comp(r.d, p.kz);
+    p.o = r.o;
+    return p;
+}
+struct HitRec {
+    double t;
+    float u, v;
+    uint32_t geom, prim;
+    bool valid;
+};
+// Returns true and the distance / barycentrics when the triangle is hit within [tmin, tmax].
+template <class R>
+inline bool intersect(const RayPre<R>& p, const float* tv, uint32_t flags, R tmin, R tmax, R& t_out,
+                      R& u_out, R& v_out) {
+    const V3<R> A = mk<R>(tv[0], tv[1], tv[2]) - p.o;
+    const V3<R> B = mk<R>(tv[3], tv[4], tv[5]) - p.o;
+    const V3<R> Cc = mk<R>(tv[6], tv[7], tv[8]) - p.o;
+    const R Ax = comp(A, p.kx) - p.Sx * comp(A, p.kz);
+    const R Ay = comp(A, p.ky) - p.Sy * comp(A, p.kz);
+    const R Bx = comp(B, p.kx) - p.Sx * comp(B, p.kz);
+    const R By = comp(B, p.ky) - p.Sy * comp(B, p.kz);
+    const R Cx = comp(Cc, p.kx) - p.Sx * comp(Cc, p.kz);
+    const R Cy = comp(Cc, p.ky) - p.Sy * comp(Cc, p.kz);
+    R U = Cx * By - Cy * Bx;
+    R V = Ax * Cy - Ay * Cx;
+    R W = Bx * Ay - By * Ax;
+    if (U == R(0) || V == R(0) || W == R(0)) {
+        // edge case: recompute the 2D edge functions in double
+        U = (R)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (R)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (R)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < R(0) || V < R(0) || W < R(0)) && (U > R(0) || V > R(0) || W > R(0))) return false;
+    const R det = U + V + W;
+    if (det == R(0)) return false;
+    const bool front = det > R(0);
+    if (!(flags & GBPT_MESH_TWO_SIDED)) {
+        const bool want_front = !(flags & GBPT_MESH_FLIP_FACING);
+        if (front != want_front) return false;
+    }
+    const R Az = p.Sz * comp(A, p.kz);
+    const R Bz = p.Sz * comp(B, p.kz);
+    const R Cz = p.Sz * comp(Cc, p.kz);
+    const R T = U * Az + V * Bz + W * Cz;
+    const R t = T / det;
+    if (!(t >= tmin && t <= tmax)) return false;
+    t_out = t;
+    u_out = V / det;
+    v_out = W / det;
+    return true;
+}
+
+template <class R>
+static HitRec trace(const Scene& s, const Ray<R>& r, uint32_t mask, bool any_hit,
+                    uint64_t* node_count = nullptr, uint64_t* tri_count = nullptr) {
+    HitRec best{};
+    best.valid = false;
+    if (s.nodes.empty() || s.tgeom.empty()) return best;
+    const RayPre<R> pre = ray_pre(r);
+    V3<R> inv;
+    auto safe_inv = [](R d) {
+        const R m = R(1e-20f);
+        return R(1) / (std::fabs(d) > m ? d : std::copysign(m, d));
+    };
+    inv = mk(safe_inv(r.d.x), safe_inv(r.d.y), safe_inv(r.d.z));
+    R tbest = r.tmax;
+    uint64_t key_best = ~0ull;
+    uint32_t stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    const R eps = sizeof(R) == 4 ? R(1.0 / (1 << 20)) : R(0);
+    while (sp > 0) {
+        const uint32_t ni = stack[--sp];
+        const Scene::Node& nd = s.nodes[ni];
+        if (node_count) ++*node_count;
+        // slab test, conservative by a relative epsilon in float mode
+        R t0 = r.tmin, t1 = tbest;
+        bool miss = false;
+        for (int a = 0; a < 3 && !miss; ++a) {
+            const R o = comp(r.o, a), iv = comp(inv, a);
+            R ta = ((R)nd.lo[a] - o) * iv, tb = ((R)nd.hi[a] - o) * iv;
+            if (ta > tb) std::swap(ta, tb);
+            ta -= std::fabs(ta) * eps;
+            tb += std::fabs(tb) * eps;
+            t0 = maxr(t0, ta);
+            t1 = minr(t1, tb);
+            if (t0 > t1) miss = true;
+        }
+        if (miss) continue;
+        if (nd.count > 0) {
+            for (uint32_t k = 0; k < nd.count; ++k) {
+                const uint32_t tri = s.perm[nd.left_or_first + k];
+                const uint32_t g = s.tgeom[tri];
+                const gbpt_geometry& geo = s.geoms[g];
+                if (((geo.instance_mask & 0xFFu) & mask) == 0) continue;
+                if (tri_count) ++*tri_count;
+                R t, u, v;
+                if (!intersect(pre, &s.tv[9 * tri], geo.flags, r.tmin, tbest, t, u, v)) continue;
+                const uint64_t key = ((uint64_t)g << 32) | s.tprim[tri];
+                if (t < tbest || key < key_best) {
+                    tbest = t;
+                    key_best = key;
+                    best.t = (double)t;
+                    best.u = (float)u;
+                    best.v = (float)v;
+                    best.geom = g;
+                    best.prim = s.tprim[tri];
+                    best.valid = true;
+                    if (any_hit) return best;
+                }
+            }
+        } else {
+            // visit the nearer child first
+            const uint32_t l = nd.left_or_first, rr = l + 1;
+            const Scene::Node &a = s.nodes[l], &b = s.nodes[rr];
+            const int ax = pre.kz;
+            const R ca = (R)a.lo[ax] + (R)a.hi[ax], cb = (R)b.lo[ax] + (R)b.hi[ax];
+            const bool a_first = (comp(r.d, ax) >= R(0)) ? (ca <= cb) : (ca > cb);
+            if (sp + 2 > 128) return best; // depth guard (never reached by the SAH build)
+            stack[sp++] = a_first ? rr : l;
+            stack[sp++] = a_first ? l : rr;
+        }
+    }
+    return best;
+}
+
+// ---- shading point (scene.slang:312-469, hit.slang) ---------------------------------------------
+template <class R> struct SP {
+    V3<R> pos;
+    uint32_t enc_face_normal;
+    V3<R> emission;
+    Frame<R> frame;
+    bool has_material;
+    MaterialBSDF<R> bsdf;
+    // for next-event estimation / MIS
+    bool emissive_tri;
+    uint32_t geom, prim;
+};
+
+template <class R> inline V3<R> fetch_pos(const Scene& s, uint32_t vi) {
+    const gbpt_packed_vertex& v = s.verts[vi];
+    return mk<R>(v.position[0], v.position[1], v.position[2]);
+}
+
+// bilinear level-0 sample with repeat addressing of the lat-long map (LatLongMap::eval,
+// environment-map.slang:23-35; world_to_latlong_map, utils/math.slang:243-250)
+template <class R> V3<R> env_eval(const Scene& s, V3<R> dir) {
+    if (s.ew == 0) return mk(R(0), R(0), R(0));
+    const float* M = s.env_to_local;
+    const V3<R> l = mk<R>((R)M[0] * dir.x + (R)M[1] * dir.y + (R)M[2] * dir.z,
+                          (R)M[3] * dir.x + (R)M[4] * dir.y + (R)M[5] * dir.z,
+                          (R)M[6] * dir.x + (R)M[7] * dir.y + (R)M[8] * dir.z);
+    const V3<R> p = normalize(l);
+    const R u = std::atan2(p.x, -p.z) * C<R>::INV_2PI + R(0.5);
+    const R v = std::acos(clampr(p.y, R(-1), R(1))) * C<R>::INV_PI;
+    if (!(u == u) || !(v == v)) return mk(R(0), R(0), R(0));
+    const R x = u * (R)s.ew - R(0.5), y = v * (R)s.eh - R(0.5);
+    const R fx = std::floor(x), fy = std::floor(y);
+    const R a = x - fx, b = y - fy;
+    const long long ix = (long long)fx, iy = (long long)fy;
+    auto wrap = [](long long i, long long n) { return (uint32_t)(((i % n) + n) % n); };
+    const uint32_t x0 = wrap(ix, s.ew), x1 = wrap(ix + 1, s.ew);
+    const uint32_t y0 = wrap(iy, s.eh), y1 = wrap(iy + 1, s.eh);
+    auto tex = [&](uint32_t xx, uint32_t yy) {
+        const float* t = &s.env[4 * ((size_t)yy * s.ew + xx)];
+        return mk<R>(t[0], t[1], t[2]);
+    };
+    const V3<R> top = tex(x0, y0) * (R(1) - a) + tex(x1, y0) * a;
+    const V3<R> bot = tex(x0, y1) * (R(1) - a) + tex(x1, y1) * a;
+    return (top * (R(1) - b) + bot * b) * (R)s.env_intensity;
+}
+
+template <class R> SP<R> env_sp(const Scene& s, const Ray<R>& ray) {
+    SP<R> sp{};
+    sp.pos = ray.o + ray.d * R(1e7f); // ENV_MAP_DISTANCE
+    sp.enc_face_normal = encode_normal((float)-ray.d.x, (float)-ray.d.y, (float)-ray.d.z);
+    sp.emission = env_eval(s, ray.d);
+    sp.frame = frame_from_normal(-ray.d);
+    sp.has_material = false;
+    sp.emissive_tri = false;
+    return sp;
+}
+
+// get_shading_point(ray, hit) with a valid triangle hit; bary are the Hit barycentrics
+template <class R>
+SP<R> surface_sp(const Scene& s, const Ray<R>& ray, uint32_t g, uint32_t prim, R bu, R bv, R ior,
+                 bool with_material) {
+    const gbpt_geometry& geo = s.geoms[g];
+    if (geo.flags & GBPT_MESH_USE_ENV_MAP) return env_sp(s, ray);
+    const uint32_t tri = geo.first_triangle + prim;
+    const uint32_t i0 = geo.first_vertex + s.idx[3 * tri + 0];
+    const uint32_t i1 = geo.first_vertex + s.idx[3 * tri + 1];
+    const uint32_t i2 = geo.first_vertex + s.idx[3 * tri + 2];
+    const gbpt_packed_vertex &v0 = s.verts[i0], &v1 = s.verts[i1], &v2 = s.verts[i2];
+    const R b0 = R(1) - bu - bv, b1 = bu, b2 = bv;
+    const V3<R> p0 = fetch_pos<R>(s, i0), p1 = fetch_pos<R>(s, i1), p2 = fetch_pos<R>(s, i2);
+    const V3<R> pos = (b0 * p0 + b1 * p1) + b2 * p2;
+    const V3<R> e01 = p1 - p0, e02 = p2 - p0;
+    V3<R> fn = normalize(cross(e01, e02));
+    if (geo.flags & GBPT_MESH_FLIP_FACING) fn = -fn;
+    V3<R> vn;
+    if (geo.flags & GBPT_MESH_FLAT_SHADING) {
+        vn = fn;
+    } else {
+        vn = normalize((b0 * decode_normal<R>(v0.encoded_normal) +
+                        b1 * decode_normal<R>(v1.encoded_normal)) +
+                       b2 * decode_normal<R>(v2.encoded_normal));
+    }
+    // tangent: per-vertex, or the UV-derived (Lengyel) fallback
+    Frame<R> frame;
+    const R uv0x = half_to_float(v0.uv & 0xffffu), uv0y = half_to_float(v0.uv >> 16);
+    const R uv1x = half_to_float(v1.uv & 0xffffu), uv1y = half_to_float(v1.uv >> 16);
+    const R uv2x = half_to_float(v2.uv & 0xffffu), uv2y = half_to_float(v2.uv >> 16);
+    if (geo.flags & GBPT_MESH_HAS_TANGENTS) {
+        auto dec_t = [&](uint32_t e, R& w) {
+            w = (e & 1u) ? R(-1) : R(1);
+            return decode_normal<R>(e & ~1u);
+        };
+        R w0, w1, w2;
+        const V3<R> t0 = dec_t(v0.encoded_tangent, w0), t1 = dec_t(v1.encoded_tangent, w1),
+                    t2 = dec_t(v2.encoded_tangent, w2);
+        const V3<R> t = (b0 * t0 + b1 * t1) + b2 * t2;
+        const R tw = (b0 * w0 + b1 * w1) + b2 * w2;
+        frame = frame_from_tangent(vn, normalize(t), signr(tw));
+    } else {
+        const R d1x = uv1x - uv0x, d1y = uv1y - uv0y, d2x = uv2x - uv0x, d2y = uv2y - uv0y;
+        const R det = d1x * d2y - d2x * d1y;
+        if (std::fabs(det) > R(1e-8f)) {
+            const R winding = (geo.flags & GBPT_MESH_FLIP_FACING) ? R(1) : R(-1);
+            const V3<R> tg = (d2y * e01 - d1y * e02) / det;
+            frame = frame_from_tangent(vn, tg, signr(det) * winding);
+        } else {
+            frame = frame_from_normal(vn);
+        }
+    }
+    V3<R> face_sd = fn;
+    bool front = true;
+    if (geo.flags & GBPT_MESH_TWO_SIDED) {
+        front = dot(-ray.d, fn) >= R(0);
+        if (!front) {
+            frame.n = -frame.n;
+            face_sd = -face_sd;
+        }
+    }
+    (void)face_sd;
+    SP<R> sp{};
+    sp.pos = pos;
+    sp.enc_face_normal = encode_normal((float)fn.x, (float)fn.y, (float)fn.z);
+    sp.has_material = with_material;
+    sp.geom = g;
+    sp.prim = prim;
+    const gbpt_material& m = s.mats[geo.material_id];
+    const bool emits =
+        m.model != GBPT_MATERIAL_DIFFUSE &&
+        (m.emission[0] != 0.0f || m.emission[1] != 0.0f || m.emission[2] != 0.0f);
+    sp.emission = (emits && front) ? mk<R>(m.emission[0], m.emission[1], m.emission[2])
+                                   : mk(R(0), R(0), R(0));
+    sp.emissive_tri = emits && front;
+    if (m.model == GBPT_MATERIAL_DIFFUSE) {
+        // DiffuseMaterial re-orthonormalises through apply_normal_map(0,0,1)
+        sp.frame = apply_normal_map(frame, mk(R(0), R(0), R(1)));
+    } else {
+        sp.frame = frame;
+    }
+    if (with_material) sp.bsdf = make_material<R>(m, mk(R(1), R(1), R(1)), ior, front);
+    return sp;
+}
+
+// Hit -> shading point (scene.slang:458-469)
+template <class R>
+SP<R> shading_point(const Scene& s, const Ray<R>& ray, const HitRec& h, R ior, bool with_material,
+                    bool half_bary) {
+    if (!h.valid) return env_sp(s, ray);
+    R bu = (R)h.u, bv = (R)h.v;
+    if (half_bary) { // the GBuffer stores barycentrics as half2 (gbuffer.slang:40-60)
+        bu = (R)half_to_float(float_to_half(h.u));
+        bv = (R)half_to_float(float_to_half(h.v));
+    }
+    return surface_sp(s, ray, h.geom, h.prim, bu, bv, ior, with_material);
+}
+
+// ---- lights for next-event estimation (new in the GB300 build; the reference has none) -------
+template <class R> inline R tri_area(const Scene& s, uint32_t tri) {
+    const V3<R> a = mk<R>(s.tv[9 * tri], s.tv[9 * tri + 1], s.tv[9 * tri + 2]);
+    const V3<R> b = mk<R>(s.tv[9 * tri + 3], s.tv[9 * tri + 4], s.tv[9 * tri + 5]);
+    const V3<R> c = mk<R>(s.tv[9 * tri + 6], s.tv[9 * tri + 7], s.tv[9 * tri + 8]);
+    return R(0.5) * length(cross(b - a, c - a));
+}
+static void build_lights(Scene& s) {
+    s.light_tri.clear();
+    s.light_cdf.clear();
+    double acc = 0.0;
+    for (uint32_t t = 0; t < s.tgeom.size(); ++t) {
+        const gbpt_geometry& g = s.geoms[s.tgeom[t]];
+        const gbpt_material& m = s.mats[g.material_id];
+        if (m.model == GBPT_MATERIAL_DIFFUSE) continue;
+        const double lum = 0.299 * m.emission[0] + 0.587 * m.emission[1] + 0.114 * m.emission[2];
+        if (!(lum > 0.0)) continue;
+        const double p = tri_area<double>(s, t) * lum;
+        if (!(p > 0.0)) continue;
+        acc += p;
+        s.light_tri.push_back(t);
+        s.light_cdf.push_back(acc);
+    }
+    s.light_total = acc;
+    for (double& c : s.light_cdf) c /= acc;
+    // environment: piecewise-constant over texels, luminance x sin(theta) with a floor
+    s.env_func.clear();
+    s.env_marg.clear();
+    s.env_cond.clear();
+    if (s.ew == 0) return;
+    const uint32_t w = s.ew, h = s.eh;
+    s.env_func.resize((size_t)w * h);
+    double mean = 0.0;
+    for (uint32_t y = 0; y < h; ++y) {
+        const double st = std::sin(3.14159265358979323846 * (y + 0.5) / h);
+        for (uint32_t x = 0; x < w; ++x) {
+            const float* t = &s.env[4 * ((size_t)y * w + x)];
+            const double l = std::max(0.0, 0.299 * t[0] + 0.587 * t[1] + 0.114 * t[2]);
+            s.env_func[(size_t)y * w + x] = l * st;
+            mean += l * st;
+        }
+    }
+    mean /= (double)w * h;
+    for (double& f : s.env_func) f += 1e-3 * mean + 1e-30;
+    s.env_cond.resize((size_t)h * (w + 1));
+    s.env_marg.resize(h + 1);
+    s.env_marg[0] = 0.0;
+    for (uint32_t y = 0; y < h; ++y) {
+        double* c = &s.env_cond[(size_t)y * (w + 1)];
+        c[0] = 0.0;
+        for (uint32_t x = 0; x < w; ++x) c[x + 1] = c[x] + s.env_func[(size_t)y * w + x];
+        s.env_marg[y + 1] = s.env_marg[y] + c[w];
+    }
+    s.env_func_int = s.env_marg[h] / ((double)w * h);
+}
+
+} // namespace oracle
+
+// ============================================================================================
+// C ABI of the oracle (ctypes from tests, bench's cpu_baseline)
+// ============================================================================================
+using namespace oracle;
+
+ORACLE_API void* oracle_scene_create(const gbpt_packed_vertex* v, uint64_t nv, const uint32_t* idx,
+                                     uint64_t nt, const gbpt_geometry* g, uint32_t ng,
+                                     const gbpt_material* m, uint32_t nm, const float* env,
+                                     uint32_t ew, uint32_t eh, const float* env_to_local,
+                                     float env_intensity) {
+    Scene* s = new Scene();
+    s->verts.assign(v, v + nv);
+    s->idx.assign(idx, idx + 3 * nt);
+    s->geoms.assign(g, g + ng);
+    s->mats.assign(m, m + nm);
+    if (env && ew && eh) {
+        s->env.assign(env, env + 4 * (size_t)ew * eh);
+        s->ew = ew;
+        s->eh = eh;
+        if (env_to_local) std::memcpy(s->env_to_local, env_to_local, sizeof(float) * 9);
+        s->env_intensity = env_intensity;
+    }
+    for (uint32_t gi = 0; gi < ng; ++gi) {
+        s->geom_tri_base.push_back((uint32_t)s->tgeom.size());
+        for (uint32_t k = 0; k < g[gi].triangle_count; ++k) {
+            const uint32_t tri = g[gi].first_triangle + k;
+            for (int c = 0; c < 3; ++c) {
+                const gbpt_packed_vertex& vv = s->verts[g[gi].first_vertex + s->idx[3 * tri + c]];
+                for (int a = 0; a < 3; ++a) s->tv.push_back(vv.position[a]);
+            }
+            s->tgeom.push_back(gi);
+            s->tprim.push_back(k);
+        }
+    }
+    build_bvh(*s);
+    build_lights(*s);
+    return s;
+}
+
+ORACLE_API void oracle_scene_destroy(void* s) { delete (Scene*)s; }
+
+template <class R>
+static void fill_hit(const HitRec& h, gbpt_hit& o) {
+    if (h.valid) {
+        o.instance_id = 0;
+        o.instance_index = 0;
+        o.primitive_id = h.prim;
+        o.geometry_index = h.geom;
+        o.barycentrics[0] = h.u;
+        o.barycentrics[1] = h.v;
+        o.t = (float)h.t;
+    } else {
+        o.instance_id = o.instance_index = o.primitive_id = o.geometry_index = 0xFFFFFFFFu;
+        o.barycentrics[0] = o.barycentrics[1] = 0.0f;
+        o.t = -1.0f;
+    }
+    o.reserved = 0;
+}
+
+// Primary hits of a pinhole camera (the GBuffer node's trace, gbuffer_rt.slang:18-27); out_t64
+// (optional) receives the distance in the oracle's precision.
+ORACLE_API int oracle_trace_primary(void* sp, const gbpt_camera* cam, uint32_t w, uint32_t h,
+                                    uint32_t mask, int fp64, gbpt_hit* out, double* out_t64) {
+    const Scene& s = *(const Scene*)sp;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < (int64_t)w * h; ++i) {
+        const uint32_t px = (uint32_t)(i % w), py = (uint32_t)(i / w);
+        HitRec hr;
+        if (fp64) {
+            hr = trace<double>(s, camera_ray<double>(*cam, px, py, w, h), mask, false);
+        } else {
+            hr = trace<float>(s, camera_ray<float>(*cam, px, py, w, h), mask, false);
+        }
+        fill_hit<float>(hr, out[i]);
+        if (out_t64) out_t64[i] = hr.valid ? hr.t : -1.0;
+    }
+    return 0;
+}
+
+ORACLE_API int oracle_trace_rays(void* sp, const gbpt_ray* rays, uint32_t n, uint32_t mask,
+                                 int fp64, int any_hit, gbpt_hit* out, uint64_t* nodes_visited,
+                                 uint64_t* tris_tested) {
+    const Scene& s = *(const Scene*)sp;
+    std::atomic<uint64_t> nn{0}, nt{0};
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        uint64_t a = 0, b = 0;
+        HitRec hr;
+        if (fp64) {
+            Ray<double> r{mk<double>(rays[i].origin[0], rays[i].origin[1], rays[i].origin[2]),
+                          mk<double>(rays[i].direction[0], rays[i].direction[1],
+                                     rays[i].direction[2]),
+                          rays[i].tmin, rays[i].tmax};
+            hr = trace<double>(s, r, mask, any_hit != 0, &a, &b);
+        } else {
+            Ray<float> r{mk<float>(rays[i].origin[0], rays[i].origin[1], rays[i].origin[2]),
+                         mk<float>(rays[i].direction[0], rays[i].direction[1],
+                                   rays[i].direction[2]),
+                         rays[i].tmin, rays[i].tmax};
+            hr = trace<float>(s, r, mask, any_hit != 0, &a, &b);
+        }
+        fill_hit<float>(hr, out[i]);
+        nn += a;
+        nt += b;
+    }
+    if (nodes_visited) *nodes_visited = nn;
+    if (tris_tested) *tris_tested = nt;
+    return 0;
+}
+
+// ---- the path tracer ------------------------------------------------------------------------
+namespace oracle {
+
+struct PathCfg {
+    int max_path_length;
+    bool emission_on_primary;
+    uint32_t mask;
+    bool nee;
+    int rr_depth;
+};
+
+struct PathCounters {
+    uint64_t rays = 0;
+};
+
+template <class R> struct LightSample {
+    V3<R> dir;    // towards the light
+    R dist;       // shadow ray length
+    V3<R> le;     // emitted radiance
+    R pdf;        // solid angle, including selection
+    bool valid;
+};
+
+// Selection: environment with probability 1/2 when both kinds exist.
+template <class R> inline R env_select_prob(const Scene& s) {
+    if (s.ew == 0) return R(0);
+    return s.light_tri.empty() ? R(1) : R(0.5);
+}
+
+template <class R> inline R env_pdf(const Scene& s, V3<R> dir) {
+    if (s.ew == 0) return R(0);
+    const float* M = s.env_to_local;
+    const V3<R> l = normalize(mk<R>((R)M[0] * dir.x + (R)M[1] * dir.y + (R)M[2] * dir.z,
+                                    (R)M[3] * dir.x + (R)M[4] * dir.y + (R)M[5] * dir.z,
+                                    (R)M[6] * dir.x + (R)M[7] * dir.y + (R)M[8] * dir.z));
+    const R u = std::atan2(l.x, -l.z) * C<R>::INV_2PI + R(0.5);
+    const R v = std::acos(clampr(l.y, R(-1), R(1))) * C<R>::INV_PI;
+    const R st = std::sin(v * C<R>::PI);
+    if (!(st > R(0))) return R(0);
+    uint32_t x = (uint32_t)std::min<double>(std::max<double>(std::floor(u * s.ew), 0.0), s.ew - 1);
+    uint32_t y = (uint32_t)std::min<double>(std::max<double>(std::floor(v * s.eh), 0.0), s.eh - 1);
+    const R pdf_uv = (R)(s.env_func[(size_t)y * s.ew + x] / s.env_func_int);
+    return pdf_uv / (R(2) * C<R>::PI * C<R>::PI * st);
+}
+
+inline uint32_t global_tri(const Scene& s, uint32_t geom, uint32_t prim) {
+    return s.geom_tri_base[geom] + prim;
+}
+
+// solid-angle pdf of reaching a point of an emissive triangle at squared distance dist2 along
+// direction dir (from the shading point towards the light)
+template <class R> inline R tri_light_pdf(const Scene& s, uint32_t tri_global, R dist2, V3<R> dir) {
+    const gbpt_geometry& g = s.geoms[s.tgeom[tri_global]];
+    const float* tv = &s.tv[9 * tri_global];
+    const V3<R> n = normalize(cross(mk<R>(tv[3] - tv[0], tv[4] - tv[1], tv[5] - tv[2]),
+                                    mk<R>(tv[6] - tv[0], tv[7] - tv[1], tv[8] - tv[2])));
+    const R cos_l = dot(dir, n);
+    const gbpt_material& m = s.mats[g.material_id];
+    const R lum = (R)(0.299 * m.emission[0] + 0.587 * m.emission[1] + 0.114 * m.emission[2]);
+    const R area = tri_area<R>(s, tri_global);
+    const R pmf = area * lum / (R)s.light_total;
+    return (R(1) - env_select_prob<R>(s)) * pmf / area * dist2 / std::fabs(cos_l);
+}
+
+template <class R, class G>
+LightSample<R> sample_light(const Scene& s, V3<R> pos, G& rng) {
+    LightSample<R> ls{};
+    ls.valid = false;
+    const R u0 = rng.next_float(), u1 = rng.next_float(), u2 = rng.next_float();
+    const R pe = env_select_prob<R>(s);
+    if (pe <= R(0) && s.light_tri.empty()) return ls;
+    if (u0 < pe) {
+        // environment: row by the marginal, column by the conditional
+        const double tr = (double)u1 * s.env_marg[s.eh];
+        uint32_t y = (uint32_t)(std::upper_bound(s.env_marg.begin() + 1, s.env_marg.end(), tr) -
+                                (s.env_marg.begin() + 1));
+        y = std::min(y, s.eh - 1);
+        const double* c = &s.env_cond[(size_t)y * (s.ew + 1)];
+        const double tc = (double)u2 * c[s.ew];
+        uint32_t x = (uint32_t)(std::upper_bound(c + 1, c + s.ew + 1, tc) - (c + 1));
+        x = std::min(x, s.ew - 1);
+        const double fy = (tr - s.env_marg[y]) / (s.env_marg[y + 1] - s.env_marg[y]);
+        const double fx = (tc - c[x]) / (c[x + 1] - c[x]);
+        const R u = (R)((x + std::min(std::max(fx, 0.0), 1.0)) / s.ew);
+        const R v = (R)((y + std::min(std::max(fy, 0.0), 1.0)) / s.eh);
+        // latlong_map_to_world (utils/math.slang:254-260), then back to world by to_local^T
+        const R phi = C<R>::PI * (R(2) * u - R(1)), theta = C<R>::PI * v;
+        const R st = std::sin(theta);
+        const V3<R> dl = mk(st * std::sin(phi), std::cos(theta), -st * std::cos(phi));
+        const float* M = s.env_to_local;
+        const V3<R> dw = mk<R>((R)M[0] * dl.x + (R)M[3] * dl.y + (R)M[6] * dl.z,
+                               (R)M[1] * dl.x + (R)M[4] * dl.y + (R)M[7] * dl.z,
+                               (R)M[2] * dl.x + (R)M[5] * dl.y + (R)M[8] * dl.z);
+        ls.dir = normalize(dw);
+        ls.dist = R(1e7f);
+        ls.le = env_eval(s, ls.dir);
+        ls.pdf = pe * env_pdf(s, ls.dir);
+        ls.valid = ls.pdf > R(0);
+        return ls;
+    }
+    // emissive triangle by power, uniform point (sample_triangle, utils/sampling.slang:31-36)
+    const double ut = pe > R(0) ? (double)((u0 - pe) / (R(1) - pe)) : (double)u0;
+    size_t k = (size_t)(std::upper_bound(s.light_cdf.begin(), s.light_cdf.end(), ut) -
+                        s.light_cdf.begin());
+    k = std::min(k, s.light_tri.size() - 1);
+    const uint32_t tri = s.light_tri[k];
+    const R x = std::sqrt(u1);
+    const R b0 = R(1) - x, b1 = x * (R(1) - u2), b2 = x * u2;
+    const V3<R> a = mk<R>(s.tv[9 * tri], s.tv[9 * tri + 1], s.tv[9 * tri + 2]);
+    const V3<R> b = mk<R>(s.tv[9 * tri + 3], s.tv[9 * tri + 4], s.tv[9 * tri + 5]);
+    const V3<R> c = mk<R>(s.tv[9 * tri + 6], s.tv[9 * tri + 7], s.tv[9 * tri + 8]);
+    const V3<R> pl = (b0 * a + b1 * b) + b2 * c;
+    V3<R> n = normalize(cross(b - a, c - a));
+    const gbpt_geometry& g = s.geoms[s.tgeom[tri]];
+    if (g.flags & GBPT_MESH_FLIP_FACING) n = -n;
+    const V3<R> d = pl - pos;
+    const R dist2 = dot(d, d);
+    const R dist = std::sqrt(dist2);
+    ls.dir = d / dist;
+    const R cos_l = -dot(ls.dir, n);
+    if (!(cos_l > R(0)) || !(dist > R(0))) return ls; // back of a one-sided emitter
+    const gbpt_material& m = s.mats[g.material_id];
+    ls.le = mk<R>(m.emission[0], m.emission[1], m.emission[2]);
+    ls.dist = dist * R(1 - 1e-4f);
+    ls.pdf = tri_light_pdf<R>(s, tri, dist2, ls.dir);
+    ls.valid = ls.pdf > R(0);
+    return ls;
+}
+
+// One sample of trace_path (render_pt.slang:24-90); with cfg.nee/rr the GB300 estimator (NEE with
+// power-heuristic MIS, Russian roulette), which has the same expectation.
+template <class R>
+V3<R> trace_path(const Scene& s, const PathCfg& cfg, Ray<R> ray, SP<R> sp, Pcg& rng,
+                 PathCounters& ctr) {
+    R current_ior = R(1);
+    V3<R> throughput = mk(R(1), R(1), R(1));
+    V3<R> radiance = cfg.emission_on_primary ? throughput * sp.emission : mk(R(0), R(0), R(0));
+    const R thr = R(1e-5f); // SCENE_THROUGHPUT_THRESHOLD (scene.slang:24)
+    for (int bounce = 1; bounce < cfg.max_path_length; ++bounce) {
+        if (!sp.has_material ||
+            (throughput.x < thr && throughput.y < thr && throughput.z < thr))
+            break;
+        if (cfg.rr_depth > 0 && bounce >= cfg.rr_depth) {
+            const R q = minr(R(1), maxr(throughput.x, maxr(throughput.y, throughput.z)));
+            if ((R)rng.next_float() >= q) break;
+            throughput = throughput / q;
+        }
+        const Frame<R>& frame = sp.frame;
+        const V3<R> wi_local = frame.to_local(-ray.d);
+        const V3<R> ng = decode_normal<R>(sp.enc_face_normal);
+        if (cfg.nee) {
+            const LightSample<R> ls = sample_light(s, sp.pos, rng);
+            if (ls.valid) {
+                const V3<R> wl_local = frame.to_local(ls.dir);
+                const bool trans = wi_local.z * wl_local.z < R(0);
+                const R wl_ng = dot(ls.dir, ng);
+                const bool geo_ok = ((dot(-ray.d, ng) < R(0)) != (wl_ng < R(0))) == trans;
+                if (geo_ok) {
+                    const V3<R> f = sp.bsdf.eval(wi_local, wl_local);
+                    const R pb = sp.bsdf.pdf(wi_local, wl_local);
+                    if (f.x > R(0) || f.y > R(0) || f.z > R(0)) {
+                        Ray<R> sr;
+                        sr.o = offset_ray_origin(sp.pos, wl_ng < R(0) ? -ng : ng);
+                        sr.d = ls.dir;
+                        sr.tmin = R(0);
+                        sr.tmax = ls.dist;
+                        ctr.rays++;
+                        const HitRec occ = trace<R>(s, sr, cfg.mask, true);
+                        if (!occ.valid) {
+                            const R wmis = pow2(ls.pdf) / (pow2(ls.pdf) + pow2(pb));
+                            radiance = radiance + throughput * f * ls.le * (wmis / ls.pdf);
+                        }
+                    }
+                }
+            }
+        }
+        const Sample<R> bs = sp.bsdf.sample_eval(wi_local, rng);
+        if (!bs.valid) break;
+        const V3<R> wo = frame.to_world(bs.wo);
+        throughput = throughput * bs.weight;
+        const bool transmission = wi_local.z * bs.wo.z < R(0);
+        if (transmission) current_ior = current_ior / sp.bsdf.eta;
+        // make_ray (hit.slang:134-146)
+        const R wo_ng = dot(wo, ng);
+        if (((dot(-ray.d, ng) < R(0)) != (wo_ng < R(0))) != transmission) break;
+        ray.o = offset_ray_origin(sp.pos, wo_ng < R(0) ? -ng : ng);
+        ray.d = wo;
+        ray.tmin = R(0);
+        ray.tmax = R(1e7f);
+        ctr.rays++;
+        const HitRec h = trace<R>(s, ray, cfg.mask, false);
+        sp = shading_point<R>(s, ray, h, current_ior, bounce + 1 < cfg.max_path_length, false);
+        V3<R> e = throughput * sp.emission;
+        if (cfg.nee && (e.x != R(0) || e.y != R(0) || e.z != R(0))) {
+            R pl = R(0);
+            if (!h.valid || (s.geoms[h.geom].flags & GBPT_MESH_USE_ENV_MAP)) {
+                pl = env_select_prob<R>(s) * env_pdf(s, ray.d);
+            } else if (sp.emissive_tri) {
+                const uint32_t tri = global_tri(s, h.geom, h.prim);
+                pl = tri_light_pdf<R>(s, tri, pow2((R)h.t), ray.d);
+            }
+            const R wb = pow2(bs.pdf) / (pow2(bs.pdf) + pow2(pl));
+            e = e * wb;
+        }
+        radiance = radiance + e;
+    }
+    return radiance;
+}
+
+// raygen main (render_pt.slang:92-130) for one pixel: returns the per-frame output (mean rgb,
+// mean luminance^2) and, for the statistical parity tests, the per-sample rgb sum of squares.
+template <class R>
+void render_pixel(const Scene& s, const gbpt_camera& cam, const gbpt_render_params& p,
+                  const PathCfg& cfg, uint32_t px, uint32_t py, double* rgba, double* sq,
+                  PathCounters& ctr) {
+    const Ray<R> primary = camera_ray<R>(cam, px, py, p.width, p.height);
+    ctr.rays++;
+    const HitRec h = trace<R>(s, primary, cfg.mask, false);
+    const SP<R> psp = shading_point<R>(s, primary, h, R(1), true, true);
+    double acc[3] = {0, 0, 0}, sm = 0.0, s2[3] = {0, 0, 0};
+    for (int smp = 0; smp < p.spp; ++smp) {
+        Pcg rng{pcg4d16(px, py, p.frame, (uint32_t)smp)};
+        const V3<R> c = trace_path<R>(s, cfg, primary, psp, rng, ctr);
+        if (!(std::isfinite((double)c.x) && std::isfinite((double)c.y) &&
+              std::isfinite((double)c.z)))
+            continue;
+        acc[0] += (double)c.x;
+        acc[1] += (double)c.y;
+        acc[2] += (double)c.z;
+        s2[0] += (double)c.x * (double)c.x;
+        s2[1] += (double)c.y * (double)c.y;
+        s2[2] += (double)c.z * (double)c.z;
+        const double l = (double)yuv_luminance(c);
+        sm += l * l;
+    }
+    const double inv = p.spp > 0 ? 1.0 / p.spp : 0.0;
+    rgba[0] = acc[0] * inv;
+    rgba[1] = acc[1] * inv;
+    rgba[2] = acc[2] * inv;
+    rgba[3] = sm * inv;
+    if (sq) {
+        sq[0] = s2[0] * inv;
+        sq[1] = s2[1] * inv;
+        sq[2] = s2[2] * inv;
+    }
+}
+
+} // namespace oracle
+
+// Renders the listed pixels (or all) at p->spp. out_rgba: 4 doubles per pixel (mean rgb, mean
+// luminance^2); out_sq (optional): 3 doubles per pixel, mean of the squared per-sample rgb.
+// threads <= 0 uses every host thread. Returns the number of traced rays in *out_rays.
+ORACLE_API int oracle_render(void* sp, const gbpt_camera* cam, const gbpt_render_params* p,
+                             int fp64, int threads, double* out_rgba, double* out_sq,
+                             uint64_t* out_rays) {
+    const Scene& s = *(const Scene*)sp;
+    PathCfg cfg{p->max_path_length, p->emission_on_primary != 0, p->instance_mask & 0xFFu,
+                p->nee != 0, p->rr_depth};
+    const uint32_t n = p->pixel_count ? p->pixel_count : p->width * p->height;
+    std::atomic<uint64_t> rays{0};
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+#pragma omp parallel
+    {
+        PathCounters ctr;
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t i = 0; i < (int64_t)n; ++i) {
+            const uint32_t pix = p->pixel_count ? p->pixels[i] : (uint32_t)i;
+            const uint32_t px = pix % p->width, py = pix / p->width;
+            double* sq = out_sq ? out_sq + 3 * i : nullptr;
+            if (fp64)
+                render_pixel<double>(s, *cam, *p, cfg, px, py, out_rgba + 4 * i, sq, ctr);
+            else
+                render_pixel<float>(s, *cam, *p, cfg, px, py, out_rgba + 4 * i, sq, ctr);
+        }
+        rays += ctr.rays;
+    }
+    if (out_rays) *out_rays = rays;
+    return 0;
+}
+
+ORACLE_API int oracle_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+// ---- BSDF property checks (tests/bsdf/bsdf-checks.slang:30-135) -----------------------------
+// kind: 0 Lambert(albedo), 1 GGX(alpha, alpha_y), 2 Conductor(alpha, f0), 3 RoughDielectric(alpha,
+// eta = 1/1.5, tint = albedo), 4 FresnelMix<GGX, Lambert>(alpha, albedo, ior_f0). out: 16 floats in
+// the reference's slot layout (furnace rgb, furnace stderr rgb, mean_cos, stderr_cos, valid,
+// max_weight_err, max_pdf_err, pdf_integral, max_recip_err, -, -, -).
+ORACLE_API int oracle_bsdf_check(int kind, const float* wi_in, const float* albedo, float alpha,
+                                 float alpha_y, const float* f0, float ior_f0, uint32_t n_samples,
+                                 uint32_t seed, float* out) {
+    using R = float;
+    const V3<R> wi = mk(wi_in[0], wi_in[1], wi_in[2]);
+    const V3<R> alb = mk(albedo[0], albedo[1], albedo[2]);
+    Lambert<R> lam{alb};
+    GGX<R> ggx{alpha, alpha_y};
+    Conductor<R> cond{GGX<R>{alpha, alpha}, mk(f0[0], f0[1], f0[2])};
+    RoughDielectric<R> rd{alpha, 1.0f / 1.5f, alb};
+    OpaqueDielectric<R> fm{GGX<R>{alpha, alpha}, Lambert<R>{alb}, ior_f0};
+    auto sample_eval = [&](V3<R> w, XorShift& rng) -> Sample<R> {
+        switch (kind) {
+        case 0: return lam.sample_eval(w, rng);
+        case 1: return ggx.sample_eval(w, rng);
+        case 2: return cond.sample_eval(w, rng);
+        case 3: return rd.sample_eval(w, rng);
+        default: return fm.sample_eval(w, rng);
+        }
+    };
+    auto evalf = [&](V3<R> a, V3<R> b) -> V3<R> {
+        switch (kind) {
+        case 0: return lam.eval(a, b);
+        case 1: return ggx.eval(a, b);
+        case 2: return cond.eval(a, b);
+        case 3: return rd.eval(a, b);
+        default: return fm.eval(a, b);
+        }
+    };
+    auto pdff = [&](V3<R> a, V3<R> b) -> R {
+        switch (kind) {
+        case 0: return lam.pdf(a, b);
+        case 1: return ggx.pdf(a, b);
+        case 2: return cond.pdf(a, b);
+        case 3: return rd.pdf(a, b);
+        default: return fm.pdf(a, b);
+        }
+    };
+    auto acc_err = [](R acc, R v) { return std::isfinite(v) ? std::max(acc, v) : 1e30f; };
+    XorShift rng{seed | 1u};
+    V3<R> mean_w = mk(0.f, 0.f, 0.f), m2_w = mk(0.f, 0.f, 0.f);
+    R mean_cos = 0, m2_cos = 0, max_w_err = 0, max_pdf_err = 0;
+    uint32_t valid = 0;
+    for (uint32_t i = 0; i < n_samples; ++i) {
+        V3<R> w = mk(0.f, 0.f, 0.f);
+        R c = 0;
+        const Sample<R> s = sample_eval(wi, rng);
+        if (s.valid) {
+            valid++;
+            w = s.weight;
+            c = s.wo.z / s.pdf;
+            const R pref = pdff(wi, s.wo);
+            const V3<R> eref = evalf(wi, s.wo);
+            max_pdf_err = acc_err(max_pdf_err, std::fabs(s.pdf - pref) /
+                                                   (std::max(std::fabs(s.pdf), std::fabs(pref)) +
+                                                    1e-6f));
+            if (pref > 0) max_w_err = acc_err(max_w_err, length(s.weight - eref / pref));
+        }
+        const R inv_i = 1.0f / (R)(i + 1);
+        const V3<R> dw = w - mean_w;
+        mean_w = mean_w + dw * inv_i;
+        m2_w = m2_w + dw * (w - mean_w);
+        const R dc = c - mean_cos;
+        mean_cos += dc * inv_i;
+        m2_cos += dc * (c - mean_cos);
+    }
+    const R inv_n = 1.0f / (R)n_samples;
+    const uint32_t NT = 256, NP = 512;
+    const R dth = (C<R>::PI * 0.5f) / (R)NT, dph = C<R>::TWO_PI / (R)NP;
+    R pdf_int = 0, max_recip = 0;
+    for (uint32_t ti = 0; ti < NT; ++ti) {
+        const R th = ((R)ti + 0.5f) * dth;
+        const R ct = std::cos(th), st = std::sin(th);
+        for (uint32_t pi = 0; pi < NP; ++pi) {
+            const R ph = ((R)pi + 0.5f) * dph;
+            const V3<R> wo = mk(st * std::cos(ph), st * std::sin(ph), ct);
+            pdf_int += pdff(wi, wo) * st * dth * dph;
+            const V3<R> fio = evalf(wi, wo) / wo.z;
+            const V3<R> foi = evalf(wo, wi) / wi.z;
+            const R d[3] = {std::fabs(fio.x - foi.x), std::fabs(fio.y - foi.y),
+                            std::fabs(fio.z - foi.z)};
+            const R m[3] = {std::max(std::fabs(fio.x), std::fabs(foi.x)) + 1e-6f,
+                            std::max(std::fabs(fio.y), std::fabs(foi.y)) + 1e-6f,
+                            std::max(std::fabs(fio.z), std::fabs(foi.z)) + 1e-6f};
+            max_recip = acc_err(max_recip, std::max(std::max(d[0] / m[0], d[1] / m[1]), d[2] / m[2]));
+        }
+    }
+    out[0] = mean_w.x;
+    out[1] = mean_w.y;
+    out[2] = mean_w.z;
+    out[3] = std::sqrt(m2_w.x) * inv_n;
+    out[4] = std::sqrt(m2_w.y) * inv_n;
+    out[5] = std::sqrt(m2_w.z) * inv_n;
+    out[6] = mean_cos;
+    out[7] = std::sqrt(m2_cos) * inv_n;
+    out[8] = (float)valid;
+    out[9] = max_w_err;
+    out[10] = max_pdf_err;
+    out[11] = pdf_int;
+    out[12] = max_recip;
+    out[13] = out[14] = out[15] = 0.0f;
+    return 0;
+}

@@ -1,0 +1,199 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Tolerances:
+  * primary hits vs the FP32 oracle: identical (geometry, primitive) ids and bit-identical t (the
+    camera ray and the watertight test are computed with the same IEEE operations on both sides);
+  * primary hits vs the FP64 oracle: t within 1e-5 relative; ids may differ only at ties, where
+    the FP64 distance to both candidates agrees within 1e-5 relative;
+  * per-pixel mean radiance vs the FP64 oracle fixture: |z| > 3 on at most 2% of the channels and
+    mean z^2 < 1.5 (z = difference over the combined standard error); relative RMSE reported.
+"""
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from oracle import binding as O
+
+pytestmark = pytest.mark.gpu
+
+
+def golden(name):
+    return np.load(ROOT / "tests" / "golden" / f"{name}.npz")
+
+
+@pytest.fixture(scope="module")
+def cornell(gpu_ctx):
+    from merian_gb300 import scene as S
+    sc = S.cornell()
+    sid = gpu_ctx.upload(sc)
+    yield sc, sid, O.OracleScene(sc), S.workload_camera("cornell-256-16spp")
+    gpu_ctx.destroy_scene(sid)
+
+
+@pytest.fixture(scope="module")
+def soup_small(gpu_ctx):
+    from merian_gb300 import scene as S
+    sc = S.soup(S.BASE_SEED, 200_000, 256, (256, 128))
+    sid = gpu_ctx.upload(sc)
+    cam = S.look_at((0.5, 0.5, -1.2), (0.5, 0.5, 0.5), (0, 1, 0), 45.0, 16 / 9)
+    yield sc, sid, O.OracleScene(sc), cam
+    gpu_ctx.destroy_scene(sid)
+
+
+def _primary_checks(gpu_ctx, sid, osc, cam, w, h):
+    from merian_gb300 import _native as N
+    g = gpu_ctx.trace_primary(sid, cam, w, h)
+    o32, _ = osc.trace_primary(cam, w, h, fp64=False, hit_dtype=N.HIT_DTYPE)
+    # FP32 oracle: exact
+    assert np.array_equal(g["geometry_index"], o32["geometry_index"])
+    assert np.array_equal(g["primitive_id"], o32["primitive_id"])
+    assert np.array_equal(g["t"].view(np.uint32), o32["t"].view(np.uint32))
+    assert np.array_equal(g["barycentrics"].view(np.uint32), o32["barycentrics"].view(np.uint32))
+    # FP64 oracle: t within 1e-5, id mismatches only at ties
+    o64, t64 = osc.trace_primary(cam, w, h, fp64=True, hit_dtype=N.HIT_DTYPE)
+    hit = g["t"] > 0
+    assert np.array_equal(hit, t64 > 0)
+    rel = np.abs(g["t"][hit].astype(np.float64) - t64[hit]) / t64[hit]
+    assert rel.max() < 1e-5
+    diff = hit & ((g["geometry_index"] != o64["geometry_index"]) |
+                  (g["primitive_id"] != o64["primitive_id"]))
+    assert diff.mean() < 1e-3
+    return hit.mean(), diff.sum()
+
+
+def test_primary_hits_cornell(gpu_ctx, cornell):
+    sc, sid, osc, cam = cornell
+    frac, ties = _primary_checks(gpu_ctx, sid, osc, cam, 256, 256)
+    assert frac > 0.9
+
+
+def test_primary_hits_soup(gpu_ctx, soup_small):
+    sc, sid, osc, cam = soup_small
+    _primary_checks(gpu_ctx, sid, osc, cam, 320, 180)
+
+
+def _random_rays(n, seed):
+    from merian_gb300 import _native as N
+    rng = np.random.default_rng(seed)
+    rays = np.zeros(n, N.RAY_DTYPE)
+    rays["origin"] = rng.uniform(-0.1, 1.1, size=(n, 3))
+    d = rng.normal(size=(n, 3))
+    rays["direction"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays["tmin"] = 0.0
+    rays["tmax"] = np.where(rng.uniform(size=n) < 0.2, rng.uniform(0.01, 0.5, size=n), 1e7)
+    return rays
+
+
+@pytest.mark.parametrize("which", ["cornell", "soup_small"])
+def test_incoherent_rays_match_oracle(gpu_ctx, which, request):
+    import torch
+    from merian_gb300 import _native as N
+    sc, sid, osc, cam = request.getfixturevalue(which)
+    rays = _random_rays(200_000, 11)
+    d_rays = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
+    d_hits = torch.zeros(len(rays) * N.HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    gpu_ctx.trace(sid, d_rays.data_ptr(), len(rays), d_hits.data_ptr())
+    gpu_ctx.synchronize()
+    g = d_hits.cpu().numpy().view(N.HIT_DTYPE)
+    o, _, _ = osc.trace_rays(rays, fp64=False, hit_dtype=N.HIT_DTYPE)
+    assert np.array_equal(g["geometry_index"], o["geometry_index"])
+    assert np.array_equal(g["primitive_id"], o["primitive_id"])
+    assert np.array_equal(g["t"].view(np.uint32), o["t"].view(np.uint32))
+    # occlusion queries agree with the existence of a closest hit
+    gpu_ctx.trace(sid, d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=True)
+    gpu_ctx.synchronize()
+    ga = d_hits.cpu().numpy().view(N.HIT_DTYPE)
+    assert np.array_equal(ga["geometry_index"] != 0xFFFFFFFF, o["geometry_index"] != 0xFFFFFFFF)
+
+
+def _stat_compare(gpu_ctx, sid, cam, g, nee, rr, frames=8, spp=4096):
+    """GPU per-pixel means (frames x spp samples, variance across frames) vs the FP64 fixture."""
+    from merian_gb300 import scene as S
+    pixels = g["pixels"]
+    w, h, L = int(g["width"]), int(g["height"]), int(g["max_path_length"])
+    outs = []
+    for f in range(frames):
+        params, keep = S.render_params(w, h, spp, L, pixels=pixels, nee=nee, rr_depth=rr,
+                                       frame=1000 + f)
+        outs.append(gpu_ctx.render(sid, cam, params)[:, :3].astype(np.float64))
+    outs = np.stack(outs)
+    m = outs.mean(0)
+    se_g = outs.std(0, ddof=1) / np.sqrt(frames)
+    gm, gv, gn = g["mean"], g["var"], int(g["spp"])
+    se_o = np.sqrt(gv / gn)
+    se = np.sqrt(se_g ** 2 + se_o ** 2)
+    ok = se > 0
+    z = (m - gm)[ok] / se[ok]
+    rel_rmse = np.sqrt(np.mean((m - gm) ** 2)) / max(np.mean(gm), 1e-12)
+    return z, rel_rmse, m, gm
+
+
+@pytest.mark.parametrize("nee,rr", [(False, 0), (True, 0), (True, 3)],
+                         ids=["bsdf", "nee", "nee_rr"])
+def test_render_cornell_converges_to_oracle(gpu_ctx, cornell, nee, rr):
+    sc, sid, osc, cam = cornell
+    z, rel_rmse, m, gm = _stat_compare(gpu_ctx, sid, cam, golden("cornell"), nee, rr)
+    print(f"cornell nee={nee} rr={rr}: rel RMSE {rel_rmse:.4%}, max|z| {np.abs(z).max():.2f}")
+    assert np.mean(np.abs(z) > 3) < 0.02
+    assert np.mean(z ** 2) < 1.5
+    assert rel_rmse < 0.01
+
+
+@pytest.mark.parametrize("nee,rr", [(False, 0), (True, 3)], ids=["bsdf", "nee_rr"])
+def test_render_soup_converges_to_oracle(gpu_ctx, soup_small, nee, rr):
+    sc, sid, osc, cam = soup_small
+    z, rel_rmse, m, gm = _stat_compare(gpu_ctx, sid, cam, golden("soup_small"), nee, rr,
+                                       frames=8, spp=2048)
+    print(f"soup nee={nee} rr={rr}: rel RMSE {rel_rmse:.4%}, max|z| {np.abs(z).max():.2f}")
+    assert np.mean(np.abs(z) > 3) < 0.02
+    assert np.mean(z ** 2) < 1.5
+    assert rel_rmse < 0.01
+
+
+def test_render_deterministic_and_subset_consistent(gpu_ctx, cornell):
+    from merian_gb300 import scene as S
+    sc, sid, osc, cam = cornell
+    p, _ = S.render_params(256, 256, 16, 5, frame=3)
+    a = gpu_ctx.render(sid, cam, p)
+    b = gpu_ctx.render(sid, cam, p)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    pix = np.arange(0, 65536, 97, dtype=np.uint32)
+    ps, keep = S.render_params(256, 256, 16, 5, frame=3, pixels=pix)
+    c = gpu_ctx.render(sid, cam, ps)
+    assert np.array_equal(c.view(np.uint32), a[pix].view(np.uint32))
+
+
+def test_render_first_bounce_tracks_fp32_oracle(gpu_ctx, cornell):
+    """Same RNG stream and same primary hit: with one bounce (path length 2) the GPU and the FP32
+    oracle agree per pixel to float round-off of the BSDF sampling."""
+    from merian_gb300 import scene as S
+    sc, sid, osc, cam = cornell
+    pix = np.arange(0, 65536, 61, dtype=np.uint32)
+    p, keep = S.render_params(256, 256, 4, 2, pixels=pix, frame=5)
+    g = gpu_ctx.render(sid, cam, p).astype(np.float64)
+    o, _, _ = osc.render(cam, p, fp64=False)
+    close = np.isclose(g[:, :3], o[:, :3], rtol=1e-3, atol=1e-5).all(axis=1)
+    assert close.mean() > 0.97, close.mean()
+
+
+def test_render_stats_and_edge_cases(gpu_ctx, cornell):
+    from merian_gb300 import scene as S
+    from merian_gb300 import _native as N
+    sc, sid, osc, cam = cornell
+    p, _ = S.render_params(64, 48, 8, 5)
+    out, st = gpu_ctx.render(sid, cam, p, stats=True)
+    assert out.shape == (64 * 48, 4) and np.all(np.isfinite(out))
+    assert st.samples == 64 * 48 * 8 and st.rays >= 64 * 48 and st.device_ms > 0
+    # zero samples: output is cleared, no work
+    p0, _ = S.render_params(8, 8, 0, 5)
+    assert np.all(gpu_ctx.render(sid, cam, p0) == 0)
+    # path length 1: emission on primary only
+    p1, _ = S.render_params(256, 256, 2, 1)
+    o1 = gpu_ctx.render(sid, cam, p1)
+    assert set(np.unique(o1[:, 0])) <= {0.0, 15.0}
+    # invalid arguments are rejected, not run
+    with pytest.raises(N.GbptError):
+        gpu_ctx.render(sid + 1000, cam, p)
+    bad, _ = S.render_params(8, 8, 1, 0)
+    with pytest.raises(N.GbptError):
+        gpu_ctx.render(sid, cam, bad)

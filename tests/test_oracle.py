@@ -1,0 +1,158 @@
+"""CPU tests of the oracle itself: the reference's BSDF property checks (tests/test_bsdf.cpp:32-58
+tolerances, 2^18 samples, seed 0x1234567, incidence 0 and 80 degrees), FP32/FP64 agreement, and
+the committed FP64 golden fixtures (re-derived at lower sample counts)."""
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from oracle import binding as O
+
+MC_SIGMA = 6.0
+MC_NUMERIC_FLOOR = 1e-3
+FLOAT_EQ_TOL = 1e-4
+PDF_REL_TOL = 1e-3
+QUADRATURE_TOL = 1e-3
+ALBEDO_REL_TOL = 0.15
+
+
+def wi_from_zenith(deg, az=0.0):
+    t, p = math.radians(deg), math.radians(az)
+    return (math.sin(t) * math.cos(p), math.sin(t) * math.sin(p), math.cos(t))
+
+
+WI_NORMAL = wi_from_zenith(0.0)
+WI_GRAZING = wi_from_zenith(80.0)
+
+
+def expect_sample_pdf_match(r):
+    assert r["valid"] > 0
+    assert abs(r["mean_cos"] - math.pi) <= MC_SIGMA * r["stderr_cos"] + MC_NUMERIC_FLOOR
+
+
+def expect_sample_eval_consistent(r):
+    assert r["max_pdf_err"] < PDF_REL_TOL
+    assert r["max_weight_err"] < FLOAT_EQ_TOL
+
+
+def expect_reciprocal(r):
+    assert r["max_recip_err"] < FLOAT_EQ_TOL
+
+
+def expect_energy_conserving(r):
+    assert np.all(np.isfinite(r["furnace"]))
+    assert np.all(r["furnace"] <= 1.0 + MC_SIGMA * r["furnace_stderr"])
+
+
+def expect_pdf_normalized(r):
+    assert abs(r["pdf_integral"] - 1.0) <= QUADRATURE_TOL
+
+
+@pytest.mark.parametrize("wi", [WI_NORMAL, WI_GRAZING], ids=["normal", "grazing"])
+def test_lambert(wi):
+    r = O.bsdf_check("lambert", wi, albedo=(0.8, 0.5, 0.2))
+    expect_sample_pdf_match(r)
+    expect_sample_eval_consistent(r)
+    expect_reciprocal(r)
+    expect_energy_conserving(r)
+    expect_pdf_normalized(r)
+    assert np.allclose(r["furnace"], [0.8, 0.5, 0.2], atol=MC_SIGMA * r["furnace_stderr"] + 1e-6)
+
+
+@pytest.mark.parametrize("alpha", [0.05, 0.3, 0.8])
+@pytest.mark.parametrize("wi", [WI_NORMAL, WI_GRAZING], ids=["normal", "grazing"])
+def test_ggx(alpha, wi):
+    r = O.bsdf_check("ggx", wi, alpha=alpha)
+    expect_sample_pdf_match(r)
+    expect_sample_eval_consistent(r)
+    expect_reciprocal(r)
+    expect_energy_conserving(r)
+
+
+@pytest.mark.parametrize("ax,ay", [(0.5, 0.05), (0.05, 0.5), (1.0, 0.01), (0.3, 0.1)])
+@pytest.mark.parametrize("zen", [30.0, 80.0])
+def test_ggx_anisotropic(ax, ay, zen):
+    r = O.bsdf_check("ggx", wi_from_zenith(zen, 40.0), alpha=ax, alpha_y=ay)
+    expect_sample_pdf_match(r)
+    expect_sample_eval_consistent(r)
+    expect_reciprocal(r)
+    expect_energy_conserving(r)
+
+
+@pytest.mark.parametrize("alpha", [0.05, 0.3, 0.8])
+@pytest.mark.parametrize("wi", [WI_NORMAL, WI_GRAZING], ids=["normal", "grazing"])
+def test_fresnel_mix(alpha, wi):
+    r = O.bsdf_check("fresnel_mix", wi, alpha=alpha, albedo=(0.7, 0.7, 0.7), ior_f0=0.04)
+    expect_sample_pdf_match(r)
+    expect_sample_eval_consistent(r)
+    expect_reciprocal(r)
+
+
+@pytest.mark.parametrize("alpha", [0.3, 0.5])
+@pytest.mark.parametrize("wi", [WI_NORMAL, WI_GRAZING], ids=["normal", "grazing"])
+def test_rough_dielectric(alpha, wi):
+    r = O.bsdf_check("rough_dielectric", wi, alpha=alpha, albedo=(0.8, 0.5, 0.2))
+    expect_sample_eval_consistent(r)
+
+
+@pytest.mark.parametrize("alpha", [0.05, 0.3, 0.8])
+@pytest.mark.parametrize("wi", [WI_NORMAL, WI_GRAZING], ids=["normal", "grazing"])
+def test_conductor(alpha, wi):
+    r = O.bsdf_check("conductor", wi, alpha=alpha, f0=(0.95, 0.64, 0.54))
+    expect_sample_pdf_match(r)
+    expect_sample_eval_consistent(r)
+    expect_reciprocal(r)
+    expect_energy_conserving(r)
+
+
+@pytest.fixture(scope="module")
+def cornell():
+    from merian_gb300 import scene as S
+    sc = S.cornell()
+    return sc, O.OracleScene(sc), S.workload_camera("cornell-256-16spp")
+
+
+def test_fp32_fp64_primary_agree(cornell):
+    from merian_gb300 import _native as N
+    sc, osc, cam = cornell
+    h32, _ = osc.trace_primary(cam, 256, 256, fp64=False, hit_dtype=N.HIT_DTYPE)
+    h64, t64 = osc.trace_primary(cam, 256, 256, fp64=True, hit_dtype=N.HIT_DTYPE)
+    same = (h32["geometry_index"] == h64["geometry_index"]) & (
+        h32["primitive_id"] == h64["primitive_id"])
+    assert same.mean() > 0.999
+    hit = h32["t"] > 0
+    assert np.array_equal(hit, h64["t"] > 0)
+    assert np.max(np.abs(h32["t"][hit] - t64[hit]) / t64[hit]) < 1e-5
+
+
+def z_scores(m1, se1, m2, se2):
+    se = np.sqrt(se1 ** 2 + se2 ** 2)
+    ok = se > 0
+    return (m1 - m2)[ok] / se[ok], ok
+
+
+def golden(name):
+    return np.load(ROOT / "tests" / "golden" / f"{name}.npz")
+
+
+@pytest.mark.parametrize("nee,rr", [(False, 0), (True, 0), (True, 3)],
+                         ids=["bsdf", "nee", "nee_rr"])
+def test_oracle_consistent_with_golden(cornell, nee, rr):
+    """The committed FP64 fixture is reproduced (within 3 sigma) by the current oracle, with the
+    reference estimator and with the NEE/roulette estimator that shares its expectation."""
+    from merian_gb300 import scene as S
+    sc, osc, cam = cornell
+    g = golden("cornell")
+    pixels = g["pixels"][:256]
+    spp = 1024
+    params, keep = S.render_params(256, 256, spp, int(g["max_path_length"]), pixels=pixels,
+                                   nee=nee, rr_depth=rr, frame=7)
+    rgba, sq, _ = osc.render(cam, params, fp64=True)
+    mean = rgba[:, :3]
+    var = np.maximum(sq - mean ** 2, 0)
+    gm, gv, gn = g["mean"][:256], g["var"][:256], int(g["spp"])
+    z, ok = z_scores(mean, np.sqrt(var / spp), gm, np.sqrt(gv / gn))
+    assert np.mean(np.abs(z) > 3) < 0.02, np.sort(np.abs(z))[-10:]
+    assert np.mean(z ** 2) < 1.5
