@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""Headline benchmark: Msamples/s (and Grays/s) of the GB300 wavefront path tracer on the
+1M-triangle soup, 1920x1080, 64 spp, path length 8, NEE + Russian roulette from depth 3.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbpt|reference]
+
+A step is one frame (1920*1080*64 path samples) rendered through the C ABI. `value` times
+gbpt_render_device with the scene and output resident in HBM; `e2e` times gbpt_render, which
+copies the frame's result to pinned host memory inside the call. Under torchrun every rank renders
+its own frame (frame seed = rank, weak scaling, no collective on the data path); the timing is the
+max over ranks. `--impl reference` times the CPU restatement of merian's `pt` (oracle/, FP32,
+every host thread) on the same workload, since the reference's Vulkan/Slang path cannot run here.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Msamples/s and Grays/s at equal RMSE vs FP64; served p50/p99 latency, 1 GB300"
+WORKLOAD = "soup-1m-1080p-64spp"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbpt", choices=["gbpt", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_ray():
+    """DRAM bytes per closest-hit ray from the committed ncu summary of the traversal kernel."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        m = re.search(r"dram_bytes_per_ray:\s*([0-9.eE+-]+)", f.read_text())
+        if m:
+            return float(m.group(1)), f.name
+    return None, None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.t:
+                self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(scene, camera, w, cpu_seconds: float, kind_label: str = "port"):
+    """FP32 oracle on every host thread, on a bounded pixel sample of the same workload."""
+    from merian_gb300 import scene as S
+    from oracle import binding as O
+    osc = O.OracleScene(scene)
+    rng = np.random.default_rng(0xC0FFEE)
+    n_total = w["width"] * w["height"]
+    probe = np.sort(rng.choice(n_total, 32, replace=False)).astype(np.uint32)
+    p, keep = S.render_params(w["width"], w["height"], w["spp"], w["max_path_length"],
+                              pixels=probe, nee=w["nee"], rr_depth=w["rr_depth"], frame=0)
+    t0 = time.perf_counter()
+    osc.render(camera, p, fp64=False)
+    dt = time.perf_counter() - t0
+    n_px = int(min(n_total, max(32, 32 * cpu_seconds / max(dt, 1e-3))))
+    pix = np.sort(rng.choice(n_total, n_px, replace=False)).astype(np.uint32)
+    p, keep = S.render_params(w["width"], w["height"], w["spp"], w["max_path_length"],
+                              pixels=pix, nee=w["nee"], rr_depth=w["rr_depth"], frame=0)
+    t0 = time.perf_counter()
+    _, _, rays = osc.render(camera, p, fp64=False)
+    dt = time.perf_counter() - t0
+    samples = n_px * w["spp"]
+    threads = O.num_threads()
+    osc.close()
+    return {"value": round(samples / dt / 1e6, 4), "unit": "Msamples/s", "cores": threads,
+            "kind": kind_label,
+            "sample": f"{n_px} random pixels x {w['spp']} spp of the same frame "
+                      f"({samples} samples, {rays} rays, {dt:.1f} s, FP32 oracle, "
+                      f"{threads} threads)",
+            "grays_per_s": round(rays / dt / 1e9, 6)}
+
+
+def build_workload(name):
+    from merian_gb300 import scene as S
+    w = S.WORKLOADS[name]
+    sc = S.workload_scene(name)
+    cam = S.workload_camera(name)
+    return w, sc, cam
+
+
+def run_reference(args):
+    rank, _, world = dist_info()
+    if rank != 0:
+        return
+    from oracle import binding as O
+    from merian_gb300 import scene as S
+    w, sc, cam = build_workload(args.workload)
+    osc = O.OracleScene(sc)
+    n_total = w["width"] * w["height"]
+    rng = np.random.default_rng(7)
+    # size one step as a bounded sample: ~ cpu_seconds / (steps + warmup) of CPU work each
+    probe = np.sort(rng.choice(n_total, 16, replace=False)).astype(np.uint32)
+    p, keep = S.render_params(w["width"], w["height"], w["spp"], w["max_path_length"],
+                              pixels=probe, nee=w["nee"], rr_depth=w["rr_depth"])
+    t0 = time.perf_counter()
+    osc.render(cam, p, fp64=False)
+    per_px = (time.perf_counter() - t0) / 16
+    budget = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    n_px = int(min(n_total, max(16, budget / max(per_px, 1e-6))))
+    times, rays_total = [], 0
+    for i in range(args.warmup + args.steps):
+        pix = np.sort(rng.choice(n_total, n_px, replace=False)).astype(np.uint32)
+        p, keep = S.render_params(w["width"], w["height"], w["spp"], w["max_path_length"],
+                                  pixels=pix, nee=w["nee"], rr_depth=w["rr_depth"], frame=i)
+        t0 = time.perf_counter()
+        _, _, rays = osc.render(cam, p, fp64=False)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+            rays_total += rays
+    samples = n_px * w["spp"]
+    ms = 1e3 * float(np.mean(times))
+    value = samples / (ms / 1e3) / 1e6
+    threads = O.num_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Msamples/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "triangles": sc.triangle_count,
+                   "width": w["width"], "height": w["height"], "spp": w["spp"],
+                   "max_path_length": w["max_path_length"], "nee": w["nee"],
+                   "rr_depth": w["rr_depth"], "step": f"{n_px} random pixels x {w['spp']} spp"},
+        "grays_per_s": round(rays_total / sum(times) / 1e9, 6),
+        "cpu_baseline": {"value": round(value, 4), "unit": "Msamples/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"{n_px} random pixels x {w['spp']} spp per step, FP32 "
+                                   "restatement of merian's pt (the Vulkan reference cannot "
+                                   "run on this box)"},
+        "e2e": {"value": round(value, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gbpt(args):
+    import torch
+    rank, local_rank, world = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local_rank)
+    from merian_gb300 import _native as N
+    from merian_gb300 import scene as S
+
+    w, sc, cam = build_workload(args.workload)
+    stream = torch.cuda.current_stream()
+    ctx = S.Context(local_rank, stream.cuda_stream)
+    sid = ctx.upload(sc)
+    bvh = ctx.scene_stats(sid)
+    W, H = w["width"], w["height"]
+    n_pix = W * H
+    out = torch.empty((n_pix, 4), dtype=torch.float32, device="cuda")
+    host_out = torch.empty((n_pix, 4), dtype=torch.float32, pin_memory=True)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def params(frame):
+        p, _ = S.render_params(W, H, w["spp"], w["max_path_length"], nee=w["nee"],
+                               rr_depth=w["rr_depth"], frame=frame)
+        return p
+
+    frame_base = 1_000_000 * rank
+    for i in range(args.warmup):
+        ctx.render_device(sid, cam, params(frame_base + i), out.data_ptr())
+    torch.cuda.synchronize()
+
+    # untimed instrumented pass: CWBVH nodes / triangles per closest-hit ray of this workload
+    ctx.set_profiling(2)
+    cst = ctx.render_device(sid, cam, params(frame_base + 999), out.data_ptr(), stats=True)
+    nodes_per_ray = cst.nodes_visited / max(cst.trace_rays, 1)
+    tris_per_ray = cst.tris_tested / max(cst.trace_rays, 1)
+    bytes_per_ray = 48.0 + 80.0 * nodes_per_ray + 48.0 * tris_per_ray
+    ctx.set_profiling(1)
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    step_ms, trace_ms, trace_rays, trace_launches, launches, rays = [], 0.0, 0, 0, 0, 0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank if "CUDA_VISIBLE_DEVICES" not in os.environ else 0) as clk:
+        for i in range(args.steps):
+            flush.zero_()                       # L2 flush outside the timed events
+            ev0.record(stream)
+            st = ctx.render_device(sid, cam, params(frame_base + args.warmup + i),
+                                   out.data_ptr(), stats=True)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            step_ms.append(ev0.elapsed_time(ev1))
+            trace_ms += st.trace_ms
+            trace_rays += st.trace_rays
+            trace_launches += st.trace_launches
+            launches += st.kernel_launches
+            rays += st.rays
+    torch.cuda.synchronize()
+    ms = float(np.mean(step_ms))
+
+    # end to end through the public API with a host output buffer (D2H inside the call)
+    ctx.set_profiling(0)
+    e2e_ms = []
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p = params(frame_base + 5000 + i)
+        N.check(ctx.lib.gbpt_render(ctx.handle, sid, N.C.byref(cam), N.C.byref(p),
+                                    host_out.data_ptr(), None))
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e = float(np.mean(e2e_ms))
+
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms, e2e], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, e2e = float(t[0]), float(t[1])
+        dist.barrier()
+
+    samples_per_step = n_pix * w["spp"]
+    value = world * samples_per_step / (ms / 1e3) / 1e6
+    e2e_value = world * samples_per_step / (e2e / 1e3) / 1e6
+    peak, peak_kind = measured_peaks()
+    achieved = (trace_rays * bytes_per_ray) / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else None
+    tpr, tsrc = ncu_traffic_per_ray()
+    traffic = None
+    if tpr is not None and trace_launches:
+        traffic = tpr * trace_rays / trace_launches
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator, same shapes and distributions as the config)",
+            "config": {"workload": args.workload, "triangles": sc.triangle_count,
+                       "width": W, "height": H, "spp": w["spp"],
+                       "max_path_length": w["max_path_length"], "nee": w["nee"],
+                       "rr_depth": w["rr_depth"], "env": "2048x1024 RGBA32F, 8 Gaussian lobes",
+                       "bvh_nodes": bvh["nodes"], "bvh_depth": bvh["depth"],
+                       "l2": "flushed between timed steps (256 MiB write)",
+                       "parallelism": f"{world} replica(s): one frame per rank, frame seed = rank"},
+            "grays_per_s": round(world * rays / args.steps / (ms / 1e3) / 1e9, 4),
+            "rays_per_sample": round(rays / args.steps / samples_per_step, 4),
+            "clocks": clk.summary(),
+            "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s",
+                    "h2d_bytes_per_step": N.C.sizeof(N.Camera) + N.C.sizeof(N.RenderParams),
+                    "d2h_bytes_per_step": n_pix * 16},
+            "gpu_launches": int(launches),
+            "roofline": {"kernel": "k_trace (CWBVH closest-hit traversal, bounce loop)",
+                         "bound": "hbm", "achieved": None if achieved is None else round(achieved, 1),
+                         "peak": peak, "unit": "GB/s",
+                         "frac": None if achieved is None else round(achieved / peak, 4),
+                         "peak_kind": f"{peak_kind} HBM copy bandwidth",
+                         "traffic": None if traffic is None else round(traffic),
+                         "traffic_source": tsrc,
+                         "bytes_per_ray": round(bytes_per_ray, 1),
+                         "nodes_per_ray": round(nodes_per_ray, 3),
+                         "tris_per_ray": round(tris_per_ray, 3),
+                         "launches_per_step": trace_launches // max(args.steps, 1),
+                         "trace_share_of_step": round(trace_ms / args.steps / ms, 4)},
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(sc, cam, w, args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gbpt(args)
+
+
+if __name__ == "__main__":
+    main()

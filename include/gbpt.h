@@ -176,6 +176,15 @@ typedef struct gbpt_render_stats {
     uint64_t shadow_rays;
     uint64_t kernel_launches;
     double device_ms;      /* device time of the call, CUDA events on the context stream */
+    /* filled when profiling is enabled (gbpt_set_profiling) */
+    double trace_ms;       /* closest-hit traversal launches of the bounce loop */
+    double shade_ms;       /* shading / scatter launches */
+    double shadow_ms;      /* NEE occlusion launches */
+    double other_ms;       /* primary hits and finalisation */
+    uint64_t trace_launches;
+    uint64_t trace_rays;   /* rays through the closest-hit traversal launches */
+    uint64_t nodes_visited; /* level 2: CWBVH nodes visited by those rays */
+    uint64_t tris_tested;   /* level 2: triangles tested by those rays */
 } gbpt_render_stats;
 
 /* Closest hit of one ray, merian Hit (hit.slang:25-65) plus the distance. Misses have
@@ -209,6 +218,11 @@ GBPT_API int gbpt_destroy(gbpt_ctx* ctx);
 GBPT_API int gbpt_synchronize(gbpt_ctx* ctx);
 GBPT_API int gbpt_memory_info(gbpt_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes,
                               uint64_t* ctx_bytes);
+/* Kernel profiling of later render calls with stats: 0 off, 1 per-kernel-class device times (CUDA
+ * events around each launch), 2 also counts CWBVH nodes and triangles visited (instrumented
+ * traversal; slower, for the bytes-per-ray roofline only). Replaces merian's Profiler scopes
+ * (include/merian/vk/utils/profiler.hpp). */
+GBPT_API int gbpt_set_profiling(gbpt_ctx* ctx, int level);
 
 /* ---- scenes -------------------------------------------------------------------------------
  * Replaces merian's Scene upload + driver BLAS/TLAS build (scene.cpp:1117-1120,1836-1882): the

@@ -68,7 +68,11 @@ class RenderParams(C.Structure):
 
 class RenderStats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("rays", C.c_uint64), ("shadow_rays", C.c_uint64),
-                ("kernel_launches", C.c_uint64), ("device_ms", C.c_double)]
+                ("kernel_launches", C.c_uint64), ("device_ms", C.c_double),
+                ("trace_ms", C.c_double), ("shade_ms", C.c_double), ("shadow_ms", C.c_double),
+                ("other_ms", C.c_double), ("trace_launches", C.c_uint64),
+                ("trace_rays", C.c_uint64), ("nodes_visited", C.c_uint64),
+                ("tris_tested", C.c_uint64)]
 
 
 class EnvMap(C.Structure):
@@ -100,6 +104,7 @@ EXPORTS = [
     ("gbpt_synchronize", C.c_int, [C.c_void_p]),
     ("gbpt_memory_info", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                    C.POINTER(C.c_uint64)]),
+    ("gbpt_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
     ("gbpt_scene_create", C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(C.c_uint32)]),
     ("gbpt_scene_destroy", C.c_int, [C.c_void_p, C.c_uint32]),
     ("gbpt_scene_stats", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64),

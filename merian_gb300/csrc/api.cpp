@@ -42,6 +42,7 @@ struct gbpt_ctx {
     gbpt_hit* d_hits = nullptr;
     uint64_t hits_cap = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    Profile prof;
 };
 
 namespace {
@@ -162,6 +163,7 @@ GBPT_API int gbpt_destroy(gbpt_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     for (auto& kv : ctx->scenes) free_scene(kv.second);
     work_free(ctx->work);
+    ctx->prof.destroy();
     if (ctx->d_misc) cudaFree(ctx->d_misc);
     if (ctx->d_hits) cudaFree(ctx->d_hits);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -192,6 +194,18 @@ GBPT_API int gbpt_memory_info(gbpt_ctx* ctx, uint64_t* free_bytes, uint64_t* tot
         for (auto& kv : ctx->scenes) b += kv.second.bytes;
         *ctx_bytes = b;
     }
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_set_profiling(gbpt_ctx* ctx, int level) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (level < 0 || level > 2) {
+        set_error("gbpt_set_profiling: level must be 0, 1 or 2");
+        return GBPT_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->prof.level = level;
     return GBPT_OK;
 }
 
@@ -503,11 +517,14 @@ static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
         GBPT_CUDA_CHECK(cudaMemsetAsync(a.out_device, 0, (size_t)n_pix * sizeof(float4), ctx->stream));
     }
     uint64_t launches = 0;
+    Profile* prof = stats && ctx->prof.level > 0 ? &ctx->prof : nullptr;
     if (stats) {
-        GBPT_CUDA_CHECK(cudaMemsetAsync(w.stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
+        GBPT_CUDA_CHECK(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
+        GBPT_CUDA_CHECK(cudaMemsetAsync(ctx->d_misc, 0, 2 * sizeof(unsigned long long), ctx->stream));
         GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev0, ctx->stream));
+        if (prof) prof->reset();
     }
-    rc = render_frame(it->second, w, a, ctx->stream, &launches);
+    rc = render_frame(it->second, w, a, ctx->stream, &launches, prof, ctx->d_misc);
     if (rc != GBPT_OK) {
         set_error(rc == GBPT_ERR_NO_MEMORY ? "render: work buffer allocation failed"
                                            : "render: kernel launch failed: " +
@@ -523,15 +540,35 @@ static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
         if ((rc = check_device_error(ctx))) return rc;
     }
     if (stats) {
-        unsigned long long st[2] = {0, 0};
+        unsigned long long st[3] = {0, 0, 0}, wk[2] = {0, 0};
         GBPT_CUDA_CHECK(cudaMemcpy(st, w.stats, sizeof(st), cudaMemcpyDeviceToHost));
+        GBPT_CUDA_CHECK(cudaMemcpy(wk, ctx->d_misc, sizeof(wk), cudaMemcpyDeviceToHost));
         float ms = 0.f;
         GBPT_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        std::memset(stats, 0, sizeof(*stats));
         stats->samples = (uint64_t)n_pix * (uint64_t)p->spp;
         stats->rays = st[0];
         stats->shadow_rays = st[1];
+        stats->trace_rays = st[2];
         stats->kernel_launches = launches;
         stats->device_ms = ms;
+        if (prof) {
+            double cls_ms[4] = {0, 0, 0, 0};
+            for (size_t i = 0; i < prof->used; ++i) {
+                float t = 0.f;
+                GBPT_CUDA_CHECK(cudaEventElapsedTime(&t, prof->ev[2 * i], prof->ev[2 * i + 1]));
+                cls_ms[prof->cls[i]] += t;
+                if (prof->cls[i] == 0) stats->trace_launches++;
+            }
+            stats->trace_ms = cls_ms[0];
+            stats->shade_ms = cls_ms[1];
+            stats->shadow_ms = cls_ms[2];
+            stats->other_ms = cls_ms[3];
+            if (prof->level >= 2) {
+                stats->nodes_visited = wk[0];
+                stats->tris_tested = wk[1];
+            }
+        }
     }
     return GBPT_OK;
 }

@@ -483,7 +483,10 @@ __global__ void __launch_bounds__(128) k_trace(DevScene sc, Work w, int qi, uint
         atomicAdd(work_ctr + 0, (unsigned long long)ctr.nodes);
         atomicAdd(work_ctr + 1, (unsigned long long)ctr.tris);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(w.stats + 0, (unsigned long long)n);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(w.stats + 0, (unsigned long long)n);
+        atomicAdd(w.stats + 2, (unsigned long long)n);
+    }
 }
 
 // Emission at the k-th path vertex, then scatter (k < L) into ray queue `qo`.
@@ -726,14 +729,42 @@ int work_reserve(Work& w, uint64_t paths, uint64_t pixels) {
     return GBPT_OK;
 }
 
+int Profile::begin(cudaStream_t st, int c) {
+    if (level <= 0) return -1;
+    if (2 * (used + 1) > ev.size()) {
+        for (int k = 0; k < 2; ++k) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return -1;
+            ev.push_back(e);
+        }
+    }
+    const int pair = (int)used++;
+    cls.push_back(c);
+    cudaEventRecord(ev[2 * pair], st);
+    return pair;
+}
+
+void Profile::end(cudaStream_t st, int pair) {
+    if (pair >= 0) cudaEventRecord(ev[2 * pair + 1], st);
+}
+
+void Profile::destroy() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    ev.clear();
+    reset();
+}
+
 int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStream_t st,
-                 uint64_t* launches) {
+                 uint64_t* launches, Profile* prof, unsigned long long* work_ctr) {
+    Profile dummy;
+    if (!prof) prof = &dummy;
+    const bool count_work = prof->level >= 2 && work_ctr != nullptr;
     const gbpt_render_params& p = args.params;
     const uint32_t S = (uint32_t)p.spp;
     const uint32_t P = args.pixel_count;
     if (S == 0 || P == 0) return GBPT_OK;
-    // wave: whole pixels, as many as fit the path capacity
-    const uint64_t target_paths = std::max<uint64_t>(S, std::min<uint64_t>(w.path_cap, 1ull << 23));
+    // wave: whole pixels, as many as fit the wave size (at least one pixel's samples)
+    const uint64_t target_paths = std::max<uint64_t>(S, kWavePaths);
     const uint32_t pix_per_wave =
         (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(P, target_paths / S));
     int rc = work_reserve(w, (uint64_t)pix_per_wave * S, pix_per_wave);
@@ -759,33 +790,48 @@ int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStr
         a.pix_count = std::min(pix_per_wave, P - base);
         const uint32_t n_paths = a.pix_count * S;
         cudaMemsetAsync(w.counters, 0, 3 * sizeof(uint32_t), st);
+        int ev = prof->begin(st, 3);
         k_primary<<<(a.pix_count + 127) / 128, 128, 0, st>>>(sc, a);
+        prof->end(st, ev);
         const int pgrid = (int)std::min<uint64_t>((n_paths + 127) / 128, (uint64_t)grid);
+        ev = prof->begin(st, 1);
         if (a.nee) k_shade_primary<true><<<pgrid, 128, 0, st>>>(sc, a, n_paths);
         else k_shade_primary<false><<<pgrid, 128, 0, st>>>(sc, a, n_paths);
-        nl += 3;
+        prof->end(st, ev);
+        nl += 2;
         if (a.nee) {
+            ev = prof->begin(st, 2);
             k_shadow<<<grid, 128, 0, st>>>(sc, w, a.mask);
+            prof->end(st, ev);
             cudaMemsetAsync(w.counters + 2, 0, sizeof(uint32_t), st);
             nl += 1;
         }
         int qi = 0;
         for (int k = 2; k <= a.max_len; ++k) {
             const int qo = qi ^ 1;
-            k_trace<false><<<grid, 128, 0, st>>>(sc, w, qi, a.mask, nullptr);
+            ev = prof->begin(st, 0);
+            if (count_work) k_trace<true><<<grid, 128, 0, st>>>(sc, w, qi, a.mask, work_ctr);
+            else k_trace<false><<<grid, 128, 0, st>>>(sc, w, qi, a.mask, nullptr);
+            prof->end(st, ev);
             cudaMemsetAsync(w.counters + qo, 0, sizeof(uint32_t), st);
+            ev = prof->begin(st, 1);
             if (a.nee) k_shade<true><<<grid, 128, 0, st>>>(sc, a, k, qi, qo);
             else k_shade<false><<<grid, 128, 0, st>>>(sc, a, k, qi, qo);
+            prof->end(st, ev);
             nl += 2;
             if (a.nee && k < a.max_len) {
+                ev = prof->begin(st, 2);
                 k_shadow<<<grid, 128, 0, st>>>(sc, w, a.mask);
+                prof->end(st, ev);
                 cudaMemsetAsync(w.counters + 2, 0, sizeof(uint32_t), st);
                 nl += 1;
             }
             qi = qo;
         }
         const uint32_t fin_threads = a.pix_count * 32u;
+        ev = prof->begin(st, 3);
         k_finalize<<<(fin_threads + 127) / 128, 128, 0, st>>>(a, args.out_device, base);
+        prof->end(st, ev);
         nl += 1;
     }
     if (launches) *launches += nl;

@@ -67,6 +67,21 @@ struct Work {
     uint64_t bytes = 0;
 };
 
+// Paths per wave: 8 Mi paths keep ~1.5 GB of path state and queues resident.
+constexpr uint64_t kWavePaths = 1ull << 23;
+
+// Optional per-kernel timing (CUDA events around each launch) and traversal work counters.
+struct Profile {
+    int level = 0; // 0 off, 1 kernel timing, 2 timing + CWBVH nodes / triangles per ray
+    std::vector<cudaEvent_t> ev; // start/end pairs
+    std::vector<int> cls;        // launch class of each pair: 0 trace, 1 shade, 2 shadow, 3 other
+    size_t used = 0;
+    int begin(cudaStream_t st, int c);
+    void end(cudaStream_t st, int pair);
+    void reset() { used = 0; cls.clear(); }
+    void destroy();
+};
+
 struct RenderArgs {
     gbpt_camera camera;
     gbpt_render_params params;
@@ -75,9 +90,9 @@ struct RenderArgs {
     float4* out_device;
 };
 
-// kernels.cu
+// kernels.cu. work_ctr (device, >= 2 counters) receives traversal work when prof->level >= 2.
 int render_frame(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
-                 uint64_t* launches);
+                 uint64_t* launches, Profile* prof, unsigned long long* work_ctr);
 int trace_rays(const SceneGPU& scene, const gbpt_ray* rays, uint32_t n, uint32_t mask, int any_hit,
                gbpt_hit* hits, unsigned long long* counters_device, cudaStream_t stream);
 int trace_primary(const SceneGPU& scene, const gbpt_camera& cam, uint32_t w, uint32_t h,

@@ -132,7 +132,8 @@ WORKLOADS = {
     # the headline: 1M-triangle soup, 1080p, 64 spp, path length 8, NEE + roulette from depth 3
     "soup-1m-1080p-64spp": dict(scene="soup", n_triangles=1_000_000, width=1920, height=1080,
                                 spp=64, max_path_length=8, nee=True, rr_depth=3,
-                                camera=dict(position=(0.5, 0.5, -1.2), target=(0.5, 0.5, 0.5),
+                                # the whole 16:9 frame sees the soup's front face
+                                camera=dict(position=(0.5, 0.5, -0.6), target=(0.5, 0.5, 0.5),
                                             vfov_deg=45.0)),
 }
 
@@ -225,6 +226,9 @@ class Context:
 
     def synchronize(self) -> None:
         N.check(self.lib.gbpt_synchronize(self.handle))
+
+    def set_profiling(self, level: int) -> None:
+        N.check(self.lib.gbpt_set_profiling(self.handle, level))
 
     def memory_info(self) -> dict:
         f, t, c = C.c_uint64(), C.c_uint64(), C.c_uint64()

@@ -124,30 +124,38 @@ def _stat_compare(gpu_ctx, sid, cam, g, nee, rr, frames=8, spp=4096):
     se = np.sqrt(se_g ** 2 + se_o ** 2)
     ok = se > 0
     z = (m - gm)[ok] / se[ok]
-    rel_rmse = np.sqrt(np.mean((m - gm) ** 2)) / max(np.mean(gm), 1e-12)
-    return z, rel_rmse, m, gm
+    scale = max(np.mean(gm), 1e-12)
+    rel_rmse = np.sqrt(np.mean((m - gm) ** 2)) / scale
+    # RMSE an unbiased pair of estimators shows from sampling noise alone
+    noise_rmse = np.sqrt(np.mean(se ** 2)) / scale
+    return z, rel_rmse, noise_rmse
+
+
+def _assert_converged(z, rel_rmse, noise_rmse):
+    # bias check: the RMSE is explained by the two estimators' sampling noise
+    assert np.mean(np.abs(z) > 3) < 0.02
+    assert np.mean(z ** 2) < 1.5
+    assert rel_rmse < 1.25 * noise_rmse + 1e-4
 
 
 @pytest.mark.parametrize("nee,rr", [(False, 0), (True, 0), (True, 3)],
                          ids=["bsdf", "nee", "nee_rr"])
 def test_render_cornell_converges_to_oracle(gpu_ctx, cornell, nee, rr):
     sc, sid, osc, cam = cornell
-    z, rel_rmse, m, gm = _stat_compare(gpu_ctx, sid, cam, golden("cornell"), nee, rr)
-    print(f"cornell nee={nee} rr={rr}: rel RMSE {rel_rmse:.4%}, max|z| {np.abs(z).max():.2f}")
-    assert np.mean(np.abs(z) > 3) < 0.02
-    assert np.mean(z ** 2) < 1.5
-    assert rel_rmse < 0.01
+    z, rel_rmse, noise = _stat_compare(gpu_ctx, sid, cam, golden("cornell"), nee, rr)
+    print(f"cornell nee={nee} rr={rr}: rel RMSE {rel_rmse:.4%} (noise {noise:.4%}), "
+          f"max|z| {np.abs(z).max():.2f}")
+    _assert_converged(z, rel_rmse, noise)
 
 
 @pytest.mark.parametrize("nee,rr", [(False, 0), (True, 3)], ids=["bsdf", "nee_rr"])
 def test_render_soup_converges_to_oracle(gpu_ctx, soup_small, nee, rr):
     sc, sid, osc, cam = soup_small
-    z, rel_rmse, m, gm = _stat_compare(gpu_ctx, sid, cam, golden("soup_small"), nee, rr,
+    z, rel_rmse, noise = _stat_compare(gpu_ctx, sid, cam, golden("soup_small"), nee, rr,
                                        frames=8, spp=2048)
-    print(f"soup nee={nee} rr={rr}: rel RMSE {rel_rmse:.4%}, max|z| {np.abs(z).max():.2f}")
-    assert np.mean(np.abs(z) > 3) < 0.02
-    assert np.mean(z ** 2) < 1.5
-    assert rel_rmse < 0.01
+    print(f"soup nee={nee} rr={rr}: rel RMSE {rel_rmse:.4%} (noise {noise:.4%}), "
+          f"max|z| {np.abs(z).max():.2f}")
+    _assert_converged(z, rel_rmse, noise)
 
 
 def test_render_deterministic_and_subset_consistent(gpu_ctx, cornell):
