@@ -264,6 +264,21 @@ GBPT_API int gbpt_trace_counted(gbpt_ctx* ctx, uint32_t scene, const gbpt_ray* r
                                 gbpt_hit* hits_device, double* nodes_per_ray,
                                 double* tris_per_ray);
 
+/* ---- test hooks (device BSDF code run in isolation) ------------------------------------------
+ * gbpt_debug_material_samples: n samples of a material at one shading point (incident direction
+ * wi in the local shading frame, RNG PCG(pcg4d16(i, seed, 0, 0)) for sample i); 12 floats per
+ * sample: wo.xyz, pdf, weight.rgb, valid, eval(wi, wo).rgb, pdf(wi, wo).
+ * gbpt_debug_bsdf_check: merian's BSDF property checks (tests/bsdf/bsdf-checks.slang:30-135) on
+ * the device BSDFs, one thread: kind 0 Lambert(albedo), 1 GGX(alpha, alpha_y), 2 conductor(alpha,
+ * f0), 3 rough dielectric(alpha, eta, tint = albedo), 4 Fresnel mix GGX/Lambert(alpha, albedo,
+ * ior_f0); 16 floats in the reference's slot layout. */
+GBPT_API int gbpt_debug_material_samples(const gbpt_material* material, int front_facing,
+                                         float ior, const float wi[3], uint32_t seed, uint32_t n,
+                                         float* out_host);
+GBPT_API int gbpt_debug_bsdf_check(int kind, const float wi[3], const float albedo[3],
+                                   float alpha, float alpha_y, const float f0[3], float ior_f0,
+                                   float eta, uint32_t n_samples, uint32_t seed, float* out16);
+
 /* ---- host helpers (no device work) ----------------------------------------------------------
  * Camera basis from look-at parameters (camera.cpp:263-266,349-367); vfov in radians. */
 GBPT_API int gbpt_camera_look_at(const float position[3], const float target[3],

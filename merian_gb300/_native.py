@@ -122,6 +122,12 @@ EXPORTS = [
     ("gbpt_trace_counted", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32,
                                      C.c_int, C.c_void_p, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double)]),
+    ("gbpt_debug_material_samples", C.c_int, [C.c_void_p, C.c_int, C.c_float,
+                                              C.POINTER(C.c_float), C.c_uint32, C.c_uint32,
+                                              C.c_void_p]),
+    ("gbpt_debug_bsdf_check", C.c_int, [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                        C.c_float, C.c_float, C.POINTER(C.c_float), C.c_float,
+                                        C.c_float, C.c_uint32, C.c_uint32, C.c_void_p]),
     ("gbpt_camera_look_at", C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_float),
                                       C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float,
                                       C.c_float, C.POINTER(Camera)]),

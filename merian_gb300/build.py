@@ -20,7 +20,7 @@ INCLUDE = ROOT / "include"
 BUILD = HERE / "_build"
 LIB = HERE / "libgbpt.so"
 
-CUDA_SOURCES = ["kernels.cu"]
+CUDA_SOURCES = ["kernels.cu", "debug_kernels.cu"]
 HOST_SOURCES = ["api.cpp", "bvh.cpp", "scenegen.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

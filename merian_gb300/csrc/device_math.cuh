@@ -512,4 +512,39 @@ template <class G> GBPT_DI BsdfSample material_sample(const Material& m, float3 
 
 GBPT_DI float yuv_luminance(float3 c) { return dot(c, f3(0.299f, 0.587f, 0.114f)); }
 
+// OpenPBRMaterial::get_sample / DiffuseMaterial::get_sample (openpbr-material.slang:220-323,
+// diffuse-material.slang:27-41) from the first four float4 of a gbpt_material record: model and
+// base colour, (metalness, alpha_x, alpha_y, specular_weight), (specular_ior, emission),
+// (transmission_weight, transmission_color). `ior` is the path's current IOR.
+GBPT_DI Material material_from_record(float4 m0, float4 m1, float4 m2, float4 m3, bool front,
+                                      float ior) {
+    Material m;
+    m.model = __float_as_uint(m0.x);
+    m.base = f3(m0.y, m0.z, m0.w);
+    m.eta = 1.0f;
+    m.tw = 0.f;
+    m.tcol = f3(1.f, 1.f, 1.f);
+    if (m.model == 0u) {
+        m.ax = m.ay = 1.f;
+        m.f0 = 0.f;
+        m.metal = 0.f;
+        m.alpha_iso = 1.f;
+        return m;
+    }
+    m.metal = m1.x;
+    m.ax = fmaxf(m1.y, kMinAlpha);
+    m.ay = fmaxf(m1.z, kMinAlpha);
+    const float sior = m2.x;
+    const float ior_t = (sior - 1.0f) / (sior + 1.0f);
+    m.f0 = fminf(fmaxf(m1.w * ior_t * ior_t, 0.0f), 1.0f);
+    const bool transmission = m.model == 2u;
+    if (transmission) {
+        m.eta = ior / (front ? sior : 1.0f);
+        m.tw = m3.x;
+        m.tcol = f3(m3.y, m3.z, m3.w);
+    }
+    m.alpha_iso = transmission ? sqrtf(m.ax * m.ay) : m.ax;
+    return m;
+}
+
 } // namespace gbpt

@@ -179,39 +179,9 @@ GBPT_DI SPd surface_sp(const DevScene& sc, float3 o, float3 d, uint32_t geom, ui
 
 // OpenPBRMaterial::get_sample / DiffuseMaterial::get_sample for this shading point
 GBPT_DI Material load_material(const DevScene& sc, uint32_t mid, bool front, float ior) {
-    const float4 m0 = __ldg(&sc.mats[5 * mid + 0]);
-    const float4 m1 = __ldg(&sc.mats[5 * mid + 1]);
-    Material m;
-    m.model = __float_as_uint(m0.x);
-    m.base = f3(m0.y, m0.z, m0.w);
-    m.eta = 1.0f;
-    if (m.model == GBPT_MATERIAL_DIFFUSE) {
-        m.ax = m.ay = 1.f;
-        m.f0 = 0.f;
-        m.metal = 0.f;
-        m.tw = 0.f;
-        m.alpha_iso = 1.f;
-        m.tcol = f3(1.f, 1.f, 1.f);
-        return m;
-    }
-    const float4 m2 = __ldg(&sc.mats[5 * mid + 2]);
-    const float4 m3 = __ldg(&sc.mats[5 * mid + 3]);
-    m.metal = m1.x;
-    m.ax = fmaxf(m1.y, kMinAlpha);
-    m.ay = fmaxf(m1.z, kMinAlpha);
-    const float sior = m2.x;
-    const float ior_t = (sior - 1.0f) / (sior + 1.0f);
-    m.f0 = fminf(fmaxf(m1.w * ior_t * ior_t, 0.0f), 1.0f);
-    m.tw = 0.f;
-    m.tcol = f3(1.f, 1.f, 1.f);
-    const bool transmission = m.model == GBPT_MATERIAL_OPENPBR_TRANSMISSION;
-    if (transmission) {
-        m.eta = ior / (front ? sior : 1.0f);
-        m.tw = m3.x;
-        m.tcol = f3(m3.y, m3.z, m3.w);
-    }
-    m.alpha_iso = transmission ? sqrtf(m.ax * m.ay) : m.ax;
-    return m;
+    return material_from_record(__ldg(&sc.mats[5 * mid + 0]), __ldg(&sc.mats[5 * mid + 1]),
+                                __ldg(&sc.mats[5 * mid + 2]), __ldg(&sc.mats[5 * mid + 3]), front,
+                                ior);
 }
 
 // ---- lights (next-event estimation; not in the reference, same expectation) ---------------------------

@@ -40,7 +40,8 @@ def load() -> C.CDLL:
         lib.oracle_trace_rays.argtypes = [vp, vp, u32, u32, i32, i32, vp, vp, vp]
         lib.oracle_render.argtypes = [vp, vp, vp, i32, i32, vp, vp, vp]
         lib.oracle_num_threads.restype = i32
-        lib.oracle_bsdf_check.argtypes = [i32, vp, vp, f32, f32, vp, f32, u32, u32, vp]
+        lib.oracle_bsdf_check.argtypes = [i32, vp, vp, f32, f32, vp, f32, f32, u32, u32, vp]
+        lib.oracle_material_samples.argtypes = [vp, i32, f32, vp, u32, u32, vp]
         _lib = lib
     return _lib
 
@@ -112,16 +113,25 @@ BSDF_KINDS = {"lambert": 0, "ggx": 1, "conductor": 2, "rough_dielectric": 3, "fr
 
 def bsdf_check(kind: str, wi, albedo=(0.8, 0.5, 0.2), alpha: float = 0.3,
                alpha_y: float | None = None, f0=(0.95, 0.64, 0.54), ior_f0: float = 0.04,
-               n_samples: int = 1 << 18, seed: int = 0x1234567) -> dict:
+               eta: float = 1.0 / 1.5, n_samples: int = 1 << 18, seed: int = 0x1234567) -> dict:
     """The reference's BSDF property checks (tests/bsdf/bsdf-checks.slang) on the oracle BSDFs."""
     out = np.zeros(16, np.float32)
     wi = np.asarray(wi, np.float32)
     al = np.asarray(albedo, np.float32)
     f0a = np.asarray(f0, np.float32)
     load().oracle_bsdf_check(BSDF_KINDS[kind], _p(wi), _p(al), alpha,
-                             alpha if alpha_y is None else alpha_y, _p(f0a), ior_f0, n_samples,
-                             seed, _p(out))
+                             alpha if alpha_y is None else alpha_y, _p(f0a), ior_f0, eta,
+                             n_samples, seed, _p(out))
     return unpack_check(out, n_samples)
+
+
+def material_samples(material: np.ndarray, front: bool, ior: float, wi, seed: int, n: int):
+    """(n, 12) float32: wo, pdf, weight, valid, eval(wi, wo), pdf(wi, wo) per sample."""
+    out = np.zeros((n, 12), np.float32)
+    m = np.ascontiguousarray(material)
+    w = np.asarray(wi, np.float32)
+    load().oracle_material_samples(_p(m), int(front), ior, _p(w), seed, n, _p(out))
+    return out
 
 
 def unpack_check(out: np.ndarray, n_samples: int) -> dict:

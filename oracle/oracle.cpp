@@ -931,16 +931,44 @@ ORACLE_API int oracle_num_threads(void) {
 // eta = 1/1.5, tint = albedo), 4 FresnelMix<GGX, Lambert>(alpha, albedo, ior_f0). out: 16 floats in
 // the reference's slot layout (furnace rgb, furnace stderr rgb, mean_cos, stderr_cos, valid,
 // max_weight_err, max_pdf_err, pdf_integral, max_recip_err, -, -, -).
+// n samples of a material at one shading point, 12 floats each (wo, pdf, weight, valid, eval,
+// pdf at wo); sample i draws from PCG(pcg4d16(i, seed, 0, 0)), as gbpt_debug_material_samples.
+ORACLE_API int oracle_material_samples(const gbpt_material* m, int front, float ior,
+                                       const float* wi_in, uint32_t seed, uint32_t n, float* out) {
+    using R = float;
+    const MaterialBSDF<R> mb = make_material<R>(*m, mk(1.f, 1.f, 1.f), ior, front != 0);
+    const V3<R> wi = mk(wi_in[0], wi_in[1], wi_in[2]);
+    for (uint32_t i = 0; i < n; ++i) {
+        Pcg rng{pcg4d16(i, seed, 0u, 0u)};
+        const Sample<R> s = mb.sample_eval(wi, rng);
+        float* o = out + 12ull * i;
+        o[0] = s.wo.x;
+        o[1] = s.wo.y;
+        o[2] = s.wo.z;
+        o[3] = s.pdf;
+        o[4] = s.weight.x;
+        o[5] = s.weight.y;
+        o[6] = s.weight.z;
+        o[7] = s.valid ? 1.f : 0.f;
+        const V3<R> e = s.valid ? mb.eval(wi, s.wo) : mk(0.f, 0.f, 0.f);
+        o[8] = e.x;
+        o[9] = e.y;
+        o[10] = e.z;
+        o[11] = s.valid ? mb.pdf(wi, s.wo) : 0.f;
+    }
+    return 0;
+}
+
 ORACLE_API int oracle_bsdf_check(int kind, const float* wi_in, const float* albedo, float alpha,
-                                 float alpha_y, const float* f0, float ior_f0, uint32_t n_samples,
-                                 uint32_t seed, float* out) {
+                                 float alpha_y, const float* f0, float ior_f0, float eta,
+                                 uint32_t n_samples, uint32_t seed, float* out) {
     using R = float;
     const V3<R> wi = mk(wi_in[0], wi_in[1], wi_in[2]);
     const V3<R> alb = mk(albedo[0], albedo[1], albedo[2]);
     Lambert<R> lam{alb};
     GGX<R> ggx{alpha, alpha_y};
     Conductor<R> cond{GGX<R>{alpha, alpha}, mk(f0[0], f0[1], f0[2])};
-    RoughDielectric<R> rd{alpha, 1.0f / 1.5f, alb};
+    RoughDielectric<R> rd{alpha, eta, alb};
     OpaqueDielectric<R> fm{GGX<R>{alpha, alpha}, Lambert<R>{alb}, ior_f0};
     auto sample_eval = [&](V3<R> w, XorShift& rng) -> Sample<R> {
         switch (kind) {
