@@ -278,6 +278,11 @@ GBPT_API int gbpt_debug_material_samples(const gbpt_material* material, int fron
 GBPT_API int gbpt_debug_bsdf_check(int kind, const float wi[3], const float albedo[3],
                                    float alpha, float alpha_y, const float f0[3], float ior_f0,
                                    float eta, uint32_t n_samples, uint32_t seed, float* out16);
+/* The primary shading point of each pixel as the render path caches it: 24 floats per pixel
+ * (position, encoded face normal bits; shading normal, material id bits; tangent, flags bits
+ * (1 = has material, 2 = front facing); bitangent, 0; emission, 0; ray direction, 0). */
+GBPT_API int gbpt_debug_primary_points(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
+                                       const gbpt_render_params* params, float* out_host);
 
 /* ---- host helpers (no device work) ----------------------------------------------------------
  * Camera basis from look-at parameters (camera.cpp:263-266,349-367); vfov in radians. */

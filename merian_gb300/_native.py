@@ -128,6 +128,8 @@ EXPORTS = [
     ("gbpt_debug_bsdf_check", C.c_int, [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                         C.c_float, C.c_float, C.POINTER(C.c_float), C.c_float,
                                         C.c_float, C.c_uint32, C.c_uint32, C.c_void_p]),
+    ("gbpt_debug_primary_points", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Camera),
+                                            C.POINTER(RenderParams), C.c_void_p]),
     ("gbpt_camera_look_at", C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_float),
                                       C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float,
                                       C.c_float, C.POINTER(Camera)]),

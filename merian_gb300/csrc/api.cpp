@@ -593,6 +593,57 @@ GBPT_API int gbpt_render_device(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera
     return render_impl(ctx, scene, camera, params, out_rgba_device, nullptr, stats);
 }
 
+GBPT_API int gbpt_debug_primary_points(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
+                                       const gbpt_render_params* p, float* out_host) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if ((rc = validate_params(camera, p))) return rc;
+    if (!out_host) {
+        set_error("gbpt_debug_primary_points: null output");
+        return GBPT_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) {
+        set_error("gbpt_debug_primary_points: unknown scene id");
+        return GBPT_ERR_NOT_FOUND;
+    }
+    Work& w = ctx->work;
+    const uint32_t n_pix = p->pixel_count ? p->pixel_count : p->width * p->height;
+    RenderArgs a;
+    a.camera = *camera;
+    a.params = *p;
+    a.pixel_count = n_pix;
+    a.pixels_device = nullptr;
+    a.out_device = nullptr;
+    if (p->pixel_count) {
+        if (p->pixel_count > w.pix_id_cap) {
+            if (w.pix_id) cudaFree(w.pix_id);
+            w.pix_id = nullptr;
+            w.pix_id_cap = 0;
+            GBPT_CUDA_CHECK(cudaMalloc((void**)&w.pix_id, (size_t)p->pixel_count * 4));
+            w.pix_id_cap = p->pixel_count;
+        }
+        GBPT_CUDA_CHECK(cudaMemcpyAsync(w.pix_id, p->pixels, (size_t)p->pixel_count * 4,
+                                        cudaMemcpyHostToDevice, ctx->stream));
+        a.pixels_device = w.pix_id;
+    }
+    float* d = nullptr;
+    const size_t bytes = (size_t)n_pix * 24 * sizeof(float);
+    GBPT_CUDA_CHECK(cudaMalloc((void**)&d, bytes));
+    rc = primary_points(it->second, w, a, ctx->stream, d);
+    if (rc == GBPT_OK) {
+        const cudaError_t e = cudaMemcpyAsync(out_host, d, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e != cudaSuccess || cudaStreamSynchronize(ctx->stream) != cudaSuccess) rc = GBPT_ERR_CUDA;
+    }
+    cudaFree(d);
+    if (rc != GBPT_OK) {
+        set_error("gbpt_debug_primary_points failed");
+        return rc;
+    }
+    return check_device_error(ctx);
+}
+
 GBPT_API int gbpt_trace_primary(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
                                 uint32_t width, uint32_t height, uint32_t instance_mask,
                                 gbpt_hit* out_hits_host) {

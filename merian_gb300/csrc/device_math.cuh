@@ -426,7 +426,17 @@ template <class G> GBPT_DI BsdfSample opaque_sample(const Material& m, float3 wi
     return mk_sample(s.wo, p, opaque_eval(m, wi, s.wo) / p);
 }
 
-// MixBSDF<OpaqueDielectric, RoughDielectric>(tw)
+// Power-heuristic weight of density a against density b as 1 / (1 + (b/a)^2): an unbounded a (a
+// near-delta lobe) gives 1 instead of inf/inf.
+GBPT_DI float power_heuristic(float a, float b) {
+    if (!(a > 0.0f)) return 0.0f;
+    const float r = b / a;
+    return 1.0f / (1.0f + r * r);
+}
+
+// MixBSDF<OpaqueDielectric, RoughDielectric>(tw). A mix weight of exactly 0 or 1 passes the
+// sampled lobe through: lerp(x, y, 1) = y and (weight * pdf) / pdf = weight, evaluated exactly
+// (rounded, the round trip turns the unbounded pdf of an index-matched refraction into NaN).
 GBPT_DI float3 dielectric_eval(const Material& m, float3 wi, float3 wo) {
     if (m.tw == 0.0f) return opaque_eval(m, wi, wo);
     if (m.tw == 1.0f) return rough_dielectric_eval(m.alpha_iso, m.eta, m.tcol, wi, wo);
@@ -441,30 +451,16 @@ GBPT_DI float dielectric_pdf(const Material& m, float3 wi, float3 wo) {
 template <class G> GBPT_DI BsdfSample dielectric_sample(const Material& m, float3 wi, G& rng) {
     if (m.tw > 0.0f && rng.next_float() < m.tw) {
         const BsdfSample s = rough_dielectric_sample(m.alpha_iso, m.eta, m.tcol, wi, rng);
-        if (!s.valid) return s;
-        float mp;
-        float3 me;
-        if (m.tw == 1.0f) {
-            mp = s.pdf;
-            me = s.weight * s.pdf;
-        } else {
-            mp = lerpf(opaque_pdf(m, wi, s.wo), s.pdf, m.tw);
-            me = lerp3(opaque_eval(m, wi, s.wo), s.weight * s.pdf, m.tw);
-        }
+        if (!s.valid || m.tw == 1.0f) return s;
+        const float mp = lerpf(opaque_pdf(m, wi, s.wo), s.pdf, m.tw);
+        const float3 me = lerp3(opaque_eval(m, wi, s.wo), s.weight * s.pdf, m.tw);
         return mk_sample(s.wo, mp, me / mp);
     }
     const BsdfSample s = opaque_sample(m, wi, rng);
-    if (!s.valid) return s;
-    float mp;
-    float3 me;
-    if (m.tw == 0.0f) {
-        mp = s.pdf;
-        me = s.weight * s.pdf;
-    } else {
-        mp = lerpf(s.pdf, rough_dielectric_pdf(m.alpha_iso, m.eta, wi, s.wo), m.tw);
-        me = lerp3(s.weight * s.pdf, rough_dielectric_eval(m.alpha_iso, m.eta, m.tcol, wi, s.wo),
-                   m.tw);
-    }
+    if (!s.valid || m.tw == 0.0f) return s;
+    const float mp = lerpf(s.pdf, rough_dielectric_pdf(m.alpha_iso, m.eta, wi, s.wo), m.tw);
+    const float3 me =
+        lerp3(s.weight * s.pdf, rough_dielectric_eval(m.alpha_iso, m.eta, m.tcol, wi, s.wo), m.tw);
     return mk_sample(s.wo, mp, me / mp);
 }
 
@@ -484,29 +480,15 @@ template <class G> GBPT_DI BsdfSample material_sample(const Material& m, float3 
     if (m.model == 0u) return lambert_sample(m.base, wi, rng);
     if (m.metal > 0.0f && rng.next_float() < m.metal) {
         const BsdfSample s = conductor_sample(m.ax, m.ay, m.base, wi, rng);
-        if (!s.valid) return s;
-        float mp;
-        float3 me;
-        if (m.metal == 1.0f) {
-            mp = s.pdf;
-            me = s.weight * s.pdf;
-        } else {
-            mp = lerpf(dielectric_pdf(m, wi, s.wo), s.pdf, m.metal);
-            me = lerp3(dielectric_eval(m, wi, s.wo), s.weight * s.pdf, m.metal);
-        }
+        if (!s.valid || m.metal == 1.0f) return s;
+        const float mp = lerpf(dielectric_pdf(m, wi, s.wo), s.pdf, m.metal);
+        const float3 me = lerp3(dielectric_eval(m, wi, s.wo), s.weight * s.pdf, m.metal);
         return mk_sample(s.wo, mp, me / mp);
     }
     const BsdfSample s = dielectric_sample(m, wi, rng);
-    if (!s.valid) return s;
-    float mp;
-    float3 me;
-    if (m.metal == 0.0f) {
-        mp = s.pdf;
-        me = s.weight * s.pdf;
-    } else {
-        mp = lerpf(s.pdf, ggx_pdf(m.ax, m.ay, wi, s.wo), m.metal);
-        me = lerp3(s.weight * s.pdf, conductor_eval(m.ax, m.ay, m.base, wi, s.wo), m.metal);
-    }
+    if (!s.valid || m.metal == 0.0f) return s;
+    const float mp = lerpf(s.pdf, ggx_pdf(m.ax, m.ay, wi, s.wo), m.metal);
+    const float3 me = lerp3(s.weight * s.pdf, conductor_eval(m.ax, m.ay, m.base, wi, s.wo), m.metal);
     return mk_sample(s.wo, mp, me / mp);
 }
 

@@ -352,7 +352,7 @@ GBPT_DI bool scatter(const DevScene& sc, const FrameArgs& a, int k, const SPd& s
                 const float3 f = material_eval(m, wi_local, wl);
                 if (f.x > 0.f || f.y > 0.f || f.z > 0.f) {
                     const float pb = material_pdf(m, wi_local, wl);
-                    const float wmis = pow2(ls.pdf) / (pow2(ls.pdf) + pow2(pb));
+                    const float wmis = power_heuristic(ls.pdf, pb);
                     const float3 c = thr * f * ls.le * (wmis / ls.pdf);
                     const float3 so = offset_ray_origin(sp.pos, wl_ng < 0.f ? -ng : ng);
                     s_o = make_float4(so.x, so.y, so.z, ls.dist);
@@ -493,7 +493,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene sc, FrameArgs a, int k, 
                 float pl = 0.f;
                 if (sp.env) pl = sc.p_env * env_pdf(sc, d);
                 else if (sp.emissive) pl = tri_light_pdf(sc, sp.emission, h.x * h.x, dot(d, sp.fn));
-                e = e * (pow2(last_pdf) / (pow2(last_pdf) + pow2(pl)));
+                e = e * power_heuristic(last_pdf, pl);
             }
             rad = rad + e;
             if (k < a.max_len)
@@ -808,6 +808,27 @@ int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStr
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return GBPT_ERR_CUDA;
     return GBPT_OK;
+}
+
+int primary_points(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStream_t st,
+                   float* out_device) {
+    const uint32_t P = args.pixel_count;
+    int rc = work_reserve(w, std::max<uint64_t>(P, 1), std::max<uint64_t>(P, 1));
+    if (rc != GBPT_OK) return rc;
+    FrameArgs a{};
+    a.cam = to_cam(args.camera);
+    a.width = args.params.width;
+    a.height = args.params.height;
+    a.mask = args.params.instance_mask & 0xFFu;
+    a.pixels = args.pixels_device;
+    a.pix_base = 0;
+    a.pix_count = P;
+    a.w = w;
+    k_primary<<<(P + 127) / 128, 128, 0, st>>>(make_dev_scene(scene), a);
+    if (cudaMemcpyAsync(out_device, w.pix, (size_t)P * 6 * sizeof(float4), cudaMemcpyDeviceToDevice,
+                        st) != cudaSuccess)
+        return GBPT_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? GBPT_OK : GBPT_ERR_CUDA;
 }
 
 int trace_rays(const SceneGPU& scene, const gbpt_ray* rays, uint32_t n, uint32_t mask, int any_hit,

@@ -93,6 +93,8 @@ struct RenderArgs {
 // kernels.cu. work_ctr (device, >= 2 counters) receives traversal work when prof->level >= 2.
 int render_frame(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
                  uint64_t* launches, Profile* prof, unsigned long long* work_ctr);
+int primary_points(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
+                   float* out_device);
 int trace_rays(const SceneGPU& scene, const gbpt_ray* rays, uint32_t n, uint32_t mask, int any_hit,
                gbpt_hit* hits, unsigned long long* counters_device, cudaStream_t stream);
 int trace_primary(const SceneGPU& scene, const gbpt_camera& cam, uint32_t w, uint32_t h,

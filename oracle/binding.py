@@ -139,3 +139,13 @@ def unpack_check(out: np.ndarray, n_samples: int) -> dict:
                 mean_cos=float(out[6]), stderr_cos=float(out[7]), valid=int(out[8]),
                 max_weight_err=float(out[9]), max_pdf_err=float(out[10]),
                 pdf_integral=float(out[11]), max_recip_err=float(out[12]), n=n_samples)
+
+
+def primary_points(osc: "OracleScene", camera, params) -> np.ndarray:
+    """FP32 primary shading points, 24 floats per pixel (gbpt_debug_primary_points layout)."""
+    n = params.pixel_count or params.width * params.height
+    out = np.zeros((n, 24), np.float32)
+    lib = load()
+    lib.oracle_primary_points.argtypes = [C.c_void_p] * 4
+    lib.oracle_primary_points(osc.h, C.addressof(camera), C.addressof(params), _p(out))
+    return out

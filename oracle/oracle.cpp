@@ -321,6 +321,7 @@ template <class R> struct SP {
     MaterialBSDF<R> bsdf;
     // for next-event estimation / MIS
     bool emissive_tri;
+    bool front;
     uint32_t geom, prim;
 };
 
@@ -365,6 +366,7 @@ template <class R> SP<R> env_sp(const Scene& s, const Ray<R>& ray) {
     sp.frame = frame_from_normal(-ray.d);
     sp.has_material = false;
     sp.emissive_tri = false;
+    sp.front = true;
     return sp;
 }
 
@@ -443,6 +445,7 @@ SP<R> surface_sp(const Scene& s, const Ray<R>& ray, uint32_t g, uint32_t prim, R
     sp.emission = (emits && front) ? mk<R>(m.emission[0], m.emission[1], m.emission[2])
                                    : mk(R(0), R(0), R(0));
     sp.emissive_tri = emits && front;
+    sp.front = front;
     if (m.model == GBPT_MATERIAL_DIFFUSE) {
         // DiffuseMaterial re-orthonormalises through apply_normal_map(0,0,1)
         sp.frame = apply_normal_map(frame, mk(R(0), R(0), R(1)));
@@ -803,7 +806,7 @@ V3<R> trace_path(const Scene& s, const PathCfg& cfg, Ray<R> ray, SP<R> sp, Pcg& 
                         ctr.rays++;
                         const HitRec occ = trace<R>(s, sr, cfg.mask, true);
                         if (!occ.valid) {
-                            const R wmis = pow2(ls.pdf) / (pow2(ls.pdf) + pow2(pb));
+                            const R wmis = power_heuristic(ls.pdf, pb);
                             radiance = radiance + throughput * f * ls.le * (wmis / ls.pdf);
                         }
                     }
@@ -835,8 +838,7 @@ V3<R> trace_path(const Scene& s, const PathCfg& cfg, Ray<R> ray, SP<R> sp, Pcg& 
                 const uint32_t tri = global_tri(s, h.geom, h.prim);
                 pl = tri_light_pdf<R>(s, tri, pow2((R)h.t), ray.d);
             }
-            const R wb = pow2(bs.pdf) / (pow2(bs.pdf) + pow2(pl));
-            e = e * wb;
+            e = e * power_heuristic(bs.pdf, pl);
         }
         radiance = radiance + e;
     }
@@ -915,6 +917,32 @@ ORACLE_API int oracle_render(void* sp, const gbpt_camera* cam, const gbpt_render
         rays += ctr.rays;
     }
     if (out_rays) *out_rays = rays;
+    return 0;
+}
+
+// FP32 primary shading points in the layout of gbpt_debug_primary_points (24 floats per pixel).
+ORACLE_API int oracle_primary_points(void* sp, const gbpt_camera* cam, const gbpt_render_params* p,
+                                     float* out) {
+    const Scene& s = *(const Scene*)sp;
+    const uint32_t n = p->pixel_count ? p->pixel_count : p->width * p->height;
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t pix = p->pixel_count ? p->pixels[i] : i;
+        const Ray<float> r = camera_ray<float>(*cam, pix % p->width, pix / p->width, p->width,
+                                               p->height);
+        const HitRec h = trace<float>(s, r, p->instance_mask & 0xFFu, false);
+        const SP<float> q = shading_point<float>(s, r, h, 1.0f, true, true);
+        float* o = out + 24ull * i;
+        const uint32_t mat = h.valid ? s.geoms[h.geom].material_id : 0u;
+        const uint32_t fl = (q.has_material ? 1u : 0u) |
+                            (q.front ? 2u : 0u);
+        const float v[24] = {q.pos.x, q.pos.y, q.pos.z, as_float(q.enc_face_normal),
+                             q.frame.n.x, q.frame.n.y, q.frame.n.z, as_float(mat),
+                             q.frame.t.x, q.frame.t.y, q.frame.t.z, as_float(fl),
+                             q.frame.b.x, q.frame.b.y, q.frame.b.z, 0.f,
+                             q.emission.x, q.emission.y, q.emission.z, 0.f,
+                             r.d.x, r.d.y, r.d.z, 0.f};
+        std::memcpy(o, v, sizeof(v));
+    }
     return 0;
 }
 

@@ -507,23 +507,34 @@ template <class R> struct OpaqueDielectric {
     }
 };
 
-// MixBSDF (bsdf-mix.slang:7-49); the draw is skipped when weight == 0 (`weight > 0.0f &&`)
+// MixBSDF (bsdf-mix.slang:7-49); the draw is skipped when weight == 0 (`weight > 0.0f &&`).
+// A weight of exactly 0 or 1 is evaluated exactly: lerp(x, y, 1) = y and the sampled lobe's
+// (weight * pdf) / pdf = weight. Rounded, that round trip turns the unbounded pdf of an
+// index-matched refraction (relative IOR 1, denominator wo.h + eta wi.h = 0) into NaN.
 template <class R, class B0, class B1> struct Mix {
     B0 b0;
     B1 b1;
     R w;
-    V3<R> eval(V3<R> wi, V3<R> wo) const { return lerp(b0.eval(wi, wo), b1.eval(wi, wo), w); }
-    R pdf(V3<R> wi, V3<R> wo) const { return lerp(b0.pdf(wi, wo), b1.pdf(wi, wo), w); }
+    V3<R> eval(V3<R> wi, V3<R> wo) const {
+        if (w == R(0)) return b0.eval(wi, wo);
+        if (w == R(1)) return b1.eval(wi, wo);
+        return lerp(b0.eval(wi, wo), b1.eval(wi, wo), w);
+    }
+    R pdf(V3<R> wi, V3<R> wo) const {
+        if (w == R(0)) return b0.pdf(wi, wo);
+        if (w == R(1)) return b1.pdf(wi, wo);
+        return lerp(b0.pdf(wi, wo), b1.pdf(wi, wo), w);
+    }
     template <class G> Sample<R> sample_eval(V3<R> wi, G& rng) const {
         if (w > R(0) && (R)rng.next_float() < w) {
             const Sample<R> s = b1.sample_eval(wi, rng);
-            if (!s.valid) return s;
+            if (!s.valid || w == R(1)) return s;
             const R mp = lerp(b0.pdf(wi, s.wo), s.pdf, w);
             const V3<R> me = lerp(b0.eval(wi, s.wo), s.weight * s.pdf, w);
             return some(s.wo, mp, me / mp);
         }
         const Sample<R> s = b0.sample_eval(wi, rng);
-        if (!s.valid) return s;
+        if (!s.valid || w == R(0)) return s;
         const R mp = lerp(s.pdf, b1.pdf(wi, s.wo), w);
         const V3<R> me = lerp(s.weight * s.pdf, b1.eval(wi, s.wo), w);
         return some(s.wo, mp, me / mp);
@@ -592,6 +603,14 @@ template <class R> inline MaterialBSDF<R> make_material(const gbpt_material& m, 
     mb.substrate.w = (R)m.metalness;
     mb.eta = eta;
     return mb;
+}
+
+// Power-heuristic weight of a strategy with density a against one with density b, written as
+// 1 / (1 + (b/a)^2) so an unbounded a (a near-delta lobe) gives 1 instead of inf/inf.
+template <class R> inline R power_heuristic(R a, R b) {
+    if (!(a > R(0))) return R(0);
+    const R r = b / a;
+    return R(1) / (R(1) + r * r);
 }
 
 // yuv_luminance (colors/colorspace_yuv.slang:5-7)
