@@ -265,6 +265,7 @@ def run_gbpt(args):
         dist.barrier()
     torch.cuda.synchronize()
     step_ms, trace_ms, trace_rays, trace_launches, launches, rays = [], 0.0, 0, 0, 0, 0
+    cls_ms = {"trace": 0.0, "shade": 0.0, "shadow": 0.0, "primary_finalize": 0.0}
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local_rank if "CUDA_VISIBLE_DEVICES" not in os.environ else 0) as clk:
         for i in range(args.steps):
@@ -276,6 +277,10 @@ def run_gbpt(args):
             torch.cuda.synchronize()
             step_ms.append(ev0.elapsed_time(ev1))
             trace_ms += st.trace_ms
+            cls_ms["trace"] += st.trace_ms
+            cls_ms["shade"] += st.shade_ms
+            cls_ms["shadow"] += st.shadow_ms
+            cls_ms["primary_finalize"] += st.other_ms
             trace_rays += st.trace_rays
             trace_launches += st.trace_launches
             launches += st.kernel_launches
@@ -332,6 +337,7 @@ def run_gbpt(args):
                     "h2d_bytes_per_step": N.C.sizeof(N.Camera) + N.C.sizeof(N.RenderParams),
                     "d2h_bytes_per_step": n_pix * 16},
             "gpu_launches": int(launches),
+            "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in cls_ms.items()},
             "roofline": {"kernel": "k_trace (CWBVH closest-hit traversal, bounce loop)",
                          "bound": "hbm", "achieved": None if achieved is None else round(achieved, 1),
                          "peak": peak, "unit": "GB/s",

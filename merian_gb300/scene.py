@@ -135,6 +135,11 @@ WORKLOADS = {
                                 # the whole 16:9 frame sees the soup's front face
                                 camera=dict(position=(0.5, 0.5, -0.6), target=(0.5, 0.5, 0.5),
                                             vfov_deg=45.0)),
+    # the same scene and estimator on a smaller frame: the case the ncu captures run on
+    "soup-1m-360p-16spp": dict(scene="soup", n_triangles=1_000_000, width=640, height=360,
+                               spp=16, max_path_length=8, nee=True, rr_depth=3,
+                               camera=dict(position=(0.5, 0.5, -0.6), target=(0.5, 0.5, 0.5),
+                                           vfov_deg=45.0)),
 }
 
 

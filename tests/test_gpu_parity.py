@@ -6,7 +6,9 @@ Tolerances:
   * primary hits vs the FP64 oracle: t within 1e-5 relative; ids may differ only at ties, where
     the FP64 distance to both candidates agrees within 1e-5 relative;
   * per-pixel mean radiance vs the FP64 oracle fixture: |z| > 3 on at most 2% of the channels and
-    mean z^2 < 1.5 (z = difference over the combined standard error); relative RMSE reported.
+    mean z^2 < 1.5 (z = difference over the combined standard error of both estimators, floored
+    at 1e-5 relative for FP32 round-off); the relative RMSE must be explained by that noise
+    (at most 1.25x the noise RMSE).
 """
 import numpy as np
 import pytest
@@ -121,7 +123,10 @@ def _stat_compare(gpu_ctx, sid, cam, g, nee, rr, frames=8, spp=4096):
     se_g = outs.std(0, ddof=1) / np.sqrt(frames)
     gm, gv, gn = g["mean"], g["var"], int(g["spp"])
     se_o = np.sqrt(gv / gn)
-    se = np.sqrt(se_g ** 2 + se_o ** 2)
+    # FP32 floor: a zero-variance pixel (the environment seen directly) still differs from the
+    # FP64 value by float round-off of the radiance itself
+    se_fp32 = 1e-5 * np.abs(gm)
+    se = np.sqrt(se_g ** 2 + se_o ** 2 + se_fp32 ** 2)
     ok = se > 0
     z = (m - gm)[ok] / se[ok]
     scale = max(np.mean(gm), 1e-12)
@@ -151,8 +156,8 @@ def test_render_cornell_converges_to_oracle(gpu_ctx, cornell, nee, rr):
 @pytest.mark.parametrize("nee,rr", [(False, 0), (True, 3)], ids=["bsdf", "nee_rr"])
 def test_render_soup_converges_to_oracle(gpu_ctx, soup_small, nee, rr):
     sc, sid, osc, cam = soup_small
-    z, rel_rmse, noise = _stat_compare(gpu_ctx, sid, cam, golden("soup_small"), nee, rr,
-                                       frames=8, spp=2048)
+    g = golden("soup_small")
+    z, rel_rmse, noise = _stat_compare(gpu_ctx, sid, cam, g, nee, rr, frames=8, spp=2048)
     print(f"soup nee={nee} rr={rr}: rel RMSE {rel_rmse:.4%} (noise {noise:.4%}), "
           f"max|z| {np.abs(z).max():.2f}")
     _assert_converged(z, rel_rmse, noise)
