@@ -72,7 +72,10 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         obj = BUILD / (src + ".o")
         objs.append(obj)
         if force or _stale(obj, [CSRC / src] + headers):
+            # no FMA contraction on the host: scene generation and BVH quantisation give the
+            # same bits on x86-64 and aarch64
             jobs.append([cxx, "-O3", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall",
+                         "-ffp-contract=off",
                          "-I", str(INCLUDE), "-I", str(CSRC), "-I", str(cuda / "include"),
                          "-c", str(CSRC / src), "-o", str(obj)])
     if jobs:

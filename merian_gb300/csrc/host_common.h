@@ -102,6 +102,62 @@ struct Pcg32 {
     }
 };
 
+// Deterministic double-precision exp / log / sin / cos for the scene generators: range reduction
+// plus truncated Taylor / atanh series using only IEEE +, -, *, / and exact power-of-two scaling,
+// so every host (any libm, any FMA policy; this code is built with -ffp-contract=off) produces
+// the same bits. Accurate to a few 1e-16 relative, which is all the generators need.
+namespace det {
+constexpr double kLn2Hi = 6.93147180369123816490e-01; // ln 2 split so n*kLn2Hi is exact
+constexpr double kLn2Lo = 1.90821492927058770002e-10;
+constexpr double kPi = 3.14159265358979323846;
+inline double exp(double x) {
+    if (x > 700.0) x = 700.0;
+    if (x < -700.0) return 0.0;
+    const double n = std::floor(x / 0.69314718055994530942 + 0.5);
+    const double r = (x - n * kLn2Hi) - n * kLn2Lo; // |r| <= ln2/2
+    double term = 1.0, sum = 1.0;
+    for (int k = 1; k <= 20; ++k) {
+        term = term * r / (double)k;
+        sum = sum + term;
+    }
+    return std::ldexp(sum, (int)n);
+}
+inline double log(double x) { // x > 0
+    int e = 0;
+    double m = std::frexp(x, &e); // x = m 2^e, m in [0.5, 1)
+    if (m < 0.70710678118654752440) {
+        m = m * 2.0;
+        e -= 1;
+    }
+    const double s = (m - 1.0) / (m + 1.0); // |s| < 0.172
+    const double s2 = s * s;
+    double term = s, sum = s;
+    for (int k = 3; k <= 41; k += 2) {
+        term = term * s2;
+        sum = sum + term / (double)k;
+    }
+    return 2.0 * sum + (double)e * kLn2Hi + (double)e * kLn2Lo;
+}
+inline void sincos(double x, double& s, double& c) {
+    // reduce to [-pi/4, pi/4] by quarter turns
+    const double q = std::floor(x / (kPi * 0.5) + 0.5);
+    const double r = x - q * (kPi * 0.5);
+    const double r2 = r * r;
+    double ts = r, ss = r, tc = 1.0, sc = 1.0;
+    for (int k = 1; k <= 12; ++k) {
+        ts = -ts * r2 / (double)((2 * k) * (2 * k + 1));
+        ss = ss + ts;
+        tc = -tc * r2 / (double)((2 * k - 1) * (2 * k));
+        sc = sc + tc;
+    }
+    const long long qi = ((long long)q % 4 + 4) % 4;
+    if (qi == 0) { s = ss; c = sc; }
+    else if (qi == 1) { s = sc; c = -ss; }
+    else if (qi == 2) { s = -ss; c = -sc; }
+    else { s = -sc; c = ss; }
+}
+} // namespace det
+
 void set_error(const std::string& msg);
 
 // ---- CWBVH (compressed 8-wide BVH, Ylitie/Karras/Laine HPG 2017 layout) -------------------

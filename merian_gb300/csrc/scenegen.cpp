@@ -1,7 +1,7 @@
 // Seeded synthetic scenes for the benchmark configurations: a tessellated Cornell box, a
-// triangle soup and a Gaussian-lobe lat-long environment. Integer PCG32 draws, so a seed gives
-// the same scene on every host (the soup's lognormal edge lengths use double-precision libm
-// log/exp/sqrt, the environment uses libm sin/cos/exp).
+// triangle soup and a Gaussian-lobe lat-long environment. Integer PCG32 draws, one per statement,
+// IEEE arithmetic without FMA contraction and the det:: transcendental functions, so a seed gives
+// the same bits on every host (x86-64 and aarch64 alike).
 #include "host_common.h"
 
 #include <cmath>
@@ -180,7 +180,7 @@ extern "C" GBPT_API int gbpt_gen_soup(uint64_t seed, uint32_t n_triangles, uint3
     }
     Pcg32 rng(seed, 0x50u);
     MeshBuilder mb{vertices, indices};
-    const double mu = std::log(0.01), sigma = 0.5;
+    const double mu = det::log(0.01), sigma = 0.5;
     // Marsaglia polar method: two normal deviates per accepted pair
     bool have_spare = false;
     double spare = 0.0;
@@ -195,7 +195,7 @@ extern "C" GBPT_API int gbpt_gen_soup(uint64_t seed, uint32_t n_triangles, uint3
             v = 2.0 * rng.uniform_d() - 1.0;
             s = u * u + v * v;
         } while (s >= 1.0 || s == 0.0);
-        const double f = std::sqrt(-2.0 * std::log(s) / s);
+        const double f = std::sqrt(-2.0 * det::log(s) / s);
         spare = v * f;
         have_spare = true;
         return u * f;
@@ -221,10 +221,15 @@ extern "C" GBPT_API int gbpt_gen_soup(uint64_t seed, uint32_t n_triangles, uint3
         geometries[g].flags = GBPT_MESH_TWO_SIDED | GBPT_MESH_FLAT_SHADING;
         geometries[g].instance_mask = 0xFFu;
         for (uint32_t t = t0; t < t1; ++t) {
-            const V3 c = v3(rng.uniform(), rng.uniform(), rng.uniform());
+            // one draw per statement: function-argument order is unspecified in C++ and differs
+            // between compilers, which would change the scene from host to host
+            const float cx = rng.uniform();
+            const float cy = rng.uniform();
+            const float cz = rng.uniform();
+            const V3 c = v3(cx, cy, cz);
             V3 p[3];
             for (int k = 0; k < 3; ++k) {
-                const float len = (float)std::exp(mu + sigma * normal());
+                const float len = (float)det::exp(mu + sigma * normal());
                 p[k] = c + len * unit_dir();
             }
             mb.triangle(p[0], p[1], p[2]);
@@ -281,14 +286,17 @@ extern "C" GBPT_API int gbpt_gen_env(uint64_t seed, uint32_t width, uint32_t hei
     for (uint32_t y = 0; y < height; ++y) {
         // latlong_map_to_world (merian math.slang:254-260) at the texel centre
         const double theta = pi * ((y + 0.5) / height);
-        const double st = std::sin(theta), ct = std::cos(theta);
+        double st, ct;
+        det::sincos(theta, st, ct);
         for (uint32_t x = 0; x < width; ++x) {
             const double phi = pi * (2.0 * ((x + 0.5) / width) - 1.0);
-            const double d[3] = {st * std::sin(phi), ct, -st * std::cos(phi)};
+            double sp, cp;
+            det::sincos(phi, sp, cp);
+            const double d[3] = {st * sp, ct, -st * cp};
             double rgb[3] = {0, 0, 0};
             for (const Lobe& l : lobes) {
                 const double c = d[0] * l.d[0] + d[1] * l.d[1] + d[2] * l.d[2];
-                const double w = std::exp(l.sharp * (c - 1.0));
+                const double w = det::exp(l.sharp * (c - 1.0));
                 for (int k = 0; k < 3; ++k) rgb[k] += l.amp[k] * w;
             }
             float* t = texels + 4 * ((size_t)y * width + x);

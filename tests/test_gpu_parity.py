@@ -23,10 +23,19 @@ def golden(name):
     return np.load(ROOT / "tests" / "golden" / f"{name}.npz")
 
 
+def _check_scene_hash(sc, name):
+    """The fixture was computed on this exact scene (the generators are host-independent)."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    from make_golden import scene_hash
+    assert scene_hash(sc) == str(golden(name)["scene_hash"]), f"{name}: scene differs from fixture"
+
+
 @pytest.fixture(scope="module")
 def cornell(gpu_ctx):
     from merian_gb300 import scene as S
     sc = S.cornell()
+    _check_scene_hash(sc, "cornell")
     sid = gpu_ctx.upload(sc)
     yield sc, sid, O.OracleScene(sc), S.workload_camera("cornell-256-16spp")
     gpu_ctx.destroy_scene(sid)
@@ -36,6 +45,7 @@ def cornell(gpu_ctx):
 def soup_small(gpu_ctx):
     from merian_gb300 import scene as S
     sc = S.soup(S.BASE_SEED, 200_000, 256, (256, 128))
+    _check_scene_hash(sc, "soup_small")
     sid = gpu_ctx.upload(sc)
     cam = S.look_at((0.5, 0.5, -1.2), (0.5, 0.5, 0.5), (0, 1, 0), 45.0, 16 / 9)
     yield sc, sid, O.OracleScene(sc), cam
