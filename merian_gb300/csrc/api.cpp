@@ -277,7 +277,9 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
         }
     }
     CwBvh bvh;
-    if (!build_cwbvh(bi, bvh, 48)) return GBPT_ERR_INVALID;
+    // each tree level puts at most one node group and one postponed triangle group on the
+    // 48-entry traversal stack
+    if (!build_cwbvh(bi, bvh, 24)) return GBPT_ERR_INVALID;
 
     SceneGPU s;
     std::lock_guard<std::mutex> lk(ctx->mu);

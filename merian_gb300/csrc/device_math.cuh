@@ -47,6 +47,8 @@ constexpr float kThroughputMin = 1e-5f;     // scene.slang:24
 constexpr float kRayTmax = 1e7f;            // hit.slang:8
 constexpr float kEnvDistance = 1e7f;        // environment-map.slang:12
 constexpr float kMinAlpha = 0.0316f * 0.0316f; // material.slang:23 (roughness^2)
+// pdf of a delta lobe; a mix passes such a sample through (w f1 / (w p1) = its own weight)
+constexpr float kInf = __builtin_huge_valf();
 
 // ---- RNG --------------------------------------------------------------------------------------
 // pcg4d16 (utils/hash.slang:138-147)
@@ -321,6 +323,10 @@ GBPT_DI float3 conductor_eval(float ax, float ay, float3 f0, float3 wi, float3 w
     return schlick3(f0, dot(wi, h)) * ggx_eval(ax, ay, wi, wo);
 }
 
+// Index-matched boundary: |eta - 1| < 1e-3 (the IOR bookkeeping yields 0.99999994 as often as 1).
+// Its transmission is a delta lobe: sampling reports pdf = inf, evaluation sees no lobe.
+GBPT_DI bool index_matched(float eta) { return fabsf(eta - 1.0f) < 1e-3f; }
+
 // RoughDielectricBSDF (bsdf-rough-dielectric.slang:65-161)
 template <class G>
 GBPT_DI BsdfSample rough_dielectric_sample(float alpha, float eta, float3 tint, float3 wi, G& rng) {
@@ -341,7 +347,9 @@ GBPT_DI BsdfSample rough_dielectric_sample(float alpha, float eta, float3 tint, 
     if (all_zero(wo) || wo.z > -kBsdfMinCos) return no_sample();
     const float wodoth = dot(wo, wm);
     const float denom = wodoth + eta * widoth;
-    const float pdf = (1.0f - R) * vndf_h_pdf(wi, wm, a2) * fabsf(wodoth) / pow2(denom);
+    const float pdf = index_matched(eta)
+                          ? __int_as_float(0x7f800000)
+                          : (1.0f - R) * vndf_h_pdf(wi, wm, a2) * fabsf(wodoth) / pow2(denom);
     const float w = pow2(eta) * g2_over_s(fabsf(wo.z), wi.z, a2) / g1_over_s(wi.z, a2);
     return mk_sample(wo, pdf, tint * w);
 }
@@ -353,9 +361,14 @@ GBPT_DI float3 rough_dielectric_eval(float alpha, float eta, float3 tint, float3
         const float g = R * ggx_eval(alpha, alpha, wi, wo);
         return f3(g, g, g);
     }
-    if (wo.z < -kBsdfMinCos) {
+    // index-matched boundary: the transmission is a delta only sampling produces, so evaluation
+    // (next-event estimation, MIS) sees no transmission lobe
+    if (wo.z < -kBsdfMinCos && !index_matched(eta)) {
         float3 h = normalize(wo + wi * eta);
         h = h * signf(h.z);
+        // only a microfacet seen from its front by wi and left through its back by wo refracts
+        // wi into wo; the other configurations are never sampled, so they carry no density here
+        if (!(dot(wi, h) > 0.0f && dot(wo, h) < 0.0f)) return f3(0.f, 0.f, 0.f);
         const float R = fresnel_dielectric(fabsf(dot(wi, h)), eta);
         // GGXBTDF::eval (brdf-ggx.slang:427-444)
         const float widoth = dot(wi, h), wodoth = dot(wo, h);
@@ -376,9 +389,10 @@ GBPT_DI float rough_dielectric_pdf(float alpha, float eta, float3 wi, float3 wo)
         const float R = fresnel_dielectric(fabsf(dot(wi, h)), eta);
         return R * vndf_pdf_wo_s(wi.z, pow2(fmaxf(0.0f, h.z)), a2);
     }
-    if (wo.z < -kBsdfMinCos) {
+    if (wo.z < -kBsdfMinCos && !index_matched(eta)) { // else a delta transmission
         float3 h = normalize(wo + wi * eta);
         h = h * signf(h.z);
+        if (!(dot(wi, h) > 0.0f && dot(wo, h) < 0.0f)) return 0.0f; // as the eval
         const float R = fresnel_dielectric(fabsf(dot(wi, h)), eta);
         const float wodoth = dot(wo, h);
         const float denom = wodoth + eta * dot(wi, h);
@@ -451,13 +465,13 @@ GBPT_DI float dielectric_pdf(const Material& m, float3 wi, float3 wo) {
 template <class G> GBPT_DI BsdfSample dielectric_sample(const Material& m, float3 wi, G& rng) {
     if (m.tw > 0.0f && rng.next_float() < m.tw) {
         const BsdfSample s = rough_dielectric_sample(m.alpha_iso, m.eta, m.tcol, wi, rng);
-        if (!s.valid || m.tw == 1.0f) return s;
+        if (!s.valid || m.tw == 1.0f || !(s.pdf < kInf)) return s;
         const float mp = lerpf(opaque_pdf(m, wi, s.wo), s.pdf, m.tw);
         const float3 me = lerp3(opaque_eval(m, wi, s.wo), s.weight * s.pdf, m.tw);
         return mk_sample(s.wo, mp, me / mp);
     }
     const BsdfSample s = opaque_sample(m, wi, rng);
-    if (!s.valid || m.tw == 0.0f) return s;
+    if (!s.valid || m.tw == 0.0f || !(s.pdf < kInf)) return s;
     const float mp = lerpf(s.pdf, rough_dielectric_pdf(m.alpha_iso, m.eta, wi, s.wo), m.tw);
     const float3 me =
         lerp3(s.weight * s.pdf, rough_dielectric_eval(m.alpha_iso, m.eta, m.tcol, wi, s.wo), m.tw);
@@ -480,13 +494,13 @@ template <class G> GBPT_DI BsdfSample material_sample(const Material& m, float3 
     if (m.model == 0u) return lambert_sample(m.base, wi, rng);
     if (m.metal > 0.0f && rng.next_float() < m.metal) {
         const BsdfSample s = conductor_sample(m.ax, m.ay, m.base, wi, rng);
-        if (!s.valid || m.metal == 1.0f) return s;
+        if (!s.valid || m.metal == 1.0f || !(s.pdf < kInf)) return s;
         const float mp = lerpf(dielectric_pdf(m, wi, s.wo), s.pdf, m.metal);
         const float3 me = lerp3(dielectric_eval(m, wi, s.wo), s.weight * s.pdf, m.metal);
         return mk_sample(s.wo, mp, me / mp);
     }
     const BsdfSample s = dielectric_sample(m, wi, rng);
-    if (!s.valid || m.metal == 0.0f) return s;
+    if (!s.valid || m.metal == 0.0f || !(s.pdf < kInf)) return s;
     const float mp = lerpf(s.pdf, ggx_pdf(m.ax, m.ay, wi, s.wo), m.metal);
     const float3 me = lerp3(s.weight * s.pdf, conductor_eval(m.ax, m.ay, m.base, wi, s.wo), m.metal);
     return mk_sample(s.wo, mp, me / mp);

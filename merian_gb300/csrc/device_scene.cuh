@@ -277,6 +277,230 @@ __device__ __forceinline__ Hit trace_ray(const DevScene& sc, float3 o, float3 d,
     return best;
 }
 
+// ---- persistent traversal -------------------------------------------------------------------------
+// Warps stay resident and pull rays from a global counter. A lane whose ray finished takes a new
+// one (one atomic per warp for all idle lanes); a warp leaves its inner loop to refill once fewer
+// than kRefillLanes lanes are still busy, and a lane postpones its pending triangle tests (pushes
+// the triangle group onto its stack) when fewer than kPostponeLanes lanes of the warp have
+// triangles to test, so node steps and triangle steps stay in lockstep across the warp. The
+// closest-hit result and the tie rule are the same as trace_ray's: only the visit order changes.
+constexpr int kRefillLanes = 20;
+constexpr int kPostponeLanes = 6;
+
+struct TraceState {
+    float3 o, d, inv;
+    float tmin;
+    uint32_t oct_inv, oct_inv4;
+    bool negx, negy, negz;
+    RayPre pre;
+    uint2 ngroup, tgroup;
+    int sp;
+    Hit best;
+    bool found;
+};
+
+GBPT_DI void trace_init(TraceState& s, float3 o, float3 d, float tmin, float tmax) {
+    s.o = o;
+    s.d = d;
+    s.inv = f3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+    s.tmin = tmin;
+    const uint32_t oct = (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) |
+                         ((__float_as_uint(d.z) >> 31) << 2);
+    s.oct_inv = 7u - oct;
+    s.oct_inv4 = s.oct_inv * 0x01010101u;
+    s.negx = (__float_as_uint(d.x) >> 31) != 0u;
+    s.negy = (__float_as_uint(d.y) >> 31) != 0u;
+    s.negz = (__float_as_uint(d.z) >> 31) != 0u;
+    s.pre = ray_pre(o, d);
+    s.ngroup = make_uint2(0u, 0x80000000u);
+    s.tgroup = make_uint2(0u, 0u);
+    s.sp = 0;
+    s.best.t = tmax;
+    s.best.u = s.best.v = 0.0f;
+    s.best.prim = 0xFFFFFFFFu;
+    s.best.geom = 0xFFFFFFFFu;
+    s.found = false;
+}
+
+// Intersects the 8 children of node `ni`; returns the hit mask (inner children in bits 24..31 in
+// traversal order, triangles in bits 0..23) and the node's child / triangle bases and imask.
+template <bool COUNT>
+GBPT_DI uint32_t intersect_node(const DevScene& sc, const TraceState& s, uint32_t ni,
+                                uint32_t& child_base, uint32_t& tri_base, uint32_t& imask,
+                                TraceCounters* ctr) {
+    if (COUNT) ctr->nodes++;
+    const uint4 n0 = __ldg(&sc.nodes[5 * ni + 0]);
+    const uint4 n1 = __ldg(&sc.nodes[5 * ni + 1]);
+    const uint4 n2 = __ldg(&sc.nodes[5 * ni + 2]);
+    const uint4 n3 = __ldg(&sc.nodes[5 * ni + 3]);
+    const uint4 n4 = __ldg(&sc.nodes[5 * ni + 4]);
+    const float kErr = 1.0f / 1048576.0f;
+    const float aix = __uint_as_float((n0.w & 0xFFu) << 23) * s.inv.x;
+    const float aiy = __uint_as_float(((n0.w >> 8) & 0xFFu) << 23) * s.inv.y;
+    const float aiz = __uint_as_float(((n0.w >> 16) & 0xFFu) << 23) * s.inv.z;
+    const float aox = (__uint_as_float(n0.x) - s.o.x) * s.inv.x;
+    const float aoy = (__uint_as_float(n0.y) - s.o.y) * s.inv.y;
+    const float aoz = (__uint_as_float(n0.z) - s.o.z) * s.inv.z;
+    const float ex = (fabsf(aox) + 255.0f * fabsf(aix)) * kErr;
+    const float ey = (fabsf(aoy) + 255.0f * fabsf(aiy)) * kErr;
+    const float ez = (fabsf(aoz) + 255.0f * fabsf(aiz)) * kErr;
+    const float nox = aox - ex, fox = aox + ex;
+    const float noy = aoy - ey, foy = aoy + ey;
+    const float noz = aoz - ez, foz = aoz + ez;
+    imask = n0.w >> 24;
+    child_base = n1.x;
+    tri_base = n1.y;
+    uint32_t hitmask = 0;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const uint32_t meta4 = half ? n1.w : n1.z;
+        const uint32_t is_inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
+        const uint32_t inner_mask4 = (is_inner4 >> 4) * 0xFFu;
+        const uint32_t bit_index4 = (meta4 ^ (s.oct_inv4 & inner_mask4)) & 0x1F1F1F1Fu;
+        const uint32_t child_bits4 = (meta4 >> 5) & 0x07070707u;
+        const uint32_t qlx = half ? n2.y : n2.x, qly = half ? n2.w : n2.z;
+        const uint32_t qlz = half ? n3.y : n3.x, qhx = half ? n3.w : n3.z;
+        const uint32_t qhy = half ? n4.y : n4.x, qhz = half ? n4.w : n4.z;
+        const uint32_t nqx = s.negx ? qhx : qlx, fqx = s.negx ? qlx : qhx;
+        const uint32_t nqy = s.negy ? qhy : qly, fqy = s.negy ? qly : qhy;
+        const uint32_t nqz = s.negz ? qhz : qlz, fqz = s.negz ? qlz : qhz;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t sh = 8u * j;
+            const float tnx = fmaf((float)((nqx >> sh) & 0xFFu), aix, nox);
+            const float tny = fmaf((float)((nqy >> sh) & 0xFFu), aiy, noy);
+            const float tnz = fmaf((float)((nqz >> sh) & 0xFFu), aiz, noz);
+            const float tfx = fmaf((float)((fqx >> sh) & 0xFFu), aix, fox);
+            const float tfy = fmaf((float)((fqy >> sh) & 0xFFu), aiy, foy);
+            const float tfz = fmaf((float)((fqz >> sh) & 0xFFu), aiz, foz);
+            const float cmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, s.tmin));
+            const float cmax = fminf(fminf(tfx, tfy), fminf(tfz, s.best.t));
+            if (cmin <= cmax) hitmask |= ((child_bits4 >> sh) & 7u) << ((bit_index4 >> sh) & 31u);
+        }
+    }
+    return hitmask;
+}
+
+// Runs the traversal of every ray i < n, pulling indices from *fetch (zero before the launch).
+// load(i, o, d, tmin, tmax) fetches ray i; store(i, hit) receives its result (geom == 0xFFFFFFFF
+// on miss; with ANY, the first hit found). Must be called by all 32 lanes of every warp.
+template <bool ANY, bool COUNT, class Load, class Store>
+__device__ __forceinline__ void trace_persistent(const DevScene& sc, uint32_t n, uint32_t* fetch,
+                                                 uint32_t ray_mask, Load load, Store store,
+                                                 TraceCounters* ctr, uint32_t* err) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint2 stack[kStackSize];
+    TraceState s;
+    uint32_t ray = 0xFFFFFFFFu;
+    bool active = false, exhausted = false;
+    while (true) {
+        __syncwarp();
+        const bool want = !active && !exhausted;
+        const uint32_t want_mask = __ballot_sync(0xFFFFFFFFu, want);
+        if (want_mask) {
+            const uint32_t leader = __ffs(want_mask) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(want_mask));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (want) {
+                ray = base + __popc(want_mask & ((1u << lane) - 1u));
+                if (ray < n) {
+                    float3 o, d;
+                    float tmin, tmax;
+                    load(ray, o, d, tmin, tmax);
+                    trace_init(s, o, d, tmin, tmax);
+                    active = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xFFFFFFFFu, active) == 0u) break;
+        // once a lane found the pool empty, leaving the inner loop to refill gains nothing
+        const bool pool_empty = __ballot_sync(0xFFFFFFFFu, exhausted) != 0u;
+        if (!active) continue;
+        // inner loop: node step, then (possibly postponed) triangle steps
+        while (true) {
+            if (s.ngroup.y > 0x00FFFFFFu) {
+                const uint32_t hits = s.ngroup.y;
+                const uint32_t bit = 31u - __clz(hits & 0xFF000000u);
+                s.ngroup.y &= ~(1u << bit);
+                if (s.ngroup.y > 0x00FFFFFFu) {
+                    if (s.sp >= kStackSize) {
+                        atomicOr(err, 1u);
+                        s.sp = 0;
+                        s.ngroup.y = 0;
+                        s.tgroup.y = 0;
+                        break;
+                    }
+                    stack[s.sp++] = s.ngroup;
+                }
+                const uint32_t slot = (bit - 24u) ^ s.oct_inv;
+                const uint32_t ni = s.ngroup.x + __popc((hits & 0xFFu) & ((1u << slot) - 1u));
+                uint32_t cb, tb, im;
+                const uint32_t hm = intersect_node<COUNT>(sc, s, ni, cb, tb, im, ctr);
+                s.ngroup = make_uint2(cb, (hm & 0xFF000000u) | im);
+                s.tgroup = make_uint2(tb, hm & 0x00FFFFFFu);
+            } else {
+                // a postponed triangle group came off the stack
+                s.tgroup = s.ngroup;
+                s.ngroup = make_uint2(0u, 0u);
+            }
+            bool done_any = false;
+            // only groups followed by node work are postponed (a group popped back is tested)
+            const bool may_postpone = s.ngroup.y > 0x00FFFFFFu;
+            while (s.tgroup.y != 0u) {
+                if (may_postpone && s.sp < kStackSize &&
+                    __popc(__activemask()) < kPostponeLanes) {
+                    stack[s.sp++] = s.tgroup;
+                    s.tgroup.y = 0u;
+                    break;
+                }
+                const uint32_t b = __ffs(s.tgroup.y) - 1u;
+                s.tgroup.y &= s.tgroup.y - 1u;
+                const uint32_t ti = s.tgroup.x + b;
+                const float4 r0 = __ldg(&sc.tris[3 * ti + 0]);
+                const float4 r1 = __ldg(&sc.tris[3 * ti + 1]);
+                const float4 r2 = __ldg(&sc.tris[3 * ti + 2]);
+                const uint32_t tfl = __float_as_uint(r2.w);
+                if (((tfl & 0xFFu) & ray_mask) == 0u) continue;
+                if (COUNT) ctr->tris++;
+                float t, u, v;
+                if (!intersect_tri(s.pre, r0, r1, r2, tfl, s.tmin, s.best.t, t, u, v)) continue;
+                const uint32_t prim = __float_as_uint(r0.w), geom = __float_as_uint(r1.w);
+                if (t < s.best.t || geom < s.best.geom ||
+                    (geom == s.best.geom && prim < s.best.prim)) {
+                    s.best.t = t;
+                    s.best.u = u;
+                    s.best.v = v;
+                    s.best.prim = prim;
+                    s.best.geom = geom;
+                    s.found = true;
+                    if (ANY) {
+                        done_any = true;
+                        break;
+                    }
+                }
+            }
+            bool done = done_any;
+            if (!done && s.ngroup.y <= 0x00FFFFFFu) {
+                if (s.sp == 0) done = true;
+                else s.ngroup = stack[--s.sp];
+            }
+            if (done) {
+                if (!s.found) {
+                    s.best.geom = 0xFFFFFFFFu;
+                    s.best.prim = 0xFFFFFFFFu;
+                }
+                store(ray, s.best);
+                active = false;
+                break;
+            }
+            if (!pool_empty && __popc(__activemask()) < kRefillLanes) break;
+        }
+    }
+}
+
 // ---- camera (camera.slang:29-56), bit-identical to the oracle's FP32 build ---------------------------
 struct CamGPU {
     float3 pos, U, V, W;

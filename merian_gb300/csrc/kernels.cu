@@ -434,21 +434,30 @@ __global__ void __launch_bounds__(128) k_shade_primary(DevScene sc, FrameArgs a,
     }
 }
 
-// Closest hit for every entry of ray queue `qi`.
+// Resident 128-thread blocks per SM the traversal kernels are register-budgeted for
+// (65536 / (8 * 128) = 64 registers per thread).
+constexpr int kTraceBlocksPerSM = 8;
+
+// Closest hit for every entry of ray queue `qi` (persistent warps, counter w.counters[4]).
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_trace(DevScene sc, Work w, int qi, uint32_t mask,
+__global__ void __launch_bounds__(128, kTraceBlocksPerSM) k_trace(DevScene sc, Work w, int qi, uint32_t mask,
                                                unsigned long long* work_ctr) {
     const uint32_t n = w.counters[qi];
-    const uint32_t stride = gridDim.x * blockDim.x;
     TraceCounters ctr{0, 0};
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float4 a = w.q_od[qi][2 * i + 0];
-        const float4 b = w.q_od[qi][2 * i + 1];
-        const Hit h = trace_ray<false, COUNT>(sc, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w, b.w,
-                                              mask, &ctr, w.counters + 3);
+    const float4* q = w.q_od[qi];
+    auto load = [&](uint32_t i, float3& o, float3& d, float& tmin, float& tmax) {
+        const float4 a = q[2 * i + 0];
+        const float4 b = q[2 * i + 1];
+        o = f3(a.x, a.y, a.z);
+        d = f3(b.x, b.y, b.z);
+        tmin = a.w;
+        tmax = b.w;
+    };
+    auto store = [&](uint32_t i, const Hit& h) {
         w.hit_tuv[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
         w.hit_geom[i] = h.geom;
-    }
+    };
+    trace_persistent<false, COUNT>(sc, n, w.counters + 4, mask, load, store, &ctr, w.counters + 3);
     if (COUNT) {
         atomicAdd(work_ctr + 0, (unsigned long long)ctr.nodes);
         atomicAdd(work_ctr + 1, (unsigned long long)ctr.tris);
@@ -522,14 +531,17 @@ __global__ void __launch_bounds__(128) k_shade(DevScene sc, FrameArgs a, int k, 
 }
 
 // Occlusion of the NEE queue; unoccluded contributions are added to their path.
-__global__ void __launch_bounds__(128) k_shadow(DevScene sc, Work w, uint32_t mask) {
+__global__ void __launch_bounds__(128, kTraceBlocksPerSM) k_shadow(DevScene sc, Work w, uint32_t mask) {
     const uint32_t n = w.counters[2];
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    auto load = [&](uint32_t i, float3& o, float3& d, float& tmin, float& tmax) {
         const float4 a = w.s_od[2 * i + 0];
         const float4 b = w.s_od[2 * i + 1];
-        const Hit h = trace_ray<true, false>(sc, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), 0.f, a.w,
-                                             mask, nullptr, w.counters + 3);
+        o = f3(a.x, a.y, a.z);
+        d = f3(b.x, b.y, b.z);
+        tmin = 0.0f;
+        tmax = a.w;
+    };
+    auto store = [&](uint32_t i, const Hit& h) {
         if (h.geom == 0xFFFFFFFFu) {
             const uint32_t p = w.s_path[i];
             const float4 c = w.s_contrib[i];
@@ -539,7 +551,9 @@ __global__ void __launch_bounds__(128) k_shadow(DevScene sc, Work w, uint32_t ma
             r.z += c.z;
             w.rad[p] = r;
         }
-    }
+    };
+    trace_persistent<true, false>(sc, n, w.counters + 5, mask, load, store, nullptr,
+                                  w.counters + 3);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         atomicAdd(w.stats + 0, (unsigned long long)n);
         atomicAdd(w.stats + 1, (unsigned long long)n);
@@ -577,17 +591,20 @@ __global__ void __launch_bounds__(128) k_finalize(FrameArgs a, float4* out, uint
     }
 }
 
-__global__ void k_trace_rays(DevScene sc, const gbpt_ray* rays, uint32_t n, uint32_t mask, int any,
-                             gbpt_hit* hits, unsigned long long* work_ctr, uint32_t* err) {
-    const uint32_t stride = gridDim.x * blockDim.x;
+template <bool ANY>
+__global__ void __launch_bounds__(128, kTraceBlocksPerSM) k_trace_rays(DevScene sc, const gbpt_ray* rays, uint32_t n,
+                                                    uint32_t mask, gbpt_hit* hits,
+                                                    unsigned long long* work_ctr, uint32_t* fetch,
+                                                    uint32_t* err) {
     TraceCounters ctr{0, 0};
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    auto load = [&](uint32_t i, float3& o, float3& d, float& tmin, float& tmax) {
         const gbpt_ray r = rays[i];
-        const float3 o = f3(r.origin[0], r.origin[1], r.origin[2]);
-        const float3 d = f3(r.direction[0], r.direction[1], r.direction[2]);
-        Hit h;
-        if (any) h = trace_ray<true, true>(sc, o, d, r.tmin, r.tmax, mask, &ctr, err);
-        else h = trace_ray<false, true>(sc, o, d, r.tmin, r.tmax, mask, &ctr, err);
+        o = f3(r.origin[0], r.origin[1], r.origin[2]);
+        d = f3(r.direction[0], r.direction[1], r.direction[2]);
+        tmin = r.tmin;
+        tmax = r.tmax;
+    };
+    auto store = [&](uint32_t i, const Hit& h) {
         gbpt_hit out;
         const bool ok = h.geom != 0xFFFFFFFFu;
         out.instance_id = ok ? 0u : 0xFFFFFFFFu;
@@ -599,7 +616,8 @@ __global__ void k_trace_rays(DevScene sc, const gbpt_ray* rays, uint32_t n, uint
         out.t = ok ? h.t : -1.0f;
         out.reserved = 0;
         hits[i] = out;
-    }
+    };
+    trace_persistent<ANY, true>(sc, n, fetch, mask, load, store, &ctr, err);
     if (work_ctr) {
         atomicAdd(work_ctr + 0, (unsigned long long)ctr.nodes);
         atomicAdd(work_ctr + 1, (unsigned long long)ctr.tris);
@@ -625,6 +643,14 @@ __global__ void k_trace_primary(DevScene sc, CamGPU cam, uint32_t w, uint32_t h,
     out.t = ok ? ht.t : -1.0f;
     out.reserved = 0;
     hits[i] = out;
+}
+
+// Blocks of 128 threads that fit the whole GPU at once (persistent kernels).
+template <class K> int persistent_grid(K kernel) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, 128, 0) != cudaSuccess || nb <= 0)
+        nb = 4;
+    return nb * num_sms();
 }
 
 CamGPU to_cam(const gbpt_camera& c) {
@@ -754,6 +780,10 @@ int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStr
     a.pixels = args.pixels_device;
     a.w = w;
     const int grid = num_sms() * 8;
+    // persistent traversal kernels: exactly the resident blocks
+    const int trace_grid = persistent_grid(k_trace<false>);
+    const int trace_grid_c = persistent_grid(k_trace<true>);
+    const int shadow_grid = persistent_grid(k_shadow);
     uint64_t nl = 0;
     for (uint32_t base = 0; base < P; base += pix_per_wave) {
         a.pix_base = base;
@@ -770,8 +800,9 @@ int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStr
         prof->end(st, ev);
         nl += 2;
         if (a.nee) {
+            cudaMemsetAsync(w.counters + 5, 0, sizeof(uint32_t), st);
             ev = prof->begin(st, 2);
-            k_shadow<<<grid, 128, 0, st>>>(sc, w, a.mask);
+            k_shadow<<<shadow_grid, 128, 0, st>>>(sc, w, a.mask);
             prof->end(st, ev);
             cudaMemsetAsync(w.counters + 2, 0, sizeof(uint32_t), st);
             nl += 1;
@@ -779,9 +810,10 @@ int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStr
         int qi = 0;
         for (int k = 2; k <= a.max_len; ++k) {
             const int qo = qi ^ 1;
+            cudaMemsetAsync(w.counters + 4, 0, sizeof(uint32_t), st);
             ev = prof->begin(st, 0);
-            if (count_work) k_trace<true><<<grid, 128, 0, st>>>(sc, w, qi, a.mask, work_ctr);
-            else k_trace<false><<<grid, 128, 0, st>>>(sc, w, qi, a.mask, nullptr);
+            if (count_work) k_trace<true><<<trace_grid_c, 128, 0, st>>>(sc, w, qi, a.mask, work_ctr);
+            else k_trace<false><<<trace_grid, 128, 0, st>>>(sc, w, qi, a.mask, nullptr);
             prof->end(st, ev);
             cudaMemsetAsync(w.counters + qo, 0, sizeof(uint32_t), st);
             ev = prof->begin(st, 1);
@@ -790,8 +822,9 @@ int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStr
             prof->end(st, ev);
             nl += 2;
             if (a.nee && k < a.max_len) {
+                cudaMemsetAsync(w.counters + 5, 0, sizeof(uint32_t), st);
                 ev = prof->begin(st, 2);
-                k_shadow<<<grid, 128, 0, st>>>(sc, w, a.mask);
+                k_shadow<<<shadow_grid, 128, 0, st>>>(sc, w, a.mask);
                 prof->end(st, ev);
                 cudaMemsetAsync(w.counters + 2, 0, sizeof(uint32_t), st);
                 nl += 1;
@@ -835,9 +868,15 @@ int trace_rays(const SceneGPU& scene, const gbpt_ray* rays, uint32_t n, uint32_t
                gbpt_hit* hits, unsigned long long* work_ctr, cudaStream_t st) {
     if (n == 0) return GBPT_OK;
     const DevScene sc = make_dev_scene(scene);
-    const int grid = (int)std::min<uint64_t>((n + 127) / 128, (uint64_t)num_sms() * 8);
     uint32_t* err = reinterpret_cast<uint32_t*>(work_ctr + 2);
-    k_trace_rays<<<grid, 128, 0, st>>>(sc, rays, n, mask & 0xFFu, any_hit, hits, work_ctr, err);
+    uint32_t* fetch = reinterpret_cast<uint32_t*>(work_ctr + 3);
+    cudaMemsetAsync(fetch, 0, sizeof(uint32_t), st);
+    if (any_hit)
+        k_trace_rays<true><<<persistent_grid(k_trace_rays<true>), 128, 0, st>>>(
+            sc, rays, n, mask & 0xFFu, hits, work_ctr, fetch, err);
+    else
+        k_trace_rays<false><<<persistent_grid(k_trace_rays<false>), 128, 0, st>>>(
+            sc, rays, n, mask & 0xFFu, hits, work_ctr, fetch, err);
     return cudaGetLastError() == cudaSuccess ? GBPT_OK : GBPT_ERR_CUDA;
 }
 

@@ -134,6 +134,20 @@ def material_samples(material: np.ndarray, front: bool, ior: float, wi, seed: in
     return out
 
 
+def bsdf_integrals(kind: str, wi, alpha: float = 0.3, eta: float = 1 / 1.5,
+                   ior_f0: float = 0.04, n_samples: int = 1 << 20, n_theta: int = 1024) -> dict:
+    """Sampler vs evaluation: furnace and valid fraction against the full-sphere quadrature of
+    eval and pdf (FP64)."""
+    out = np.zeros(4, np.float64)
+    w = np.asarray(wi, np.float64)
+    lib = load()
+    lib.oracle_bsdf_integrals.argtypes = [C.c_int, C.c_void_p, C.c_double, C.c_double,
+                                          C.c_double, C.c_uint32, C.c_uint32, C.c_void_p]
+    lib.oracle_bsdf_integrals(BSDF_KINDS[kind], _p(w), alpha, eta, ior_f0, n_samples, n_theta,
+                              _p(out))
+    return dict(furnace=out[0], eval_integral=out[1], valid=out[2], pdf_integral=out[3])
+
+
 def unpack_check(out: np.ndarray, n_samples: int) -> dict:
     return dict(furnace=out[0:3].astype(np.float64), furnace_stderr=out[3:6].astype(np.float64),
                 mean_cos=float(out[6]), stderr_cos=float(out[7]), valid=int(out[8]),

@@ -959,6 +959,77 @@ ORACLE_API int oracle_num_threads(void) {
 // eta = 1/1.5, tint = albedo), 4 FresnelMix<GGX, Lambert>(alpha, albedo, ior_f0). out: 16 floats in
 // the reference's slot layout (furnace rgb, furnace stderr rgb, mean_cos, stderr_cos, valid,
 // max_weight_err, max_pdf_err, pdf_integral, max_recip_err, -, -, -).
+// Consistency of a BSDF's evaluation with its sampler, the property next-event estimation and MIS
+// rely on: out = {mean sample weight (furnace, r channel), full-sphere quadrature of eval (r),
+// fraction of valid samples, full-sphere quadrature of pdf}. kind as oracle_bsdf_check.
+ORACLE_API int oracle_bsdf_integrals(int kind, const double* wi_in, double alpha, double eta,
+                                     double ior_f0, uint32_t n_samples, uint32_t n_theta,
+                                     double* out) {
+    using R = double;
+    const V3<R> wi = mk(wi_in[0], wi_in[1], wi_in[2]);
+    const V3<R> alb = mk(0.7, 0.7, 0.7);
+    Lambert<R> lam{alb};
+    GGX<R> ggx{alpha, alpha};
+    Conductor<R> cond{GGX<R>{alpha, alpha}, mk(0.95, 0.64, 0.54)};
+    RoughDielectric<R> rd{alpha, eta, mk(1.0, 1.0, 1.0)};
+    OpaqueDielectric<R> fm{GGX<R>{alpha, alpha}, Lambert<R>{alb}, ior_f0};
+    auto se = [&](XorShift& rng) -> Sample<R> {
+        switch (kind) {
+        case 0: return lam.sample_eval(wi, rng);
+        case 1: return ggx.sample_eval(wi, rng);
+        case 2: return cond.sample_eval(wi, rng);
+        case 3: return rd.sample_eval(wi, rng);
+        default: return fm.sample_eval(wi, rng);
+        }
+    };
+    auto ev = [&](V3<R> wo) -> R {
+        switch (kind) {
+        case 0: return lam.eval(wi, wo).x;
+        case 1: return ggx.eval(wi, wo).x;
+        case 2: return cond.eval(wi, wo).x;
+        case 3: return rd.eval(wi, wo).x;
+        default: return fm.eval(wi, wo).x;
+        }
+    };
+    auto pd = [&](V3<R> wo) -> R {
+        switch (kind) {
+        case 0: return lam.pdf(wi, wo);
+        case 1: return ggx.pdf(wi, wo);
+        case 2: return cond.pdf(wi, wo);
+        case 3: return rd.pdf(wi, wo);
+        default: return fm.pdf(wi, wo);
+        }
+    };
+    XorShift rng{0x1234567u};
+    double fur = 0.0;
+    uint32_t valid = 0;
+    for (uint32_t i = 0; i < n_samples; ++i) {
+        const Sample<R> s = se(rng);
+        if (s.valid) {
+            fur += s.weight.x;
+            ++valid;
+        }
+    }
+    const uint32_t n_phi = 2 * n_theta;
+    double ie = 0.0, ip = 0.0;
+    for (uint32_t ti = 0; ti < n_theta; ++ti) {
+        const double t = (ti + 0.5) * C<R>::PI / n_theta;
+        const double st = std::sin(t), ct = std::cos(t);
+        for (uint32_t pi = 0; pi < n_phi; ++pi) {
+            const double p = (pi + 0.5) * C<R>::TWO_PI / n_phi;
+            const V3<R> wo = mk(st * std::cos(p), st * std::sin(p), ct);
+            const double dw = st * (C<R>::PI / n_theta) * (C<R>::TWO_PI / n_phi);
+            ie += ev(wo) * dw;
+            ip += pd(wo) * dw;
+        }
+    }
+    out[0] = fur / n_samples;
+    out[1] = ie;
+    out[2] = (double)valid / n_samples;
+    out[3] = ip;
+    return 0;
+}
+
 // n samples of a material at one shading point, 12 floats each (wo, pdf, weight, valid, eval,
 // pdf at wo); sample i draws from PCG(pcg4d16(i, seed, 0, 0)), as gbpt_debug_material_samples.
 ORACLE_API int oracle_material_samples(const gbpt_material* m, int front, float ior,

@@ -429,7 +429,9 @@ template <class R> struct RoughDielectric {
             return none<R>();
         const R wodoth = dot(wo, wm);
         const R denom = wodoth + eta * widoth;
-        const R pdf = (R(1) - Rf) * ggx_vndf_h_pdf(wi, wm, a2) * std::fabs(wodoth) / pow2(denom);
+        const R pdf = index_matched()
+                          ? R(INFINITY)
+                          : (R(1) - Rf) * ggx_vndf_h_pdf(wi, wm, a2) * std::fabs(wodoth) / pow2(denom);
         const R w = pow2(eta) * smith_g2_over_widotn_s(std::fabs(wo.z), wi.z, a2) /
                     smith_g1_over_widotn_s(wi.z, a2);
         return some(wo, pdf, tint * w);
@@ -441,14 +443,24 @@ template <class R> struct RoughDielectric {
             const R Rf = fresnel_dielectric(std::fabs(dot(wi, h)), eta);
             return Rf * GGX<R>{alpha, alpha}.eval(wi, wo);
         }
-        if (wo.z < -R(BSDF_MIN_COS)) {
+        if (wo.z < -R(BSDF_MIN_COS) && !index_matched()) {
             V3<R> h = normalize(wo + wi * eta);
             h = h * signr(h.z);
+            // only a microfacet that wi sees from its front and wo leaves through its back
+            // refracts wi into wo; the reference's formula also counts the other side, which
+            // the sampler never produces (evaluation must match sample_eval for NEE and MIS)
+            if (!(dot(wi, h) > R(0) && dot(wo, h) < R(0))) return mk(R(0), R(0), R(0));
             const R Rf = fresnel_dielectric(std::fabs(dot(wi, h)), eta);
             return (R(1) - Rf) * btdf_eval(wi, wo);
         }
+        // Index-matched boundary (|eta - 1| < 1e-3; the IOR bookkeeping lands on 0.99999994 as
+        // often as on 1): every microfacet refracts (nearly) straight through, a delta lobe that
+        // only sample_eval produces (it reports pdf = inf). The microfacet formula would give a
+        // density the sampler never draws, so evaluation (next-event estimation, MIS) sees no
+        // transmission lobe there.
         return mk(R(0), R(0), R(0));
     }
+    bool index_matched() const { return std::fabs(eta - R(1)) < R(1e-3); }
     // GGXBTDF::eval (brdf-ggx.slang:427-444)
     V3<R> btdf_eval(V3<R> wi, V3<R> wo) const {
         if ((wi.z < R(BSDF_MIN_COS)) || (wo.z > -R(BSDF_MIN_COS))) return mk(R(0), R(0), R(0));
@@ -470,9 +482,10 @@ template <class R> struct RoughDielectric {
             const R Rf = fresnel_dielectric(std::fabs(dot(wi, h)), eta);
             return Rf * ggx_vndf_pdf_wo_s(wi.z, pow2(maxr(R(0), h.z)), a2);
         }
-        if (wo.z < -R(BSDF_MIN_COS)) {
+        if (wo.z < -R(BSDF_MIN_COS) && !index_matched()) { // else a delta transmission
             V3<R> h = normalize(wo + wi * eta);
             h = h * signr(h.z);
+            if (!(dot(wi, h) > R(0) && dot(wo, h) < R(0))) return R(0); // as eval()
             const R Rf = fresnel_dielectric(std::fabs(dot(wi, h)), eta);
             const R wodoth = dot(wo, h);
             const R denom = wodoth + eta * dot(wi, h);
@@ -528,13 +541,14 @@ template <class R, class B0, class B1> struct Mix {
     template <class G> Sample<R> sample_eval(V3<R> wi, G& rng) const {
         if (w > R(0) && (R)rng.next_float() < w) {
             const Sample<R> s = b1.sample_eval(wi, rng);
-            if (!s.valid || w == R(1)) return s;
+            // a delta sample (pdf = inf) passes through: w f1 / (w p1) = its own weight
+            if (!s.valid || w == R(1) || !(s.pdf < R(INFINITY))) return s;
             const R mp = lerp(b0.pdf(wi, s.wo), s.pdf, w);
             const V3<R> me = lerp(b0.eval(wi, s.wo), s.weight * s.pdf, w);
             return some(s.wo, mp, me / mp);
         }
         const Sample<R> s = b0.sample_eval(wi, rng);
-        if (!s.valid || w == R(0)) return s;
+        if (!s.valid || w == R(0) || !(s.pdf < R(INFINITY))) return s;
         const R mp = lerp(s.pdf, b1.pdf(wi, s.wo), w);
         const V3<R> me = lerp(s.weight * s.pdf, b1.eval(wi, s.wo), w);
         return some(s.wo, mp, me / mp);

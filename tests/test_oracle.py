@@ -107,6 +107,21 @@ def test_conductor(alpha, wi):
     expect_energy_conserving(r)
 
 
+@pytest.mark.parametrize("kind,alpha,eta", [
+    ("lambert", 1.0, 1.0), ("ggx", 0.05, 1.0), ("ggx", 0.5, 1.0), ("conductor", 0.3, 1.0),
+    ("fresnel_mix", 0.3, 1.0), ("rough_dielectric", 0.05, 1 / 1.5),
+    ("rough_dielectric", 0.23, 1 / 1.5), ("rough_dielectric", 0.5, 1 / 1.5),
+    ("rough_dielectric", 0.23, 1.5), ("rough_dielectric", 0.5, 1.5)])
+@pytest.mark.parametrize("zen", [10.0, 50.0, 80.0])
+def test_eval_pdf_match_sampler(kind, alpha, eta, zen):
+    """Next-event estimation and MIS use eval() and pdf(); they must integrate (full sphere) to
+    what sample_eval delivers: the furnace value and the fraction of valid samples."""
+    r = O.bsdf_integrals(kind, wi_from_zenith(zen), alpha=alpha, eta=eta, n_samples=1 << 20,
+                         n_theta=768)
+    assert abs(r["eval_integral"] - r["furnace"]) < 3e-3 * max(r["furnace"], 0.1) + 2e-3
+    assert abs(r["pdf_integral"] - r["valid"]) < 3e-3 + 2e-3 * (alpha < 0.1)
+
+
 @pytest.fixture(scope="module")
 def cornell():
     from merian_gb300 import scene as S
@@ -154,5 +169,29 @@ def test_oracle_consistent_with_golden(cornell, nee, rr):
     var = np.maximum(sq - mean ** 2, 0)
     gm, gv, gn = g["mean"][:256], g["var"][:256], int(g["spp"])
     z, ok = z_scores(mean, np.sqrt(var / spp), gm, np.sqrt(gv / gn))
+    assert np.mean(np.abs(z) > 3) < 0.02, np.sort(np.abs(z))[-10:]
+    assert np.mean(z ** 2) < 1.5
+
+
+@pytest.mark.parametrize("nee,rr", [(True, 0), (True, 3)], ids=["nee", "nee_rr"])
+def test_oracle_nee_unbiased_on_soup(nee, rr):
+    """NEE with MIS (environment + glass, two-sided sheets, index-matched boundaries) converges to
+    the reference's BSDF-only estimator of the committed soup fixture."""
+    from merian_gb300 import scene as S
+    g = golden("soup_small")
+    sc = S.soup(S.BASE_SEED, 200_000, 256, (256, 128))
+    osc = O.OracleScene(sc)
+    cam = S.look_at((0.5, 0.5, -1.2), (0.5, 0.5, 0.5), (0, 1, 0), 45.0, 16 / 9)
+    pixels = g["pixels"][:192]
+    spp = 1024
+    params, keep = S.render_params(320, 180, spp, 8, pixels=pixels, nee=nee, rr_depth=rr,
+                                   frame=11)
+    rgba, sq, _ = osc.render(cam, params, fp64=True)
+    mean = rgba[:, :3]
+    var = np.maximum(sq - mean ** 2, 0)
+    gm, gv, gn = g["mean"][:192], g["var"][:192], int(g["spp"])
+    se = np.sqrt(var / spp + gv / gn + (1e-5 * gm) ** 2)
+    ok = se > 0
+    z = (mean - gm)[ok] / se[ok]
     assert np.mean(np.abs(z) > 3) < 0.02, np.sort(np.abs(z))[-10:]
     assert np.mean(z ** 2) < 1.5
