@@ -247,6 +247,22 @@ GBPT_API int gbpt_render_device(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera
                                 const gbpt_render_params* params, float* out_rgba_device,
                                 gbpt_render_stats* stats);
 
+/* Rendering for callers that cannot allocate device memory while they render: a host whose own
+ * allocator owns the GPU's memory, a real-time loop that must not block in cudaMalloc/cudaFree
+ * (either can synchronise the whole device), or a process whose memory budget is fixed when it
+ * starts. It runs the same wavefront as gbpt_render_device, but every scratch buffer comes from a
+ * fixed 64 MiB device array compiled into the library, held by each GPU that loads the library
+ * until the process exits; this call allocates nothing. The scene must already be resident
+ * (gbpt_scene_create, an earlier set-up step) and out_rgba_device is caller-owned device memory.
+ * Limits: spp at most the paths one pass over the array holds (242,182), a pixel
+ * subset of at most 65,536 entries; larger requests return GBPT_ERR_INVALID. The first call on a
+ * device looks up the array's device address, so make it before any stream capture. All calls
+ * share the array: calls that overlap on the GPU (other streams or threads) race on it. The call
+ * waits for its work to finish before it returns.
+ * (No counterpart in the reference: merian's node always renders into graph-allocated images.) */
+GBPT_API int gbpt_render_device_noalloc(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
+                                        const gbpt_render_params* params, float* out_rgba_device);
+
 /* ---- traversal queries (the GBuffer node's primary hit, and raw ray queries) ---------------
  * gbpt_trace_primary: the hit merian's GBuffer (Raytraced) node stores for each pixel
  * (gbuffer_rt.slang:18-58) with full-precision barycentrics and t, written to a host array of

@@ -115,6 +115,8 @@ EXPORTS = [
     ("gbpt_render_device", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Camera),
                                      C.POINTER(RenderParams), C.c_void_p,
                                      C.POINTER(RenderStats)]),
+    ("gbpt_render_device_noalloc", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Camera),
+                                             C.POINTER(RenderParams), C.c_void_p]),
     ("gbpt_trace_primary", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.c_uint32,
                                      C.c_uint32, C.c_uint32, C.c_void_p]),
     ("gbpt_trace", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int,

@@ -595,6 +595,41 @@ GBPT_API int gbpt_render_device(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera
     return render_impl(ctx, scene, camera, params, out_rgba_device, nullptr, stats);
 }
 
+// Render through the library's fixed scratch array: no device allocation on this path.
+GBPT_API int gbpt_render_device_noalloc(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
+                                        const gbpt_render_params* p, float* out_rgba_device) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if ((rc = validate_params(camera, p))) return rc;
+    if (!out_rgba_device) {
+        set_error("gbpt_render_device_noalloc: null output");
+        return GBPT_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) {
+        set_error("gbpt_render_device_noalloc: unknown scene id");
+        return GBPT_ERR_NOT_FOUND;
+    }
+    const uint32_t n_pix = p->pixel_count ? p->pixel_count : p->width * p->height;
+    if (p->spp == 0) {
+        GBPT_CUDA_CHECK(cudaMemsetAsync(out_rgba_device, 0, (size_t)n_pix * sizeof(float4),
+                                        ctx->stream));
+        GBPT_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        return GBPT_OK;
+    }
+    RenderArgs a;
+    a.camera = *camera;
+    a.params = *p;
+    a.pixel_count = n_pix;
+    a.pixels_device = nullptr;
+    a.out_device = (float4*)out_rgba_device;
+    std::string err;
+    rc = render_frame_static(it->second, a, p->pixel_count ? p->pixels : nullptr, ctx->stream, err);
+    if (rc != GBPT_OK) set_error("gbpt_render_device_noalloc: " + err);
+    return rc;
+}
+
 GBPT_API int gbpt_debug_primary_points(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
                                        const gbpt_render_params* p, float* out_host) {
     int rc = check_ctx(ctx);

@@ -16,6 +16,8 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
+#include <type_traits>
 
 namespace gbpt {
 
@@ -683,6 +685,7 @@ void work_free(Work& w) {
 }
 
 int work_reserve(Work& w, uint64_t paths, uint64_t pixels) {
+    if (w.fixed) return (paths <= w.path_cap && pixels <= w.pixel_cap) ? GBPT_OK : GBPT_ERR_NO_MEMORY;
     if (!w.counters) {
         uint64_t b = 0;
         if (alloc(w.counters, 16, b) != cudaSuccess) return GBPT_ERR_NO_MEMORY;
@@ -760,7 +763,7 @@ int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStr
     const uint32_t P = args.pixel_count;
     if (S == 0 || P == 0) return GBPT_OK;
     // wave: whole pixels, as many as fit the wave size (at least one pixel's samples)
-    const uint64_t target_paths = std::max<uint64_t>(S, kWavePaths);
+    const uint64_t target_paths = std::max<uint64_t>(S, w.fixed ? w.path_cap : kWavePaths);
     const uint32_t pix_per_wave =
         (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(P, target_paths / S));
     int rc = work_reserve(w, (uint64_t)pix_per_wave * S, pix_per_wave);
@@ -878,6 +881,137 @@ int trace_rays(const SceneGPU& scene, const gbpt_ray* rays, uint32_t n, uint32_t
         k_trace_rays<false><<<persistent_grid(k_trace_rays<false>), 128, 0, st>>>(
             sc, rays, n, mask & 0xFFu, hits, work_ctr, fetch, err);
     return cudaGetLastError() == cudaSuccess ? GBPT_OK : GBPT_ERR_CUDA;
+}
+
+// ---- rendering without allocation ------------------------------------------------------------------
+// Some callers must not allocate device memory while they render: a host whose allocator has
+// already reserved the GPU for itself, a real-time loop that may not block in cudaMalloc/cudaFree
+// (both can synchronise the device), or a process under a hard memory budget fixed at start-up.
+// For them the same wavefront runs with every scratch buffer carved from this fixed array, which
+// each GPU that loads the library holds until the process exits. Every call shares it and it keeps
+// the last call's contents: the counters are cleared per call, and calls that overlap on the GPU
+// (other streams, other host threads) race on it.
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+namespace {
+constexpr uint64_t kStaticCounterBytes = 256; // 16 counters + 8 stats words, padded
+constexpr uint64_t kStaticPixelBytes = (uint64_t)kStaticMaxPixelList * 4;
+// per path: throughput, radiance (16 + 16), rng (4), two ray queues (2 x 36), hits (20),
+// shadow queue (52); plus a 96-byte primary point per pixel, budgeted as one pixel per path
+constexpr uint64_t kStaticBytesPerPath = 16 + 16 + 4 + 2 * (32 + 4) + (16 + 4) + (32 + 16 + 4) + 96;
+
+std::mutex g_static_mu;
+void* g_static_ptr[64] = {};
+
+// The array's device address on the current device, looked up on the first call per device.
+int static_scratch_address(int dev, unsigned char** out) {
+    if (dev < 0 || dev >= 64) return GBPT_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess || !p) return GBPT_ERR_CUDA;
+        g_static_ptr[dev] = p;
+    }
+    *out = (unsigned char*)g_static_ptr[dev];
+    return GBPT_OK;
+}
+} // namespace
+
+uint64_t static_scratch_paths() {
+    // 16 x 256 bytes of slack for the alignment of the carved arrays
+    return (kStaticScratchBytes - kStaticCounterBytes - kStaticPixelBytes - 16 * 256) /
+           kStaticBytesPerPath;
+}
+
+int render_frame_static(const SceneGPU& scene, const RenderArgs& args, const uint32_t* pixels_host,
+                        cudaStream_t st, std::string& err) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        err = "cudaGetDevice failed";
+        return GBPT_ERR_CUDA;
+    }
+    unsigned char* base = nullptr;
+    int rc = static_scratch_address(dev, &base);
+    if (rc != GBPT_OK) {
+        err = "cudaGetSymbolAddress of the static scratch array failed";
+        return rc;
+    }
+    const uint64_t N = static_scratch_paths();
+    const uint64_t S = (uint64_t)args.params.spp;
+    if (S > N) {
+        err = "spp " + std::to_string(S) + " exceeds the " + std::to_string(N) +
+              " paths the static scratch holds per wave";
+        return GBPT_ERR_INVALID;
+    }
+    if (args.pixel_count > kStaticMaxPixelList && pixels_host) {
+        err = "pixel list longer than " + std::to_string(kStaticMaxPixelList) + " entries";
+        return GBPT_ERR_INVALID;
+    }
+    // carve the work buffers: counters, pixel list, then per-path and per-pixel arrays
+    Work w;
+    w.fixed = true;
+    w.path_cap = N;
+    w.pixel_cap = N;
+    unsigned char* p = base;
+    w.counters = (uint32_t*)p;
+    w.stats = (unsigned long long*)(p + 64);
+    p += kStaticCounterBytes;
+    uint32_t* pix_ids = (uint32_t*)p;
+    p += kStaticPixelBytes;
+    auto carve = [&](auto*& ptr, uint64_t count) {
+        using T = std::remove_reference_t<decltype(*ptr)>;
+        ptr = (T*)p;
+        p += (count * sizeof(T) + 255) & ~255ull;
+    };
+    carve(w.thr, N);
+    carve(w.rad, N);
+    carve(w.rng, N);
+    carve(w.q_od[0], 2 * N);
+    carve(w.q_od[1], 2 * N);
+    carve(w.q_path[0], N);
+    carve(w.q_path[1], N);
+    carve(w.hit_tuv, N);
+    carve(w.hit_geom, N);
+    carve(w.s_od, 2 * N);
+    carve(w.s_contrib, N);
+    carve(w.s_path, N);
+    carve(w.pix, 6 * N);
+    if ((uint64_t)(p - base) > kStaticScratchBytes) {
+        err = "static scratch layout overflow";
+        return GBPT_ERR_INVALID;
+    }
+    if (cudaMemsetAsync(w.counters, 0, kStaticCounterBytes, st) != cudaSuccess) {
+        err = "cudaMemsetAsync failed";
+        return GBPT_ERR_CUDA;
+    }
+    RenderArgs a = args;
+    if (pixels_host && args.pixel_count) {
+        if (cudaMemcpyAsync(pix_ids, pixels_host, (size_t)args.pixel_count * 4,
+                            cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            err = "cudaMemcpyAsync of the pixel list failed";
+            return GBPT_ERR_CUDA;
+        }
+        a.pixels_device = pix_ids;
+    } else {
+        a.pixels_device = nullptr;
+    }
+    rc = render_frame(scene, w, a, st, nullptr, nullptr, nullptr);
+    if (rc != GBPT_OK) {
+        err = "render launch failed";
+        return rc;
+    }
+    uint32_t flag = 0;
+    if (cudaMemcpyAsync(&flag, w.counters + 3, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        err = "synchronisation failed";
+        return GBPT_ERR_CUDA;
+    }
+    if (flag) {
+        err = "kernel error flag raised (traversal stack overflow)";
+        return GBPT_ERR_DEVICE;
+    }
+    return GBPT_OK;
 }
 
 int trace_primary(const SceneGPU& scene, const gbpt_camera& cam, uint32_t w, uint32_t h,

@@ -42,6 +42,9 @@ struct SceneGPU {
 struct Work {
     uint64_t path_cap = 0;  // paths per wave
     uint64_t pixel_cap = 0; // pixels per wave
+    // true when the buffers are carved from memory the Work does not own: they are never grown
+    // or freed, and a wave never exceeds path_cap
+    bool fixed = false;
     // path state (SoA, indexed by wave-local path id)
     float4* thr = nullptr;  // throughput rgb, current IOR
     float4* rad = nullptr;  // radiance rgb, pdf of the last BSDF sample
@@ -95,6 +98,13 @@ int render_frame(const SceneGPU& scene, Work& work, const RenderArgs& args, cuda
                  uint64_t* launches, Profile* prof, unsigned long long* work_ctr);
 int primary_points(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
                    float* out_device);
+
+// Rendering from the library's fixed scratch array (kernels.cu): no allocation, synchronous.
+constexpr uint64_t kStaticScratchBytes = 64ull << 20;
+constexpr uint32_t kStaticMaxPixelList = 1u << 16;
+uint64_t static_scratch_paths();
+int render_frame_static(const SceneGPU& scene, const RenderArgs& args, const uint32_t* pixels_host,
+                        cudaStream_t stream, std::string& err);
 int trace_rays(const SceneGPU& scene, const gbpt_ray* rays, uint32_t n, uint32_t mask, int any_hit,
                gbpt_hit* hits, unsigned long long* counters_device, cudaStream_t stream);
 int trace_primary(const SceneGPU& scene, const gbpt_camera& cam, uint32_t w, uint32_t h,
