@@ -37,12 +37,16 @@ L2_FLUSH_BYTES = 256 << 20
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--warmup", type=int, default=None)
     ap.add_argument("--impl", default="gbpt", choices=["gbpt", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # the mixed workloads (--workload batch-256 | served-stream)
+    ap.add_argument("--scenes", type=int, default=None, help="scenes of a mixed workload")
+    ap.add_argument("--requests", type=int, default=96, help="requests per served-stream rate")
+    ap.add_argument("--rates", default="50,200,2000", help="served-stream arrival rates, req/s")
     return ap.parse_args()
 
 
@@ -349,6 +353,7 @@ def run_gbpt(args):
                          "nodes_per_ray": round(nodes_per_ray, 3),
                          "tris_per_ray": round(tris_per_ray, 3),
                          "launches_per_step": trace_launches // max(args.steps, 1),
+                         "trace_rays_per_step": trace_rays // max(args.steps, 1),
                          "trace_share_of_step": round(trace_ms / args.steps / ms, 4)},
         }
         if world == 1 and not args.no_cpu_baseline:
@@ -360,10 +365,216 @@ def run_gbpt(args):
         dist.destroy_process_group()
 
 
+def _flush_l2(torch, buf):
+    buf.zero_()
+    torch.cuda.synchronize()
+
+
+def run_batch_mix(args):
+    """Config 3: independent scenes (triangles log-uniform 1k-2M), one request each, rendered
+    by plain per-request gbpt_render_device launches and by one gbpt_render_batch call (with and
+    without CUDA-graph replay of the ticks). All outputs stay in HBM; the outputs of both paths
+    are compared bit for bit."""
+    import torch
+    from merian_gb300 import _native as N
+    from merian_gb300 import scene as S
+    from merian_gb300 import workloads as WL
+    torch.cuda.set_device(0)
+    n = args.scenes or 256
+    specs, reqs = WL.batch_mix(S.BASE_SEED, n)
+    stream = torch.cuda.current_stream()
+    ctx = S.Context(0, stream.cuda_stream)
+    t0 = time.perf_counter()
+    sids = WL.upload_all(ctx, specs)
+    setup_s = time.perf_counter() - t0
+    jobs, out_plain, out_batch = [], [], []
+    for r in reqs:
+        kind = specs[r.scene].kind
+        jobs.append((sids[r.scene], WL.camera(kind, r.width, r.height), WL.params(kind, r)))
+        out_plain.append(torch.empty((r.width * r.height, 4), device="cuda"))
+        out_batch.append(torch.empty((r.width * r.height, 4), device="cuda"))
+    samples = sum(r.width * r.height * r.spp for r in reqs)
+    creqs = (N.Request * n)()
+    for i, (sid, cam, p) in enumerate(jobs):
+        creqs[i] = ctx.request(sid, cam, p, out_device=out_batch[i].data_ptr())
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def plain():
+        for (sid, cam, p), o in zip(jobs, out_plain):
+            ctx.render_device(sid, cam, p, o.data_ptr())
+
+    def batched():
+        N.check(ctx.lib.gbpt_render_batch(ctx.handle, creqs, n, None))
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(args.steps):
+            _flush_l2(torch, flush)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.mean(ts))
+
+    with ClockSampler(0) as clk:
+        ms_plain = timed(plain)
+        ms_batch = timed(batched)
+        ctx.set_graphs(True)
+        ms_graph = timed(batched)
+        ctx.set_graphs(False)
+    identical = all(torch.equal(a.view(torch.int32), b.view(torch.int32))
+                    for a, b in zip(out_plain, out_batch))
+    mps = lambda ms: round(samples / (ms / 1e3) / 1e6, 3)
+    best = min(ms_batch, ms_graph)
+    line = {
+        "metric": "Msamples/s of a request batch: one tick engine for all requests vs plain "
+                  "per-request launches (same outputs, bit for bit)",
+        "workload": "batch-256", "value": mps(best), "unit": "Msamples/s",
+        "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(best, 3), "dtype": "f32", "data": "synthetic",
+        "plain": {"value": mps(ms_plain), "ms_per_step": round(ms_plain, 3)},
+        "batched": {"value": mps(ms_batch), "ms_per_step": round(ms_batch, 3)},
+        "batched_graphs": {"value": mps(ms_graph), "ms_per_step": round(ms_graph, 3)},
+        "speedup_vs_plain": round(ms_plain / best, 3),
+        "outputs_identical": identical,
+        "clocks": clk.summary(),
+        "config": {"workload": "batch-256", "scenes": n, "requests": n,
+                   "triangles_total": sum(s.triangles for s in specs),
+                   "cornell_scenes": sum(s.kind == "cornell" for s in specs),
+                   "samples_per_step": samples,
+                   "resolutions": "256^2 / 512^2 / 1024^2", "spp": "uniform 1..64",
+                   "estimator": "NEE + RR from 3; path length 5 (Cornell) / 8 (soup)",
+                   "scene_setup_s": round(setup_s, 1),
+                   "l2": "flushed between timed steps (256 MiB write)"},
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def _percentile(xs, q):
+    return float(np.percentile(np.asarray(xs), q)) if xs else None
+
+
+def run_served(args):
+    """Config 4: Poisson arrivals over resident scenes (triangles log-uniform 10k-5M), 5 % of
+    requests bringing a new 100k-triangle scene; each rate is served by the request server
+    (continuous batching) and, with the same arrivals, by a serial queue of plain gbpt_render
+    calls. Latency = completion - scheduled arrival; outputs go to host memory."""
+    import torch
+    from merian_gb300 import _native as N
+    from merian_gb300 import scene as S
+    from merian_gb300 import workloads as WL
+    torch.cuda.set_device(0)
+    n_scenes = args.scenes or 32
+    rates = [float(x) for x in args.rates.split(",") if x]
+    specs, _ = WL.served_stream(S.BASE_SEED, n_scenes, 0)
+    ctx = S.Context(0)
+    t0 = time.perf_counter()
+    sids = WL.upload_all(ctx, specs)
+    setup_s = time.perf_counter() - t0
+    results = []
+
+    def prepare(rate):
+        _, reqs = WL.served_stream(S.BASE_SEED, n_scenes, args.requests, rate)
+        new_scenes = {i: r.upload.build() for i, r in enumerate(reqs) if r.upload}
+        return reqs, new_scenes
+
+    def job(r, sid):
+        kind = "soup" if r.upload else specs[r.scene].kind
+        return sid, WL.camera(kind, r.width, r.height), WL.params(kind, r)
+
+    with ClockSampler(0) as clk:
+        for rate in rates:
+            reqs, new_scenes = prepare(rate)
+            samples = sum(r.width * r.height * r.spp for r in reqs)
+            row = {"rate_req_s": rate, "requests": len(reqs),
+                   "uploads": len(new_scenes), "samples": samples}
+            for mode in ("served", "plain"):
+                outs = [np.empty((r.width * r.height, 4), np.float32) for r in reqs]
+                made = []
+                lat = [None] * len(reqs)
+                if mode == "served":
+                    ctx.server_start()
+                start = ctx.clock() + 0.05
+                tickets = [None] * len(reqs)
+                for i, r in enumerate(reqs):
+                    delay = start + r.arrival_s - ctx.clock()
+                    if delay > 0:
+                        time.sleep(delay)
+                    sid = sids[r.scene]
+                    if r.upload:
+                        sid = ctx.upload(new_scenes[i])
+                        made.append(sid)
+                    sid, cam, p = job(r, sid)
+                    if mode == "served":
+                        tickets[i] = ctx.submit(sid, cam, p, out_host=outs[i])
+                    else:
+                        N.check(ctx.lib.gbpt_render(ctx.handle, sid, N.C.byref(cam),
+                                                    N.C.byref(p), N.ptr(outs[i]), None))
+                        lat[i] = ctx.clock() - (start + r.arrival_s)
+                end = ctx.clock()
+                if mode == "served":
+                    for i, t in enumerate(tickets):
+                        rc, st = ctx.wait(t, -1.0)
+                        if rc != 0:
+                            raise RuntimeError(f"served request {i} failed: {rc}")
+                        lat[i] = st.done_s - (start + reqs[i].arrival_s)
+                        end = max(end, st.done_s)
+                    info = ctx.server_info()
+                    ctx.server_stop()
+                for sid in made:
+                    ctx.destroy_scene(sid)
+                span = end - start
+                row[mode] = {"p50_ms": round(1e3 * _percentile(lat, 50), 1),
+                             "p99_ms": round(1e3 * _percentile(lat, 99), 1),
+                             "mean_ms": round(1e3 * float(np.mean(lat)), 1),
+                             "makespan_s": round(span, 3),
+                             "msamples_per_s": round(samples / span / 1e6, 3)}
+                if mode == "served":
+                    row[mode]["ticks"] = info["ticks"]
+            row["throughput_ratio"] = round(row["served"]["msamples_per_s"] /
+                                            row["plain"]["msamples_per_s"], 3)
+            results.append(row)
+    best = max(results, key=lambda r: r["served"]["msamples_per_s"])
+    line = {
+        "metric": "served p50/p99 latency and Msamples/s: request server (continuous batching) "
+                  "vs a serial queue of plain gbpt_render calls, same arrivals",
+        "workload": "served-stream", "value": best["served"]["msamples_per_s"],
+        "unit": "Msamples/s", "higher_is_better": True, "n_gpus": 1, "dtype": "f32",
+        "data": "synthetic", "rates": results, "clocks": clk.summary(),
+        "config": {"workload": "served-stream", "resident_scenes": n_scenes,
+                   "triangles_resident": sum(s.triangles for s in specs),
+                   "requests_per_rate": args.requests,
+                   "resolutions": "512^2 / 1024^2 / 1920x1080", "spp": "1 / 4 / 16 / 64",
+                   "uploads": "5 % of requests bring a new 100k-triangle soup (BVH build + "
+                              "upload inside the request's latency)",
+                   "estimator": "NEE + RR from 3; path length 5 (Cornell) / 8 (soup)",
+                   "scene_setup_s": round(setup_s, 1)},
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
+    mixed = args.workload in ("batch-256", "served-stream")
+    if args.steps is None:
+        args.steps = 1 if mixed else 5
+    if args.warmup is None:
+        args.warmup = 1 if mixed else 3
     if args.impl == "reference":
+        if mixed:  # the CPU reference is timed on the headline frame only
+            args.workload = WORKLOAD
         run_reference(args)
+    elif args.workload == "batch-256":
+        run_batch_mix(args)
+    elif args.workload == "served-stream":
+        run_served(args)
     else:
         run_gbpt(args)
 

@@ -199,6 +199,24 @@ typedef struct gbpt_hit {
     uint32_t reserved;
 } gbpt_hit;
 
+/* One texel of the GBuffer (Raytraced) node's outputs (gbuffer.slang:71-85 textures tex0..tex3,
+ * plus gbuffer_rt.slang's emission output), 64 bytes. */
+typedef struct gbpt_gbuffer_texel {
+    uint32_t encoded_normal; /* tex0.x: shading normal, oct-encoded (encoding.slang:6-30) */
+    uint32_t grad_z;         /* tex0.y: half2 depth change per pixel step in x and y */
+    uint32_t instance_id;    /* tex1: PackedHitInfo (misses: all ids 0xFFFF...) */
+    uint32_t primitive_id;
+    uint16_t geometry_index;
+    uint16_t instance_index;
+    uint32_t barycentrics;   /* half2 */
+    float motion[2];         /* tex2.xy: pixel-space motion vector */
+    float linear_z;          /* tex2.z: |position - camera|, at most 65504 */
+    float delta_z;           /* tex2.w */
+    float albedo[3];         /* tex3.rgb: the BSDF's albedo toward the camera; on a miss the
+                                environment radiance */
+    float emission[3];       /* emitted radiance toward the camera */
+} gbpt_gbuffer_texel;
+
 /* A ray in device memory: origin, tmin, direction, tmax (two float4). */
 typedef struct gbpt_ray {
     float origin[3];
@@ -263,6 +281,109 @@ GBPT_API int gbpt_render_device(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera
 GBPT_API int gbpt_render_device_noalloc(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
                                         const gbpt_render_params* params, float* out_rgba_device);
 
+/* ---- batches and the request server ------------------------------------------------------
+ * merian renders one request per graph iteration (Graph::run_node -> RenderPT::process,
+ * graph.cpp:323-360); these calls have no counterpart there. They render many requests whose
+ * paths share the wavefront's ticks (up to 8 Mi paths of whole pixels from up to 256 requests
+ * per tick), so small requests fill the GPU together. Every result equals, bit for bit, what
+ * gbpt_render / gbpt_render_device return for the request alone. */
+
+/* One request: a scene, a camera, the node parameters (params.pixels is a host list, copied
+ * during the call) and exactly one output, host or device (RGBA32F, one texel per pixel or per
+ * listed pixel). */
+typedef struct gbpt_request {
+    uint32_t scene;
+    uint32_t reserved;
+    gbpt_camera camera;
+    gbpt_render_params params;
+    float* out_host;
+    float* out_device;
+} gbpt_request;
+
+/* Renders n requests together and returns when every output is written. stats, when non-NULL,
+ * sums over the batch. */
+GBPT_API int gbpt_render_batch(gbpt_ctx* ctx, const gbpt_request* requests, uint32_t n,
+                               gbpt_render_stats* stats);
+/* gbpt_render_batch replays each tick from a captured CUDA graph (one per path length and
+ * estimator) when enabled (1), or launches the kernels one by one (0, the default). */
+GBPT_API int gbpt_set_graphs(gbpt_ctx* ctx, int enable);
+
+/* The request server: one host thread per context admits submitted requests in arrival order
+ * while their outputs fit a device arena reserved from free HBM at start, and renders the
+ * admitted ones together, one tick after another (continuous batching: a request submitted while
+ * others run joins the next tick). Scenes stay resident; a scene used by a queued or running
+ * request cannot be destroyed (GBPT_ERR_BUSY). */
+typedef struct gbpt_server_config {
+    uint64_t wave_paths;  /* paths per tick; 0 = 8 Mi (at most 2^24) */
+    uint64_t arena_bytes; /* device arena for host-output staging and pixel lists;
+                             0 = a quarter of the free HBM, at most 16 GiB */
+    int32_t use_graphs;   /* replay ticks from captured CUDA graphs */
+    uint32_t max_active;  /* requests admitted at once; 0 = 1024 */
+} gbpt_server_config;
+
+#define GBPT_REQ_QUEUED 0
+#define GBPT_REQ_RUNNING 1
+#define GBPT_REQ_DONE 2
+#define GBPT_REQ_CANCELLED 3
+#define GBPT_REQ_FAILED 4
+
+typedef struct gbpt_request_status {
+    int32_t state;   /* GBPT_REQ_* */
+    int32_t error;   /* status code of a failed request */
+    double submit_s; /* gbpt_clock() at submission, admission and completion */
+    double admit_s;
+    double done_s;
+    uint64_t samples; /* pixels x spp */
+} gbpt_request_status;
+
+typedef struct gbpt_server_stats {
+    uint64_t queued, active, completed;
+    uint64_t ticks, kernel_launches, paths;
+    uint64_t arena_bytes, wave_paths;
+} gbpt_server_stats;
+
+/* Seconds on the host's steady clock, the clock of gbpt_request_status. */
+GBPT_API double gbpt_clock(void);
+GBPT_API int gbpt_server_start(gbpt_ctx* ctx, const gbpt_server_config* config);
+/* Cancels queued requests, finishes admitted ones and joins the server thread. */
+GBPT_API int gbpt_server_stop(gbpt_ctx* ctx);
+/* Queues a request; the caller keeps out_host / out_device valid until it has finished. */
+GBPT_API int gbpt_server_submit(gbpt_ctx* ctx, const gbpt_request* request, uint64_t* ticket);
+/* GBPT_OK when done, GBPT_ERR_BUSY while queued or running, GBPT_ERR_CANCELLED, or the error of a
+ * failed request; status (optional) receives its state and timestamps. */
+GBPT_API int gbpt_server_poll(gbpt_ctx* ctx, uint64_t ticket, gbpt_request_status* status);
+/* As poll, after waiting up to timeout_s seconds (negative: without limit) for the request. */
+GBPT_API int gbpt_server_wait(gbpt_ctx* ctx, uint64_t ticket, double timeout_s,
+                              gbpt_request_status* status);
+/* A queued request is dropped at once; a running one stops at the next tick boundary. */
+GBPT_API int gbpt_server_cancel(gbpt_ctx* ctx, uint64_t ticket);
+/* Forgets a finished request's record. */
+GBPT_API int gbpt_server_release(gbpt_ctx* ctx, uint64_t ticket);
+GBPT_API int gbpt_server_info(gbpt_ctx* ctx, gbpt_server_stats* stats);
+
+/* ---- the nodes either side of the renderer ------------------------------------------------
+ * Accumulate (accumulate.slang:233-257, static camera): per texel, when history > 0 and the
+ * previous output is finite, n = min(history + 1, max_history), a = max(1 - alpha, 1/n),
+ * out = out + a * (src - out), history = n; otherwise out = src, history = 1. With alpha = 1
+ * and max_history = INFINITY (merian's gltf.json settings) out is the running mean of the
+ * frames. RGBA32F device buffers of `texels` texels; history is one float per texel (zero, or
+ * clear = 1, restarts). Enqueued on the context stream. */
+GBPT_API int gbpt_accumulate(gbpt_ctx* ctx, const float* src_device, float* out_device,
+                             float* history_device, uint64_t texels, float alpha,
+                             float max_history, int clear);
+/* Error Plot (error_to_buffer.slang): out8[0..3] = mean over texels of (reference - input)^2
+ * per RGBA channel (MSE), out8[4..7] = mean |reference - input| (MAE), summed in double in a
+ * fixed order. Synchronous. */
+GBPT_API int gbpt_error_metrics(gbpt_ctx* ctx, const float* reference_device,
+                                const float* input_device, uint64_t texels, double* out8);
+/* Image Write / Image Read of PFM files (image_io.cpp:53-176): channels 1, 3 or 4 (RGBA is
+ * written as RGB), top row first in memory, bottom row first in the file. gbpt_image_read_pfm
+ * with texels = NULL returns the size only. Host only. */
+GBPT_API int gbpt_image_write_pfm(const char* path, const float* texels, uint32_t width,
+                                  uint32_t height, uint32_t channels);
+GBPT_API int gbpt_image_read_pfm(const char* path, float* texels, uint32_t channels,
+                                 uint32_t* width, uint32_t* height);
+
 /* ---- traversal queries (the GBuffer node's primary hit, and raw ray queries) ---------------
  * gbpt_trace_primary: the hit merian's GBuffer (Raytraced) node stores for each pixel
  * (gbuffer_rt.slang:18-58) with full-precision barycentrics and t, written to a host array of
@@ -271,6 +392,12 @@ GBPT_API int gbpt_render_device_noalloc(gbpt_ctx* ctx, uint32_t scene, const gbp
 GBPT_API int gbpt_trace_primary(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
                                 uint32_t width, uint32_t height, uint32_t instance_mask,
                                 gbpt_hit* out_hits_host);
+/* The GBuffer (Raytraced) node (gbuffer_rt.slang:18-94) on the same traversal: width*height
+ * gbpt_gbuffer_texel in DEVICE memory, row-major, enqueued on the context stream. The camera is
+ * static: motion vectors are 0. The albedo is what "demodulate albedo" divides out. */
+GBPT_API int gbpt_gbuffer(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
+                          uint32_t width, uint32_t height, uint32_t instance_mask,
+                          gbpt_gbuffer_texel* out_device);
 GBPT_API int gbpt_trace(gbpt_ctx* ctx, uint32_t scene, const gbpt_ray* rays_device, uint32_t n,
                         uint32_t instance_mask, int any_hit, gbpt_hit* hits_device);
 /* Average CWBVH nodes visited and triangles tested per ray of the last gbpt_trace call made with
@@ -318,6 +445,11 @@ GBPT_API uint32_t gbpt_pack_half2(float x, float y);
  * Env: width x height RGBA32F sum of 8 Gaussian lobes. */
 GBPT_API int gbpt_gen_cornell(uint64_t seed, gbpt_packed_vertex* vertices, uint32_t* indices,
                               gbpt_geometry* geometries, gbpt_material* materials);
+/* The same box with every grid refined tess times per side: 1024 tess^2 triangles, 3 vertices per
+ * triangle, 8 geometries and materials (tess in [1, 64]; tess = 1 is gbpt_gen_cornell). */
+GBPT_API int gbpt_gen_cornell_tess(uint64_t seed, uint32_t tess, gbpt_packed_vertex* vertices,
+                                   uint32_t* indices, gbpt_geometry* geometries,
+                                   gbpt_material* materials);
 GBPT_API int gbpt_gen_soup(uint64_t seed, uint32_t n_triangles, uint32_t n_geometries,
                            gbpt_packed_vertex* vertices, uint32_t* indices,
                            gbpt_geometry* geometries, gbpt_material* materials);

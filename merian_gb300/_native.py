@@ -6,6 +6,7 @@ the array types so scenes can be built and passed without copies.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
@@ -47,6 +48,12 @@ HIT_DTYPE = np.dtype([("instance_id", "<u4"), ("instance_index", "<u4"), ("primi
                       ("reserved", "<u4")])
 RAY_DTYPE = np.dtype([("origin", "<f4", 3), ("tmin", "<f4"), ("direction", "<f4", 3),
                       ("tmax", "<f4")])
+GBUFFER_DTYPE = np.dtype([("encoded_normal", "<u4"), ("grad_z", "<u4"), ("instance_id", "<u4"),
+                          ("primitive_id", "<u4"), ("geometry_index", "<u2"),
+                          ("instance_index", "<u2"), ("barycentrics", "<u4"),
+                          ("motion", "<f4", 2), ("linear_z", "<f4"), ("delta_z", "<f4"),
+                          ("albedo", "<f4", 3), ("emission", "<f4", 3)])
+assert GBUFFER_DTYPE.itemsize == 64
 assert VERTEX_DTYPE.itemsize == 24 and GEOMETRY_DTYPE.itemsize == 24
 assert MATERIAL_DTYPE.itemsize == 80 and HIT_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 32
 
@@ -95,8 +102,54 @@ class SceneDesc(C.Structure):
                 ("instance_count", C.c_uint32)]
 
 
+class Request(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("reserved", C.c_uint32), ("camera", Camera),
+                ("params", RenderParams), ("out_host", C.c_void_p), ("out_device", C.c_void_p)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("wave_paths", C.c_uint64), ("arena_bytes", C.c_uint64),
+                ("use_graphs", C.c_int32), ("max_active", C.c_uint32)]
+
+
+class RequestStatus(C.Structure):
+    _fields_ = [("state", C.c_int32), ("error", C.c_int32), ("submit_s", C.c_double),
+                ("admit_s", C.c_double), ("done_s", C.c_double), ("samples", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("queued", C.c_uint64), ("active", C.c_uint64), ("completed", C.c_uint64),
+                ("ticks", C.c_uint64), ("kernel_launches", C.c_uint64), ("paths", C.c_uint64),
+                ("arena_bytes", C.c_uint64), ("wave_paths", C.c_uint64)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
+
 # (name, restype, argtypes) of every exported entry point declared in include/gbpt.h
 EXPORTS = [
+    ("gbpt_render_batch", C.c_int, [C.c_void_p, C.POINTER(Request), C.c_uint32,
+                                    C.POINTER(RenderStats)]),
+    ("gbpt_set_graphs", C.c_int, [C.c_void_p, C.c_int]),
+    ("gbpt_clock", C.c_double, []),
+    ("gbpt_server_start", C.c_int, [C.c_void_p, C.POINTER(ServerConfig)]),
+    ("gbpt_server_stop", C.c_int, [C.c_void_p]),
+    ("gbpt_server_submit", C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+    ("gbpt_server_poll", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(RequestStatus)]),
+    ("gbpt_server_wait", C.c_int, [C.c_void_p, C.c_uint64, C.c_double,
+                                   C.POINTER(RequestStatus)]),
+    ("gbpt_server_cancel", C.c_int, [C.c_void_p, C.c_uint64]),
+    ("gbpt_server_release", C.c_int, [C.c_void_p, C.c_uint64]),
+    ("gbpt_server_info", C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    ("gbpt_gbuffer", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.c_uint32, C.c_uint32,
+                               C.c_uint32, C.c_void_p]),
+    ("gbpt_accumulate", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64,
+                                  C.c_float, C.c_float, C.c_int]),
+    ("gbpt_error_metrics", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64,
+                                     C.POINTER(C.c_double)]),
+    ("gbpt_image_write_pfm", C.c_int, [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                       C.c_uint32]),
+    ("gbpt_image_read_pfm", C.c_int, [C.c_char_p, C.c_void_p, C.c_uint32,
+                                      C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     ("gbpt_abi_version", C.c_uint32, []),
     ("gbpt_last_error", C.c_char_p, []),
     ("gbpt_create", C.c_int, [C.c_int, C.c_uint64, C.POINTER(C.c_void_p)]),
@@ -138,6 +191,8 @@ EXPORTS = [
     ("gbpt_encode_normal", C.c_uint32, [C.POINTER(C.c_float)]),
     ("gbpt_pack_half2", C.c_uint32, [C.c_float, C.c_float]),
     ("gbpt_gen_cornell", C.c_int, [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("gbpt_gen_cornell_tess", C.c_int, [C.c_uint64, C.c_uint32, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p]),
     ("gbpt_gen_soup", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                                 C.c_void_p, C.c_void_p]),
     ("gbpt_gen_env", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p]),
@@ -157,7 +212,8 @@ def load(path: Path | str | None = None) -> C.CDLL:
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = Path(path) if path else LIB_PATH
+    # GBPT_LIBRARY selects another build of the library (a tuning variant)
+    p = Path(path) if path else Path(os.environ.get("GBPT_LIBRARY", LIB_PATH))
     if not p.exists():
         raise RuntimeError(f"{p} is missing: build it with `python -m merian_gb300.build` "
                            "(the path tracer has no CPU fallback)")

@@ -20,8 +20,8 @@ INCLUDE = ROOT / "include"
 BUILD = HERE / "_build"
 LIB = HERE / "libgbpt.so"
 
-CUDA_SOURCES = ["kernels.cu", "debug_kernels.cu"]
-HOST_SOURCES = ["api.cpp", "bvh.cpp", "scenegen.cpp"]
+CUDA_SOURCES = ["wavefront.cu", "kernels.cu", "nodes.cu", "debug_kernels.cu"]
+HOST_SOURCES = ["api.cpp", "server.cpp", "bvh.cpp", "scenegen.cpp", "image_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -50,8 +50,13 @@ def _stale(target: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) -> Path:
+def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False,
+          defines: tuple[str, ...] = (), lib: Path = LIB, build_dir: Path = BUILD) -> Path:
+    """Compiles the library. `defines` (NAME=VALUE) override the kernels' tuning constants; a
+    variant goes to its own `lib` and `build_dir`."""
     cuda = _cuda_home()
+    BUILD = Path(build_dir)
+    LIB = Path(lib)
     nvcc = str(cuda / "bin" / "nvcc")
     cxx = os.environ.get("CXX", "g++")
     BUILD.mkdir(parents=True, exist_ok=True)
@@ -63,6 +68,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         objs.append(obj)
         if force or _stale(obj, [CSRC / src] + headers):
             cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                   *[f"-D{d}" for d in defines],
                    "-Xcompiler", "-fvisibility=hidden", "-I", str(INCLUDE), "-I", str(CSRC),
                    "-c", str(CSRC / src), "-o", str(obj)]
             if ptxas_info:

@@ -1,5 +1,7 @@
-// C ABI of the GB300 path tracer (declared in include/gbpt.h): context, scene upload, render and
-// traversal queries. Host-only C++ on the CUDA runtime; the kernels live in kernels.cu.
+// C ABI of the GB300 path tracer (declared in include/gbpt.h): context, scene upload, render,
+// batches and traversal queries. Host-only C++ on the CUDA runtime; the kernels live in
+// wavefront.cu and kernels.cu, the request server in server.cpp.
+#include "context.h"
 #include "gbpt.h"
 #include "host_common.h"
 #include "runtime.h"
@@ -26,35 +28,29 @@ struct GeomHost {
 };
 static_assert(sizeof(GeomHost) == 16, "GeomGPU layout");
 
+int check_ctx(gbpt_ctx* ctx) {
+    if (!ctx) {
+        set_error("null context");
+        return GBPT_ERR_INVALID;
+    }
+    const cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+        return GBPT_ERR_CUDA;
+    }
+    return GBPT_OK;
+}
+
+double host_clock() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
 } // namespace gbpt
 
 using namespace gbpt;
 
-struct gbpt_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    std::mutex mu;
-    std::map<uint32_t, SceneGPU> scenes;
-    uint32_t next_scene = 1;
-    Work work;
-    unsigned long long* d_misc = nullptr; // [0] nodes, [1] tris, [2] error word
-    gbpt_hit* d_hits = nullptr;
-    uint64_t hits_cap = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    Profile prof;
-};
-
 namespace {
-
-#define GBPT_CUDA_CHECK(call)                                                                      \
-    do {                                                                                           \
-        const cudaError_t e_ = (call);                                                             \
-        if (e_ != cudaSuccess) {                                                                   \
-            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                         \
-            return e_ == cudaErrorMemoryAllocation ? GBPT_ERR_NO_MEMORY : GBPT_ERR_CUDA;           \
-        }                                                                                          \
-    } while (0)
 
 int upload(void** dst, const void* src, size_t bytes, uint64_t& total) {
     if (bytes == 0) {
@@ -79,19 +75,6 @@ void free_scene(SceneGPU& s) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     s = SceneGPU{};
-}
-
-int check_ctx(gbpt_ctx* ctx) {
-    if (!ctx) {
-        set_error("null context");
-        return GBPT_ERR_INVALID;
-    }
-    const cudaError_t e = cudaSetDevice(ctx->device);
-    if (e != cudaSuccess) {
-        set_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
-        return GBPT_ERR_CUDA;
-    }
-    return GBPT_OK;
 }
 
 // Reads and clears the kernels' error word; returns GBPT_ERR_DEVICE when it was set.
@@ -160,8 +143,10 @@ GBPT_API int gbpt_create(int device, uint64_t stream, gbpt_ctx** out_ctx) {
 GBPT_API int gbpt_destroy(gbpt_ctx* ctx) {
     if (!ctx) return GBPT_OK;
     cudaSetDevice(ctx->device);
+    server_shutdown(ctx->server);
     cudaStreamSynchronize(ctx->stream);
     for (auto& kv : ctx->scenes) free_scene(kv.second);
+    ctx->batch.release();
     work_free(ctx->work);
     ctx->prof.destroy();
     if (ctx->d_misc) cudaFree(ctx->d_misc);
@@ -423,6 +408,11 @@ GBPT_API int gbpt_scene_destroy(gbpt_ctx* ctx, uint32_t scene) {
         set_error("gbpt_scene_destroy: unknown scene id");
         return GBPT_ERR_NOT_FOUND;
     }
+    auto users = ctx->scene_users.find(scene);
+    if (users != ctx->scene_users.end() && users->second > 0) {
+        set_error("gbpt_scene_destroy: the scene is used by queued or running server requests");
+        return GBPT_ERR_BUSY;
+    }
     GBPT_CUDA_CHECK(cudaStreamSynchronize(ctx->stream)); // work in flight may still read it
     free_scene(it->second);
     ctx->scenes.erase(it);
@@ -446,7 +436,9 @@ GBPT_API int gbpt_scene_stats(gbpt_ctx* ctx, uint32_t scene, uint64_t* nodes, ui
     return GBPT_OK;
 }
 
-static int validate_params(const gbpt_camera* cam, const gbpt_render_params* p) {
+} // extern "C"
+
+int gbpt::validate_params(const gbpt_camera* cam, const gbpt_render_params* p) {
     if (!cam || !p) {
         set_error("null camera or params");
         return GBPT_ERR_INVALID;
@@ -471,6 +463,11 @@ static int validate_params(const gbpt_camera* cam, const gbpt_render_params* p) 
     }
     return GBPT_OK;
 }
+
+extern "C" {
+
+static int read_stats(gbpt_ctx* ctx, uint64_t samples, uint64_t launches, Profile* prof,
+                      gbpt_render_stats* stats);
 
 static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
                        const gbpt_render_params* p, float* out_dev, float* out_host,
@@ -541,14 +538,23 @@ static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
     if (stats || out_host) {
         if ((rc = check_device_error(ctx))) return rc;
     }
-    if (stats) {
+    if (stats) return read_stats(ctx, (uint64_t)n_pix * (uint64_t)p->spp, launches, prof, stats);
+    return GBPT_OK;
+}
+
+// Fills stats after a synchronised render: device counters, the event pair ev0/ev1 and, when
+// profiling, the per-class kernel times.
+static int read_stats(gbpt_ctx* ctx, uint64_t samples, uint64_t launches, Profile* prof,
+                      gbpt_render_stats* stats) {
+    Work& w = ctx->work;
+    {
         unsigned long long st[3] = {0, 0, 0}, wk[2] = {0, 0};
         GBPT_CUDA_CHECK(cudaMemcpy(st, w.stats, sizeof(st), cudaMemcpyDeviceToHost));
         GBPT_CUDA_CHECK(cudaMemcpy(wk, ctx->d_misc, sizeof(wk), cudaMemcpyDeviceToHost));
         float ms = 0.f;
         GBPT_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
         std::memset(stats, 0, sizeof(*stats));
-        stats->samples = (uint64_t)n_pix * (uint64_t)p->spp;
+        stats->samples = samples;
         stats->rays = st[0];
         stats->shadow_rays = st[1];
         stats->trace_rays = st[2];
@@ -628,6 +634,117 @@ GBPT_API int gbpt_render_device_noalloc(gbpt_ctx* ctx, uint32_t scene, const gbp
     rc = render_frame_static(it->second, a, p->pixel_count ? p->pixels : nullptr, ctx->stream, err);
     if (rc != GBPT_OK) set_error("gbpt_render_device_noalloc: " + err);
     return rc;
+}
+
+// Many requests through the context's tick engine: their paths share ticks.
+GBPT_API int gbpt_render_batch(gbpt_ctx* ctx, const gbpt_request* reqs, uint32_t n,
+                               gbpt_render_stats* stats) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (n && !reqs) {
+        set_error("gbpt_render_batch: null request array");
+        return GBPT_ERR_INVALID;
+    }
+    uint64_t list_words = 0, host_texels = 0, samples = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        if ((rc = validate_params(&reqs[i].camera, &reqs[i].params))) return rc;
+        if (!reqs[i].out_host == !reqs[i].out_device) {
+            set_error("gbpt_render_batch: request " + std::to_string(i) +
+                      " needs exactly one of out_host and out_device");
+            return GBPT_ERR_INVALID;
+        }
+        const gbpt_render_params& p = reqs[i].params;
+        const uint64_t np = p.pixel_count ? p.pixel_count : (uint64_t)p.width * p.height;
+        list_words += p.pixel_count;
+        if (reqs[i].out_host) host_texels += np;
+        samples += np * (uint64_t)p.spp;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    std::vector<BatchItem> items(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        auto it = ctx->scenes.find(reqs[i].scene);
+        if (it == ctx->scenes.end()) {
+            set_error("gbpt_render_batch: request " + std::to_string(i) + ": unknown scene id");
+            return GBPT_ERR_NOT_FOUND;
+        }
+        items[i].scene = &it->second;
+    }
+    // pixel lists and host outputs go through the context's staging buffers
+    Work& w = ctx->work;
+    if (list_words > w.pix_id_cap) {
+        if (w.pix_id) cudaFree(w.pix_id);
+        w.pix_id = nullptr;
+        w.pix_id_cap = 0;
+        GBPT_CUDA_CHECK(cudaMalloc((void**)&w.pix_id, (size_t)list_words * 4));
+        w.pix_id_cap = list_words;
+    }
+    if (host_texels > w.out_cap) {
+        if (w.out) cudaFree(w.out);
+        w.out = nullptr;
+        w.out_cap = 0;
+        GBPT_CUDA_CHECK(cudaMalloc((void**)&w.out, (size_t)host_texels * sizeof(float4)));
+        w.out_cap = host_texels;
+    }
+    uint64_t list_at = 0, out_at = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const gbpt_render_params& p = reqs[i].params;
+        const uint32_t np = p.pixel_count ? p.pixel_count : p.width * p.height;
+        items[i].camera = reqs[i].camera;
+        items[i].params = reqs[i].params;
+        items[i].pixel_count = np;
+        items[i].pixels_device = nullptr;
+        if (p.pixel_count) {
+            GBPT_CUDA_CHECK(cudaMemcpyAsync(w.pix_id + list_at, p.pixels, (size_t)p.pixel_count * 4,
+                                            cudaMemcpyHostToDevice, ctx->stream));
+            items[i].pixels_device = w.pix_id + list_at;
+            list_at += p.pixel_count;
+        }
+        if (reqs[i].out_host) {
+            items[i].out_device = w.out + out_at;
+            out_at += np;
+        } else {
+            items[i].out_device = (float4*)reqs[i].out_device;
+        }
+        if (p.spp == 0)
+            GBPT_CUDA_CHECK(cudaMemsetAsync(items[i].out_device, 0, (size_t)np * sizeof(float4),
+                                            ctx->stream));
+    }
+    uint64_t launches = 0;
+    Profile* prof = stats && ctx->prof.level > 0 ? &ctx->prof : nullptr;
+    if (stats) {
+        GBPT_CUDA_CHECK(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
+        GBPT_CUDA_CHECK(cudaMemsetAsync(ctx->d_misc, 0, 2 * sizeof(unsigned long long), ctx->stream));
+        GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev0, ctx->stream));
+        if (prof) prof->reset();
+    }
+    ctx->batch.work = &w;
+    ctx->batch.stream = ctx->stream;
+    rc = render_batch(ctx->batch, items.data(), n, &launches, prof, ctx->d_misc);
+    if (rc != GBPT_OK) {
+        set_error(rc == GBPT_ERR_NO_MEMORY ? "gbpt_render_batch: work buffer allocation failed"
+                                           : "gbpt_render_batch: launch failed: " +
+                                                 cuda_error_string(cudaGetLastError()));
+        return rc;
+    }
+    if (stats) GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev1, ctx->stream));
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!reqs[i].out_host) continue;
+        GBPT_CUDA_CHECK(cudaMemcpyAsync(reqs[i].out_host, items[i].out_device,
+                                        (size_t)items[i].pixel_count * sizeof(float4),
+                                        cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if ((rc = check_device_error(ctx))) return rc;
+    if (stats) return read_stats(ctx, samples, launches, prof, stats);
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_set_graphs(gbpt_ctx* ctx, int enable) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->batch.use_graphs = enable != 0;
+    if (!enable) ctx->batch.release();
+    return GBPT_OK;
 }
 
 GBPT_API int gbpt_debug_primary_points(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
@@ -714,6 +831,28 @@ GBPT_API int gbpt_trace_primary(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera
     GBPT_CUDA_CHECK(cudaMemcpyAsync(out_hits_host, ctx->d_hits, n * sizeof(gbpt_hit),
                                     cudaMemcpyDeviceToHost, ctx->stream));
     return check_device_error(ctx);
+}
+
+GBPT_API int gbpt_gbuffer(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
+                          uint32_t width, uint32_t height, uint32_t instance_mask,
+                          gbpt_gbuffer_texel* out_device) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!camera || !out_device || width == 0 || height == 0 ||
+        (uint64_t)width * height > (1ull << 31)) {
+        set_error("gbpt_gbuffer: invalid arguments");
+        return GBPT_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) {
+        set_error("gbpt_gbuffer: unknown scene id");
+        return GBPT_ERR_NOT_FOUND;
+    }
+    rc = gbuffer(it->second, *camera, width, height, instance_mask, out_device,
+                 reinterpret_cast<uint32_t*>(ctx->d_misc + 2), ctx->stream);
+    if (rc) set_error("gbpt_gbuffer: launch failed");
+    return rc;
 }
 
 static int trace_common(gbpt_ctx* ctx, uint32_t scene, const gbpt_ray* rays, uint32_t n,

@@ -1,0 +1,63 @@
+// The context object behind the C ABI and the helpers its translation units share (api.cpp,
+// server.cpp). Host-only C++.
+#pragma once
+
+#include "gbpt.h"
+#include "runtime.h"
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+
+#include <cuda_runtime.h>
+
+namespace gbpt {
+void set_error(const std::string& msg);
+struct Server; // server.cpp
+struct ServerDeleter {
+    void operator()(Server* s) const;
+};
+using ServerPtr = std::unique_ptr<Server, ServerDeleter>;
+// Stops the server thread (cancelling queued requests) and frees its resources.
+void server_shutdown(ServerPtr& s);
+} // namespace gbpt
+
+struct gbpt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::mutex mu;
+    std::map<uint32_t, gbpt::SceneGPU> scenes; // node addresses stay valid until erased
+    std::map<uint32_t, int> scene_users;       // server requests holding a scene (queued or running)
+    uint32_t next_scene = 1;
+    gbpt::Work work;
+    gbpt::TickEngine batch; // gbpt_render_batch, over `work`
+    unsigned long long* d_misc = nullptr; // [0] nodes, [1] tris, [2] error word
+    gbpt_hit* d_hits = nullptr;
+    uint64_t hits_cap = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    gbpt::Profile prof;
+    gbpt::ServerPtr server;
+};
+
+namespace gbpt {
+
+#define GBPT_CUDA_CHECK(call)                                                                      \
+    do {                                                                                           \
+        const cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                                   \
+            ::gbpt::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                 \
+            return e_ == cudaErrorMemoryAllocation ? GBPT_ERR_NO_MEMORY : GBPT_ERR_CUDA;           \
+        }                                                                                          \
+    } while (0)
+
+// Null check and cudaSetDevice for the context's device.
+int check_ctx(gbpt_ctx* ctx);
+// Camera / parameter validation shared by every render entry point.
+int validate_params(const gbpt_camera* cam, const gbpt_render_params* p);
+// Seconds on the host's steady clock (request timestamps).
+double host_clock();
+
+} // namespace gbpt

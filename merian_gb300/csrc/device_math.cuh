@@ -508,6 +508,46 @@ template <class G> GBPT_DI BsdfSample material_sample(const Material& m, float3 
 
 GBPT_DI float yuv_luminance(float3 c) { return dot(c, f3(0.299f, 0.587f, 0.114f)); }
 
+// Directional albedo fit of GGX with height-correlated Smith G2 (ggx_integral_approx_ and
+// ggx_integral_approx_correlated, brdf-ggx.slang:285-316): bias and scale are ratios of
+// polynomials in (cos theta, alpha), the bias suppressed for F0 near 0. The coefficient rows are
+// the reference's fit (row-major, mul(M, x) = rows . x).
+GBPT_DI float3 ggx_preintegrated(float3 F0, float alpha, float cos_theta) {
+    const float c = fabsf(cos_theta), c2 = c * c, c3 = c2 * c;
+    const float a = alpha, a2 = a * a, a3 = a2 * a;
+    const float n1 = (0.995367f + -1.38839f * c) + (-0.24751f + 1.97442f * c) * a;
+    const float d1 = (1.0f + 2.68132f * c + 52.366f * c3) +
+                     (16.0932f + -3.98452f * c + 59.3013f * c3) * a +
+                     (-5.18731f + 255.259f * c + 2544.07f * c3) * a3;
+    const float n2 = (-0.0564526f + 3.82901f * c) + (16.91f + -11.0303f * c) * a;
+    const float d2 = (1.0f + 4.11118f * c2 + -1.37886f * c3) +
+                     (19.3254f + -28.9947f * c2 + 16.9514f * c3) * a +
+                     (0.545386f + 96.0994f * c2 + -79.4492f * c3) * a3;
+    float bias = n1 / d1;
+    const float scale = n2 / d2;
+    const float luma = (F0.x + F0.y + F0.z) * (1.0f / 3.0f);
+    bias *= fminf(fmaxf(luma * 50.0f, 0.0f), 1.0f);
+    const float sc = fmaxf(0.0f, scale), b = fmaxf(0.0f, bias);
+    return f3(F0.x * sc + b, F0.y * sc + b, F0.z * sc + b);
+}
+
+// BSDF::get_albedo of the material toward wi (the GBuffer's albedo): Lambert albedo
+// (brdf-lambert-diffuse.slang:50-52); conductor, Fresnel mix, rough dielectric and mix as
+// bsdf-conductor-fresnel.slang:39-41, bsdf-fresnel-mix.slang:50-53,
+// bsdf-rough-dielectric.slang:111-115, bsdf-mix.slang:51-54.
+GBPT_DI float3 material_albedo(const Material& m, float3 wi) {
+    if (m.model == 0u) return m.base;
+    const float a_xy = sqrtf(m.ax * m.ay);
+    const float3 one = f3(1.f, 1.f, 1.f);
+    const float3 spec = ggx_preintegrated(f3(m.f0, m.f0, m.f0), a_xy, wi.z);
+    const float3 opaque = spec + (one - spec) * m.base;
+    const float fd = ((1.0f - m.eta) / (1.0f + m.eta)) * ((1.0f - m.eta) / (1.0f + m.eta));
+    const float3 sd = ggx_preintegrated(f3(fd, fd, fd), sqrtf(m.alpha_iso * m.alpha_iso), wi.z);
+    const float3 diel = sd + (one - sd) * (m.eta * m.eta * m.tcol);
+    const float3 cond = ggx_preintegrated(m.base, a_xy, wi.z);
+    return lerp3(lerp3(opaque, diel, m.tw), cond, m.metal);
+}
+
 // OpenPBRMaterial::get_sample / DiffuseMaterial::get_sample (openpbr-material.slang:220-323,
 // diffuse-material.slang:27-41) from the first four float4 of a gbpt_material record: model and
 // base colour, (metalness, alpha_x, alpha_y, specular_weight), (specular_ior, emission),

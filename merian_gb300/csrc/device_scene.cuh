@@ -284,10 +284,22 @@ __device__ __forceinline__ Hit trace_ray(const DevScene& sc, float3 o, float3 d,
 // the triangle group onto its stack) when fewer than kPostponeLanes lanes of the warp have
 // triangles to test, so node steps and triangle steps stay in lockstep across the warp. The
 // closest-hit result and the tie rule are the same as trace_ray's: only the visit order changes.
-constexpr int kRefillLanes = 20;
-constexpr int kPostponeLanes = 6;
+#ifndef GBPT_SMEM_STACK
+#define GBPT_SMEM_STACK 0
+#endif
+#ifndef GBPT_REFILL_LANES
+#define GBPT_REFILL_LANES 20
+#endif
+#ifndef GBPT_POSTPONE_LANES
+#define GBPT_POSTPONE_LANES 6
+#endif
+constexpr int kRefillLanes = GBPT_REFILL_LANES;
+constexpr int kPostponeLanes = GBPT_POSTPONE_LANES;
 
 struct TraceState {
+    const uint4* nodes;  // the ray's scene (rays of one launch may belong to different scenes)
+    const float4* tris;
+    uint32_t mask;       // instance mask of the ray
     float3 o, d, inv;
     float tmin;
     uint32_t oct_inv, oct_inv4;
@@ -322,18 +334,31 @@ GBPT_DI void trace_init(TraceState& s, float3 o, float3 d, float tmin, float tma
     s.found = false;
 }
 
+// Byte j of w as a float. With GBPT_BOX_PRMT the byte is placed in the mantissa of 2^23 with
+// one byte permute and 2^23 subtracted (exact), instead of a shift, a mask and an int-to-float
+// conversion.
+#ifndef GBPT_BOX_PRMT
+#define GBPT_BOX_PRMT 0
+#endif
+GBPT_DI float qbyte(uint32_t w, int j) {
+#if GBPT_BOX_PRMT
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (uint32_t)j)) - 8388608.0f;
+#else
+    return (float)((w >> (8 * j)) & 0xFFu);
+#endif
+}
+
 // Intersects the 8 children of node `ni`; returns the hit mask (inner children in bits 24..31 in
 // traversal order, triangles in bits 0..23) and the node's child / triangle bases and imask.
 template <bool COUNT>
-GBPT_DI uint32_t intersect_node(const DevScene& sc, const TraceState& s, uint32_t ni,
-                                uint32_t& child_base, uint32_t& tri_base, uint32_t& imask,
-                                TraceCounters* ctr) {
+GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& child_base,
+                                uint32_t& tri_base, uint32_t& imask, TraceCounters* ctr) {
     if (COUNT) ctr->nodes++;
-    const uint4 n0 = __ldg(&sc.nodes[5 * ni + 0]);
-    const uint4 n1 = __ldg(&sc.nodes[5 * ni + 1]);
-    const uint4 n2 = __ldg(&sc.nodes[5 * ni + 2]);
-    const uint4 n3 = __ldg(&sc.nodes[5 * ni + 3]);
-    const uint4 n4 = __ldg(&sc.nodes[5 * ni + 4]);
+    const uint4 n0 = __ldg(&s.nodes[5 * ni + 0]);
+    const uint4 n1 = __ldg(&s.nodes[5 * ni + 1]);
+    const uint4 n2 = __ldg(&s.nodes[5 * ni + 2]);
+    const uint4 n3 = __ldg(&s.nodes[5 * ni + 3]);
+    const uint4 n4 = __ldg(&s.nodes[5 * ni + 4]);
     const float kErr = 1.0f / 1048576.0f;
     const float aix = __uint_as_float((n0.w & 0xFFu) << 23) * s.inv.x;
     const float aiy = __uint_as_float(((n0.w >> 8) & 0xFFu) << 23) * s.inv.y;
@@ -367,12 +392,12 @@ GBPT_DI uint32_t intersect_node(const DevScene& sc, const TraceState& s, uint32_
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const uint32_t sh = 8u * j;
-            const float tnx = fmaf((float)((nqx >> sh) & 0xFFu), aix, nox);
-            const float tny = fmaf((float)((nqy >> sh) & 0xFFu), aiy, noy);
-            const float tnz = fmaf((float)((nqz >> sh) & 0xFFu), aiz, noz);
-            const float tfx = fmaf((float)((fqx >> sh) & 0xFFu), aix, fox);
-            const float tfy = fmaf((float)((fqy >> sh) & 0xFFu), aiy, foy);
-            const float tfz = fmaf((float)((fqz >> sh) & 0xFFu), aiz, foz);
+            const float tnx = fmaf(qbyte(nqx, j), aix, nox);
+            const float tny = fmaf(qbyte(nqy, j), aiy, noy);
+            const float tnz = fmaf(qbyte(nqz, j), aiz, noz);
+            const float tfx = fmaf(qbyte(fqx, j), aix, fox);
+            const float tfy = fmaf(qbyte(fqy, j), aiy, foy);
+            const float tfz = fmaf(qbyte(fqz, j), aiz, foz);
             const float cmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, s.tmin));
             const float cmax = fminf(fminf(tfx, tfy), fminf(tfz, s.best.t));
             if (cmin <= cmax) hitmask |= ((child_bits4 >> sh) & 7u) << ((bit_index4 >> sh) & 31u);
@@ -382,14 +407,26 @@ GBPT_DI uint32_t intersect_node(const DevScene& sc, const TraceState& s, uint32_
 }
 
 // Runs the traversal of every ray i < n, pulling indices from *fetch (zero before the launch).
-// load(i, o, d, tmin, tmax) fetches ray i; store(i, hit) receives its result (geom == 0xFFFFFFFF
-// on miss; with ANY, the first hit found). Must be called by all 32 lanes of every warp.
+// load(i, state) sets ray i's scene (nodes, tris), mask and calls trace_init; store(i, hit)
+// receives its result (geom == 0xFFFFFFFF on miss; with ANY, the first hit found). Must be called
+// by all 32 lanes of every warp.
 template <bool ANY, bool COUNT, class Load, class Store>
-__device__ __forceinline__ void trace_persistent(const DevScene& sc, uint32_t n, uint32_t* fetch,
-                                                 uint32_t ray_mask, Load load, Store store,
-                                                 TraceCounters* ctr, uint32_t* err) {
+__device__ __forceinline__ void trace_persistent(uint32_t n, uint32_t* fetch, Load load,
+                                                 Store store, TraceCounters* ctr, uint32_t* err) {
     const uint32_t lane = threadIdx.x & 31u;
+#if GBPT_SMEM_STACK > 0
+    // the first GBPT_SMEM_STACK entries of every thread's stack in shared memory (thread-strided:
+    // no bank conflicts), the rest in local memory; launched with 128-thread blocks
+    __shared__ uint2 smem_stack[GBPT_SMEM_STACK * 128];
+    uint2 stack_local[kStackSize - GBPT_SMEM_STACK];
+    auto st_ref = [&](int i) -> uint2& {
+        return i < GBPT_SMEM_STACK ? smem_stack[i * 128 + threadIdx.x]
+                                   : stack_local[i - GBPT_SMEM_STACK];
+    };
+#else
     uint2 stack[kStackSize];
+    auto st_ref = [&](int i) -> uint2& { return stack[i]; };
+#endif
     TraceState s;
     uint32_t ray = 0xFFFFFFFFu;
     bool active = false, exhausted = false;
@@ -405,10 +442,7 @@ __device__ __forceinline__ void trace_persistent(const DevScene& sc, uint32_t n,
             if (want) {
                 ray = base + __popc(want_mask & ((1u << lane) - 1u));
                 if (ray < n) {
-                    float3 o, d;
-                    float tmin, tmax;
-                    load(ray, o, d, tmin, tmax);
-                    trace_init(s, o, d, tmin, tmax);
+                    load(ray, s);
                     active = true;
                 } else {
                     exhausted = true;
@@ -433,12 +467,12 @@ __device__ __forceinline__ void trace_persistent(const DevScene& sc, uint32_t n,
                         s.tgroup.y = 0;
                         break;
                     }
-                    stack[s.sp++] = s.ngroup;
+                    st_ref(s.sp++) = s.ngroup;
                 }
                 const uint32_t slot = (bit - 24u) ^ s.oct_inv;
                 const uint32_t ni = s.ngroup.x + __popc((hits & 0xFFu) & ((1u << slot) - 1u));
                 uint32_t cb, tb, im;
-                const uint32_t hm = intersect_node<COUNT>(sc, s, ni, cb, tb, im, ctr);
+                const uint32_t hm = intersect_node<COUNT>(s, ni, cb, tb, im, ctr);
                 s.ngroup = make_uint2(cb, (hm & 0xFF000000u) | im);
                 s.tgroup = make_uint2(tb, hm & 0x00FFFFFFu);
             } else {
@@ -452,18 +486,18 @@ __device__ __forceinline__ void trace_persistent(const DevScene& sc, uint32_t n,
             while (s.tgroup.y != 0u) {
                 if (may_postpone && s.sp < kStackSize &&
                     __popc(__activemask()) < kPostponeLanes) {
-                    stack[s.sp++] = s.tgroup;
+                    st_ref(s.sp++) = s.tgroup;
                     s.tgroup.y = 0u;
                     break;
                 }
                 const uint32_t b = __ffs(s.tgroup.y) - 1u;
                 s.tgroup.y &= s.tgroup.y - 1u;
                 const uint32_t ti = s.tgroup.x + b;
-                const float4 r0 = __ldg(&sc.tris[3 * ti + 0]);
-                const float4 r1 = __ldg(&sc.tris[3 * ti + 1]);
-                const float4 r2 = __ldg(&sc.tris[3 * ti + 2]);
+                const float4 r0 = __ldg(&s.tris[3 * ti + 0]);
+                const float4 r1 = __ldg(&s.tris[3 * ti + 1]);
+                const float4 r2 = __ldg(&s.tris[3 * ti + 2]);
                 const uint32_t tfl = __float_as_uint(r2.w);
-                if (((tfl & 0xFFu) & ray_mask) == 0u) continue;
+                if (((tfl & 0xFFu) & s.mask) == 0u) continue;
                 if (COUNT) ctr->tris++;
                 float t, u, v;
                 if (!intersect_tri(s.pre, r0, r1, r2, tfl, s.tmin, s.best.t, t, u, v)) continue;
@@ -485,7 +519,7 @@ __device__ __forceinline__ void trace_persistent(const DevScene& sc, uint32_t n,
             bool done = done_any;
             if (!done && s.ngroup.y <= 0x00FFFFFFu) {
                 if (s.sp == 0) done = true;
-                else s.ngroup = stack[--s.sp];
+                else s.ngroup = st_ref(--s.sp);
             }
             if (done) {
                 if (!s.found) {

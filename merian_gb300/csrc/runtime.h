@@ -64,10 +64,24 @@ struct Work {
     uint64_t pix_id_cap = 0;
     float4* out = nullptr;      // device output staging for host-output renders
     uint64_t out_cap = 0;
-    // counters: [0],[1] queue counts, [2] shadow count, [3] error flags, [4..7] scratch
+    // counters: [0],[1] queue counts, [2] shadow count, [3] error flags, [4],[5] fetch cursors
     uint32_t* counters = nullptr;
-    unsigned long long* stats = nullptr; // [0] rays, [1] shadow rays
+    unsigned long long* stats = nullptr; // [0] rays, [1] shadow rays, [2] closest-hit rays
+    // request, scene and tick tables of the batch being rendered
+    void* tables = nullptr;
+    uint64_t tables_bytes = 0;
     uint64_t bytes = 0;
+};
+
+// One request of a batch: a scene, a camera, the render parameters and a device output of
+// pixel_count float4 (mean rgb, mean squared luminance), indexed like the pixel list.
+struct BatchItem {
+    const SceneGPU* scene = nullptr;
+    gbpt_camera camera{};
+    gbpt_render_params params{};
+    const uint32_t* pixels_device = nullptr; // nullptr: all pixels, row-major
+    uint32_t pixel_count = 0;
+    float4* out_device = nullptr;
 };
 
 // Paths per wave: 8 Mi paths keep ~1.5 GB of path state and queues resident.
@@ -93,11 +107,54 @@ struct RenderArgs {
     float4* out_device;
 };
 
-// kernels.cu. work_ctr (device, >= 2 counters) receives traversal work when prof->level >= 2.
+// A request as the tick engine sees it: its pixels are scheduled in list order, whole pixels
+// per tick; cursor counts the pixels already scheduled.
+struct TickItem : BatchItem {
+    uint32_t cursor = 0;
+};
+
+// Plans ticks over requests, uploads each tick's tables and enqueues its kernels on one stream
+// (wavefront.cu). A tick is at most `wave` paths of whole pixels from up to 256 requests.
+struct TickEngine {
+    Work* work = nullptr;
+    cudaStream_t stream = nullptr;
+    uint64_t wave = kWavePaths;
+    // replay each tick shape (path length, NEE) from a captured CUDA graph; needs a stream that
+    // can be captured, and keeps a whole wave of work buffers
+    bool use_graphs = false;
+    // internal
+    struct Graph {
+        uint32_t shape;
+        cudaGraphExec_t exec;
+        uint64_t launches;
+    };
+    std::vector<Graph> graphs;
+    const void* graph_work = nullptr; // the buffers the graphs were captured with
+    const void* graph_tables = nullptr;
+    std::vector<unsigned char> stage;
+    std::vector<const SceneGPU*> scene_ptrs;
+    int grids[4] = {0, 0, 0, 0};
+    void release(); // destroys the graphs
+};
+
+// Enqueues the next tick over items (earlier items first; a request is never overtaken by a later
+// one). *n_paths = 0 when no item has pixels left. `done` receives the indices of the items whose
+// last pixels are in this tick: their outputs are final once the tick has run. work_ctr (device,
+// >= 2 counters) receives traversal work when prof->level >= 2.
+int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64_t* n_paths,
+                 std::vector<uint32_t>* done, uint64_t* launches, Profile* prof,
+                 unsigned long long* work_ctr);
+// Renders every item (ticks until all pixels are scheduled); results are independent of the
+// other items in the batch, bit for bit.
+int render_batch(TickEngine& e, const BatchItem* items, uint32_t n_items, uint64_t* launches,
+                 Profile* prof, unsigned long long* work_ctr);
 int render_frame(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
                  uint64_t* launches, Profile* prof, unsigned long long* work_ctr);
 int primary_points(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
                    float* out_device);
+// Bytes of tick tables for ticks of at most max_chunks requests.
+uint64_t tick_table_bytes(uint32_t max_chunks);
+int num_sms();
 
 // Rendering from the library's fixed scratch array (kernels.cu): no allocation, synchronous.
 constexpr uint64_t kStaticScratchBytes = 64ull << 20;
@@ -109,6 +166,8 @@ int trace_rays(const SceneGPU& scene, const gbpt_ray* rays, uint32_t n, uint32_t
                gbpt_hit* hits, unsigned long long* counters_device, cudaStream_t stream);
 int trace_primary(const SceneGPU& scene, const gbpt_camera& cam, uint32_t w, uint32_t h,
                   uint32_t mask, gbpt_hit* hits_device, uint32_t* err_device, cudaStream_t stream);
+int gbuffer(const SceneGPU& scene, const gbpt_camera& cam, uint32_t w, uint32_t h, uint32_t mask,
+            gbpt_gbuffer_texel* out_device, uint32_t* err_device, cudaStream_t stream);
 int work_reserve(Work& work, uint64_t paths, uint64_t pixels);
 void work_free(Work& work);
 

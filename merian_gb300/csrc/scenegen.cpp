@@ -87,11 +87,11 @@ struct MeshBuilder {
 
 using namespace gbpt;
 
-extern "C" GBPT_API int gbpt_gen_cornell(uint64_t seed, gbpt_packed_vertex* vertices,
-                                         uint32_t* indices, gbpt_geometry* geometries,
-                                         gbpt_material* materials) {
-    if (!vertices || !indices || !geometries || !materials) {
-        set_error("gbpt_gen_cornell: null output buffer");
+// The Cornell box with every grid refined `tess` times per side (1024 tess^2 triangles).
+static int gen_cornell(uint64_t seed, uint32_t tess, gbpt_packed_vertex* vertices,
+                       uint32_t* indices, gbpt_geometry* geometries, gbpt_material* materials) {
+    if (!vertices || !indices || !geometries || !materials || tess == 0 || tess > 64) {
+        set_error("gbpt_gen_cornell: null output buffer or tessellation outside [1, 64]");
         return GBPT_ERR_INVALID;
     }
     Pcg32 rng(seed, 0xC0A1u);
@@ -99,10 +99,13 @@ extern "C" GBPT_API int gbpt_gen_cornell(uint64_t seed, gbpt_packed_vertex* vert
     for (auto& a : albedo)
         for (float& c : a) c = 0.2f + 0.6f * rng.uniform();
 
+    const int t = (int)tess, nw = 8 * t, nb = 4 * t;
     MeshBuilder mb{vertices, indices};
     const auto all = [](int, int) { return true; };
     const auto ident = [](V3 p) { return p; };
-    const auto light_cell = [](int i, int j) { return i >= 3 && i <= 4 && j >= 3 && j <= 4; };
+    const auto light_cell = [t](int i, int j) {
+        return i >= 3 * t && i < 5 * t && j >= 3 * t && j < 5 * t;
+    };
     uint32_t g = 0;
     auto begin_geom = [&](uint32_t material, uint32_t flags) {
         geometries[g].first_vertex = 0; // indices are absolute (all geometries share the pool)
@@ -117,23 +120,23 @@ extern "C" GBPT_API int gbpt_gen_cornell(uint64_t seed, gbpt_packed_vertex* vert
     };
     // walls: front faces point into the box (counter-clockwise seen from inside)
     begin_geom(0, 0); // floor, y = 0
-    mb.grid(v3(0, 0, 0), v3(0, 0, 1), v3(1, 0, 0), 8, all, ident);
+    mb.grid(v3(0, 0, 0), v3(0, 0, 1), v3(1, 0, 0), nw, all, ident);
     end_geom();
     begin_geom(1, 0); // ceiling without the light cells, y = 1
-    mb.grid(v3(0, 1, 0), v3(1, 0, 0), v3(0, 0, 1), 8,
+    mb.grid(v3(0, 1, 0), v3(1, 0, 0), v3(0, 0, 1), nw,
             [&](int i, int j) { return !light_cell(i, j); }, ident);
     end_geom();
     begin_geom(7, 0); // emissive 0.25 x 0.25 ceiling patch
-    mb.grid(v3(0, 1, 0), v3(1, 0, 0), v3(0, 0, 1), 8, light_cell, ident);
+    mb.grid(v3(0, 1, 0), v3(1, 0, 0), v3(0, 0, 1), nw, light_cell, ident);
     end_geom();
     begin_geom(2, 0); // back wall, z = 1
-    mb.grid(v3(0, 0, 1), v3(0, 1, 0), v3(1, 0, 0), 8, all, ident);
+    mb.grid(v3(0, 0, 1), v3(0, 1, 0), v3(1, 0, 0), nw, all, ident);
     end_geom();
     begin_geom(3, 0); // left wall, x = 0
-    mb.grid(v3(0, 0, 0), v3(0, 1, 0), v3(0, 0, 1), 8, all, ident);
+    mb.grid(v3(0, 0, 0), v3(0, 1, 0), v3(0, 0, 1), nw, all, ident);
     end_geom();
     begin_geom(4, 0); // right wall, x = 1
-    mb.grid(v3(1, 0, 0), v3(0, 0, 1), v3(0, 1, 0), 8, all, ident);
+    mb.grid(v3(1, 0, 0), v3(0, 0, 1), v3(0, 1, 0), nw, all, ident);
     end_geom();
 
     // two boxes standing on the floor, rotated about y by -17 and +17 degrees
@@ -149,15 +152,15 @@ extern "C" GBPT_API int gbpt_gen_cornell(uint64_t seed, gbpt_packed_vertex* vert
             return v3(cr * lx + sr * lz + bx.cx, ly, -sr * lx + cr * lz + bx.cz);
         };
         begin_geom(5 + b, 0);
-        mb.grid(v3(1, 0, 0), v3(0, 1, 0), v3(0, 0, 1), 4, all, xf); // +x
-        mb.grid(v3(0, 0, 0), v3(0, 0, 1), v3(0, 1, 0), 4, all, xf); // -x
-        mb.grid(v3(0, 1, 0), v3(0, 0, 1), v3(1, 0, 0), 4, all, xf); // +y
-        mb.grid(v3(0, 0, 0), v3(1, 0, 0), v3(0, 0, 1), 4, all, xf); // -y
-        mb.grid(v3(0, 0, 1), v3(1, 0, 0), v3(0, 1, 0), 4, all, xf); // +z
-        mb.grid(v3(0, 0, 0), v3(0, 1, 0), v3(1, 0, 0), 4, all, xf); // -z
+        mb.grid(v3(1, 0, 0), v3(0, 1, 0), v3(0, 0, 1), nb, all, xf); // +x
+        mb.grid(v3(0, 0, 0), v3(0, 0, 1), v3(0, 1, 0), nb, all, xf); // -x
+        mb.grid(v3(0, 1, 0), v3(0, 0, 1), v3(1, 0, 0), nb, all, xf); // +y
+        mb.grid(v3(0, 0, 0), v3(1, 0, 0), v3(0, 0, 1), nb, all, xf); // -y
+        mb.grid(v3(0, 0, 1), v3(1, 0, 0), v3(0, 1, 0), nb, all, xf); // +z
+        mb.grid(v3(0, 0, 0), v3(0, 1, 0), v3(1, 0, 0), nb, all, xf); // -z
         end_geom();
     }
-    if (mb.nt != 1024 || g != 8) {
+    if (mb.nt != 1024u * tess * tess || g != 8) {
         set_error("gbpt_gen_cornell: internal size mismatch");
         return GBPT_ERR_INVALID;
     }
@@ -168,6 +171,19 @@ extern "C" GBPT_API int gbpt_gen_cornell(uint64_t seed, gbpt_packed_vertex* vert
     materials[7].specular_weight = 0.0f;
     materials[7].emission[0] = materials[7].emission[1] = materials[7].emission[2] = 15.0f;
     return GBPT_OK;
+}
+
+extern "C" GBPT_API int gbpt_gen_cornell(uint64_t seed, gbpt_packed_vertex* vertices,
+                                         uint32_t* indices, gbpt_geometry* geometries,
+                                         gbpt_material* materials) {
+    return gen_cornell(seed, 1, vertices, indices, geometries, materials);
+}
+
+extern "C" GBPT_API int gbpt_gen_cornell_tess(uint64_t seed, uint32_t tess,
+                                              gbpt_packed_vertex* vertices, uint32_t* indices,
+                                              gbpt_geometry* geometries,
+                                              gbpt_material* materials) {
+    return gen_cornell(seed, tess, vertices, indices, geometries, materials);
 }
 
 extern "C" GBPT_API int gbpt_gen_soup(uint64_t seed, uint32_t n_triangles, uint32_t n_geometries,

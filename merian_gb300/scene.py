@@ -58,14 +58,19 @@ class SceneData:
         return d, keep
 
 
-def cornell(seed: int = BASE_SEED) -> SceneData:
-    """The 1,024-triangle Cornell box (gbpt_gen_cornell)."""
+def cornell(seed: int = BASE_SEED, tess: int = 1) -> SceneData:
+    """The Cornell box: 1,024 triangles (gbpt_gen_cornell), or every grid refined `tess` times per
+    side, 1,024 tess^2 triangles (gbpt_gen_cornell_tess)."""
     lib = N.load()
-    v = np.zeros(3072, N.VERTEX_DTYPE)
-    i = np.zeros((1024, 3), np.uint32)
+    nt = 1024 * tess * tess
+    v = np.zeros(3 * nt, N.VERTEX_DTYPE)
+    i = np.zeros((nt, 3), np.uint32)
     g = np.zeros(8, N.GEOMETRY_DTYPE)
     m = np.zeros(8, N.MATERIAL_DTYPE)
-    N.check(lib.gbpt_gen_cornell(seed, N.ptr(v), N.ptr(i), N.ptr(g), N.ptr(m)))
+    if tess == 1:
+        N.check(lib.gbpt_gen_cornell(seed, N.ptr(v), N.ptr(i), N.ptr(g), N.ptr(m)))
+    else:
+        N.check(lib.gbpt_gen_cornell_tess(seed, tess, N.ptr(v), N.ptr(i), N.ptr(g), N.ptr(m)))
     return SceneData(v, i, g, m)
 
 
@@ -239,3 +244,70 @@ class Context:
         f, t, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
         N.check(self.lib.gbpt_memory_info(self.handle, C.byref(f), C.byref(t), C.byref(c)))
         return dict(free=f.value, total=t.value, ctx=c.value)
+
+    # ---- batches and the request server ----------------------------------------------------
+    @staticmethod
+    def request(sid: int, camera: N.Camera, params: N.RenderParams, out_host: np.ndarray | None = None,
+                out_device: int | None = None) -> N.Request:
+        r = N.Request()
+        r.scene = sid
+        r.camera = camera
+        r.params = params
+        r.out_host = N.ptr(out_host) if out_host is not None else None
+        r.out_device = out_device
+        return r
+
+    def render_batch(self, jobs, stats: bool = False):
+        """jobs: (scene id, camera, params) triples; returns one (n, 4) float32 array per job."""
+        outs, reqs = [], (N.Request * max(len(jobs), 1))()
+        for i, (sid, cam, params) in enumerate(jobs):
+            n = params.pixel_count or params.width * params.height
+            outs.append(np.empty((n, 4), np.float32))
+            reqs[i] = self.request(sid, cam, params, out_host=outs[-1])
+        st = N.RenderStats()
+        N.check(self.lib.gbpt_render_batch(self.handle, reqs, len(jobs),
+                                           C.byref(st) if stats else None))
+        return (outs, st) if stats else outs
+
+    def set_graphs(self, enable: bool) -> None:
+        N.check(self.lib.gbpt_set_graphs(self.handle, int(enable)))
+
+    def clock(self) -> float:
+        return self.lib.gbpt_clock()
+
+    def server_start(self, wave_paths: int = 0, arena_bytes: int = 0, use_graphs: bool = False,
+                     max_active: int = 0) -> None:
+        cfg = N.ServerConfig(wave_paths, arena_bytes, int(use_graphs), max_active)
+        N.check(self.lib.gbpt_server_start(self.handle, C.byref(cfg)))
+
+    def server_stop(self) -> None:
+        N.check(self.lib.gbpt_server_stop(self.handle))
+
+    def submit(self, sid: int, camera: N.Camera, params: N.RenderParams,
+               out_host: np.ndarray | None = None, out_device: int | None = None) -> int:
+        """Queues a request; out_host (or the device buffer) must stay alive until it finishes."""
+        t = C.c_uint64()
+        r = self.request(sid, camera, params, out_host, out_device)
+        N.check(self.lib.gbpt_server_submit(self.handle, C.byref(r), C.byref(t)))
+        return t.value
+
+    def poll(self, ticket: int) -> tuple[int, N.RequestStatus]:
+        st = N.RequestStatus()
+        rc = self.lib.gbpt_server_poll(self.handle, ticket, C.byref(st))
+        return rc, st
+
+    def wait(self, ticket: int, timeout_s: float = -1.0) -> tuple[int, N.RequestStatus]:
+        st = N.RequestStatus()
+        rc = self.lib.gbpt_server_wait(self.handle, ticket, timeout_s, C.byref(st))
+        return rc, st
+
+    def cancel(self, ticket: int) -> None:
+        N.check(self.lib.gbpt_server_cancel(self.handle, ticket))
+
+    def release(self, ticket: int) -> None:
+        N.check(self.lib.gbpt_server_release(self.handle, ticket))
+
+    def server_info(self) -> dict:
+        st = N.ServerStats()
+        N.check(self.lib.gbpt_server_info(self.handle, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in N.ServerStats._fields_}

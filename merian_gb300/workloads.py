@@ -1,0 +1,111 @@
+"""Seeded synthetic request mixes: the batched configuration (many independent scenes rendered
+together) and the served stream (Poisson arrivals over resident scenes).
+
+Scenes below 100k triangles are the Cornell box with its grids refined (gbpt_gen_cornell_tess,
+tessellated walls and boxes as in the 1,024-triangle box); larger ones are the triangle soup of the
+headline configuration with a 512x256 Gaussian-lobe environment. Every request uses the
+estimator of its scene type: Cornell boxes path length 5, soups path length 8, both with NEE and
+Russian roulette from depth 3.
+"""
+from __future__ import annotations
+
+import math
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import scene as S
+
+BATCH_RESOLUTIONS = ((256, 256), (512, 512), (1024, 1024))
+SERVED_RESOLUTIONS = ((512, 512), (1024, 1024), (1920, 1080))
+SERVED_SPP = (1, 4, 16, 64)
+
+
+@dataclass
+class SceneSpec:
+    kind: str  # "cornell" or "soup"
+    triangles: int
+    seed: int
+
+    def build(self) -> S.SceneData:
+        if self.kind == "cornell":
+            tess = max(1, int(round(math.sqrt(self.triangles / 1024))))
+            return S.cornell(self.seed, tess)
+        n_geom = max(1, min(4096, self.triangles // 64))
+        return S.soup(self.seed, self.triangles, n_geom, (512, 256))
+
+
+@dataclass
+class RequestSpec:
+    scene: int  # index into the scene list
+    width: int
+    height: int
+    spp: int
+    frame: int
+    arrival_s: float = 0.0
+    upload: SceneSpec | None = None  # a request that brings its own new scene
+
+
+def scene_spec(rng: np.random.Generator, lo: float, hi: float) -> SceneSpec:
+    n = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+    kind = "cornell" if n < 100_000 else "soup"
+    if kind == "cornell":  # the refined box has 1024 tess^2 triangles
+        tess = max(1, int(round(math.sqrt(n / 1024))))
+        n = 1024 * tess * tess
+    return SceneSpec(kind, n, int(rng.integers(1 << 62)))
+
+
+def camera(kind: str, width: int, height: int):
+    if kind == "cornell":
+        return S.look_at((0.5, 0.5, -1.4), (0.5, 0.5, 0.0), (0.0, 1.0, 0.0), 40.0, width / height)
+    return S.look_at((0.5, 0.5, -0.6), (0.5, 0.5, 0.5), (0.0, 1.0, 0.0), 45.0, width / height)
+
+
+def params(kind: str, req: RequestSpec):
+    L = 5 if kind == "cornell" else 8
+    p, _ = S.render_params(req.width, req.height, req.spp, L, nee=True, rr_depth=3,
+                           frame=req.frame)
+    return p
+
+
+def batch_mix(seed: int = S.BASE_SEED, n: int = 256, tri_range=(1e3, 2e6)):
+    """n independent scenes (triangles log-uniform in tri_range), one request each: resolution
+    from {256^2, 512^2, 1024^2}, spp uniform in 1..64."""
+    rng = np.random.default_rng(seed)
+    scenes = [scene_spec(rng, *tri_range) for _ in range(n)]
+    reqs = []
+    for i in range(n):
+        w, h = BATCH_RESOLUTIONS[rng.integers(len(BATCH_RESOLUTIONS))]
+        reqs.append(RequestSpec(i, w, h, int(rng.integers(1, 65)), frame=i))
+    return scenes, reqs
+
+
+def served_stream(seed: int = S.BASE_SEED, n_scenes: int = 32, n_requests: int = 96,
+                  rate: float = 200.0, tri_range=(1e4, 5e6), upload_fraction: float = 0.05):
+    """n_scenes resident scenes (triangles log-uniform in tri_range) and n_requests Poisson
+    arrivals at `rate` per second; resolution from {512^2, 1024^2, 1920x1080}, spp from
+    {1, 4, 16, 64}; a fraction of the requests brings a new 100k-triangle soup."""
+    rng = np.random.default_rng(seed)
+    scenes = [scene_spec(rng, *tri_range) for _ in range(n_scenes)]
+    t = 0.0
+    reqs = []
+    for i in range(n_requests):
+        t += float(rng.exponential(1.0 / rate))
+        w, h = SERVED_RESOLUTIONS[rng.integers(len(SERVED_RESOLUTIONS))]
+        spp = SERVED_SPP[rng.integers(len(SERVED_SPP))]
+        up = None
+        if rng.uniform() < upload_fraction:
+            up = SceneSpec("soup", 100_000, int(rng.integers(1 << 62)))
+        reqs.append(RequestSpec(int(rng.integers(n_scenes)), w, h, spp, frame=i, arrival_s=t,
+                                upload=up))
+    return scenes, reqs
+
+
+def upload_all(ctx: S.Context, specs, threads: int = 16):
+    """Builds and uploads the scenes on a thread pool (generation and BVH construction run in
+    the library without the GIL); returns the scene ids in order."""
+    def one(spec):
+        return ctx.upload(spec.build())
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        return list(ex.map(one, specs))

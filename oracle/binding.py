@@ -40,6 +40,7 @@ def load() -> C.CDLL:
         lib.oracle_trace_rays.argtypes = [vp, vp, u32, u32, i32, i32, vp, vp, vp]
         lib.oracle_render.argtypes = [vp, vp, vp, i32, i32, vp, vp, vp]
         lib.oracle_num_threads.restype = i32
+        lib.oracle_gbuffer.argtypes = [vp, vp, u32, u32, u32, vp]
         lib.oracle_bsdf_check.argtypes = [i32, vp, vp, f32, f32, vp, f32, f32, u32, u32, vp]
         lib.oracle_material_samples.argtypes = [vp, i32, f32, vp, u32, u32, vp]
         _lib = lib
@@ -92,6 +93,12 @@ class OracleScene:
         load().oracle_trace_rays(self.h, _p(rays), len(rays), mask, int(fp64), int(any_hit),
                                  _p(hits), C.addressof(nn), C.addressof(nt))
         return hits, nn.value, nt.value
+
+    def gbuffer(self, camera, width: int, height: int, mask: int = 0xFF, texel_dtype=None):
+        """FP32 GBuffer texels (gbpt_gbuffer_texel layout), row-major."""
+        out = np.zeros(width * height, texel_dtype)
+        load().oracle_gbuffer(self.h, C.addressof(camera), width, height, mask, _p(out))
+        return out
 
     def render(self, camera, params, fp64: bool = True, threads: int = 0):
         """(rgba (n,4) float64, mean of squared per-sample rgb (n,3), traced rays)."""

@@ -855,10 +855,18 @@ void render_pixel(const Scene& s, const gbpt_camera& cam, const gbpt_render_para
     ctr.rays++;
     const HitRec h = trace<R>(s, primary, cfg.mask, false);
     const SP<R> psp = shading_point<R>(s, primary, h, R(1), true, true);
+    // "demodulate albedo" (render_pt.slang:105-116): every sample divided by the GBuffer albedo
+    // floored at 1e-2 (gbuffer.slang:135-140), taken at the full-precision hit
+    V3<R> demod = mk(R(1), R(1), R(1));
+    if (p.demodulate_albedo) {
+        const SP<R> g = shading_point<R>(s, primary, h, R(1), true, false);
+        const V3<R> a = g.has_material ? g.bsdf.get_albedo(g.frame.to_local(-primary.d)) : g.emission;
+        demod = mk(maxr(a.x, R(1e-2f)), maxr(a.y, R(1e-2f)), maxr(a.z, R(1e-2f)));
+    }
     double acc[3] = {0, 0, 0}, sm = 0.0, s2[3] = {0, 0, 0};
     for (int smp = 0; smp < p.spp; ++smp) {
         Pcg rng{pcg4d16(px, py, p.frame, (uint32_t)smp)};
-        const V3<R> c = trace_path<R>(s, cfg, primary, psp, rng, ctr);
+        const V3<R> c = trace_path<R>(s, cfg, primary, psp, rng, ctr) / demod;
         if (!(std::isfinite((double)c.x) && std::isfinite((double)c.y) &&
               std::isfinite((double)c.z)))
             continue;
@@ -942,6 +950,72 @@ ORACLE_API int oracle_primary_points(void* sp, const gbpt_camera* cam, const gbp
                              q.emission.x, q.emission.y, q.emission.z, 0.f,
                              r.d.x, r.d.y, r.d.z, 0.f};
         std::memcpy(o, v, sizeof(v));
+    }
+    return 0;
+}
+
+// The GBuffer (Raytraced) node for a static camera (gbuffer_rt.slang:18-94, gbuffer.slang:40-160)
+// in FP32: per pixel one gbpt_gbuffer_texel. Motion vectors are 0 and delta_z is
+// |pos - camera| - linear_z (0): the previous camera and transforms equal the current ones.
+ORACLE_API int oracle_gbuffer(void* sp, const gbpt_camera* cam, uint32_t w, uint32_t h,
+                              uint32_t mask, gbpt_gbuffer_texel* out) {
+    using R = float;
+    const Scene& s = *(const Scene*)sp;
+    const V3<R> U = mk<R>(cam->U[0], cam->U[1], cam->U[2]), V = mk<R>(cam->V[0], cam->V[1], cam->V[2]),
+                W = mk<R>(cam->W[0], cam->W[1], cam->W[2]);
+    const V3<R> cpos = mk<R>(cam->position[0], cam->position[1], cam->position[2]);
+    auto pinhole = [&](uint32_t px, uint32_t py) { // camera.slang:34-37
+        const R x = ((R)px + R(0.5) + (R)cam->jitter[0]) / (R)w;
+        const R y = ((R)py + R(0.5) + (R)cam->jitter[1]) / (R)h;
+        return normalize((R(2) * x + R(-1)) * U + (R(-2) * y + R(1)) * V + W);
+    };
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < (int64_t)w * h; ++i) {
+        const uint32_t px = (uint32_t)(i % w), py = (uint32_t)(i / w);
+        const Ray<R> r = camera_ray<R>(*cam, px, py, w, h);
+        const HitRec hr = trace<R>(s, r, mask & 0xFFu, false);
+        gbpt_gbuffer_texel t{};
+        t.instance_id = hr.valid ? 0u : 0xFFFFFFFFu;
+        t.primitive_id = hr.valid ? hr.prim : 0xFFFFFFFFu;
+        t.geometry_index = (uint16_t)(hr.valid ? hr.geom : 0xFFFFFFFFu);
+        t.instance_index = (uint16_t)(hr.valid ? 0u : 0xFFFFFFFFu);
+        t.barycentrics = hr.valid ? ((uint32_t)float_to_half(hr.v) << 16) | float_to_half(hr.u) : 0u;
+        const bool env = !hr.valid || (s.geoms[hr.geom].flags & GBPT_MESH_USE_ENV_MAP);
+        if (env) {
+            const SP<R> e = env_sp<R>(s, r);
+            t.encoded_normal = encode_normal(e.frame.n.x, e.frame.n.y, e.frame.n.z);
+            t.linear_z = std::min(length(e.pos - r.o), 65504.0f);
+            for (int c = 0; c < 3; ++c) {
+                t.albedo[c] = (&e.emission.x)[c];
+                t.emission[c] = (&e.emission.x)[c];
+            }
+        } else {
+            const SP<R> q = shading_point<R>(s, r, hr, R(1), true, false);
+            const gbpt_geometry& g = s.geoms[hr.geom];
+            const uint32_t tri = g.first_triangle + hr.prim;
+            const V3<R> p0 = fetch_pos<R>(s, g.first_vertex + s.idx[3 * tri + 0]);
+            const V3<R> p1 = fetch_pos<R>(s, g.first_vertex + s.idx[3 * tri + 1]);
+            const V3<R> p2 = fetch_pos<R>(s, g.first_vertex + s.idx[3 * tri + 2]);
+            V3<R> fn = normalize(cross(p1 - p0, p2 - p0));
+            if (g.flags & GBPT_MESH_FLIP_FACING) fn = -fn;
+            const R lz = length(q.pos - r.o);
+            // Surface::compute_grad_z (hit.slang:99-103)
+            const R n_dot_oo = dot(fn, q.pos - r.o);
+            const R gx = n_dot_oo / dot(fn, pinhole(px + 1, py)) - lz;
+            const R gy = n_dot_oo / dot(fn, pinhole(px, py + 1)) - lz;
+            t.grad_z = ((uint32_t)float_to_half(gy) << 16) | float_to_half(gx);
+            t.encoded_normal = encode_normal(q.frame.n.x, q.frame.n.y, q.frame.n.z);
+            t.linear_z = std::min(lz, 65504.0f);
+            t.delta_z = length(q.pos - cpos) - lz;
+            const V3<R> a = q.bsdf.get_albedo(q.frame.to_local(-r.d));
+            t.albedo[0] = a.x;
+            t.albedo[1] = a.y;
+            t.albedo[2] = a.z;
+            t.emission[0] = q.emission.x;
+            t.emission[1] = q.emission.y;
+            t.emission[2] = q.emission.z;
+        }
+        out[i] = t;
     }
     return 0;
 }

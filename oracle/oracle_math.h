@@ -336,8 +336,43 @@ template <class R> inline Sample<R> some(V3<R> wo, R pdf, V3<R> w) { return {wo,
 static constexpr float BSDF_MIN_COS = 1e-6f; // bsdf.slang:13
 
 // LambertDiffuseBRDF (brdf-lambert-diffuse.slang:32-90); sample_cos (utils/sampling.slang:24-29)
+// Directional albedo fit of GGX with the height-correlated Smith G2 (ggx_integral_approx_ and
+// ggx_integral_approx_correlated, brdf-ggx.slang:285-316): bias and scale as ratios of polynomials
+// in (cos theta, alpha), the bias suppressed for F0 near 0. Matrix rows as the reference writes
+// them (float2x2 / float3x3 are row-major; mul(M, x) = rows . x).
+template <class R> inline V3<R> ggx_preintegrated(V3<R> F0, R alpha, R cos_theta) {
+    const R c = std::fabs(cos_theta);
+    const R X[4] = {R(1), c, c * c, c * c * c};
+    const R Y[4] = {R(1), alpha, alpha * alpha, alpha * alpha * alpha};
+    const R M1[2][2] = {{R(0.995367f), R(-1.38839f)}, {R(-0.24751f), R(1.97442f)}};
+    const R M2[3][3] = {{R(1.0f), R(2.68132f), R(52.366f)},
+                        {R(16.0932f), R(-3.98452f), R(59.3013f)},
+                        {R(-5.18731f), R(255.259f), R(2544.07f)}};
+    const R M3[2][2] = {{R(-0.0564526f), R(3.82901f)}, {R(16.91f), R(-11.0303f)}};
+    const R M4[3][3] = {{R(1.0f), R(4.11118f), R(-1.37886f)},
+                        {R(19.3254f), R(-28.9947f), R(16.9514f)},
+                        {R(0.545386f), R(96.0994f), R(-79.4492f)}};
+    const R xyw[3] = {X[0], X[1], X[3]}, xzw[3] = {X[0], X[2], X[3]}, Yxyw[3] = {Y[0], Y[1], Y[3]};
+    R n1 = 0, d1 = 0, n2 = 0, d2 = 0;
+    for (int i = 0; i < 2; ++i) {
+        n1 += (M1[i][0] * X[0] + M1[i][1] * X[1]) * Y[i];
+        n2 += (M3[i][0] * X[0] + M3[i][1] * X[1]) * Y[i];
+    }
+    for (int i = 0; i < 3; ++i) {
+        d1 += (M2[i][0] * xyw[0] + M2[i][1] * xyw[1] + M2[i][2] * xyw[2]) * Yxyw[i];
+        d2 += (M4[i][0] * xzw[0] + M4[i][1] * xzw[1] + M4[i][2] * xzw[2]) * Yxyw[i];
+    }
+    R bias = n1 / d1;
+    const R scale = n2 / d2;
+    const R luma = (F0.x + F0.y + F0.z) * (R(1) / R(3));
+    bias *= clampr(luma * R(50), R(0), R(1));
+    const R sc = maxr(R(0), scale), b = maxr(R(0), bias);
+    return mk(F0.x * sc + b, F0.y * sc + b, F0.z * sc + b);
+}
+
 template <class R> struct Lambert {
     V3<R> albedo;
+    V3<R> get_albedo(V3<R>) const { return albedo; } // brdf-lambert-diffuse.slang:50-52
     template <class G> Sample<R> sample_eval(V3<R> wi, G& rng) const {
         const R x0 = rng.next_float(), x1 = rng.next_float();
         const R su = std::sqrt(x0);
@@ -359,6 +394,10 @@ template <class R> struct Lambert {
 // GGXBRDF (brdf-ggx.slang:331-397)
 template <class R> struct GGX {
     R ax, ay;
+    // brdf-ggx.slang:399-406: the isotropic fit at sqrt(ax ay)
+    V3<R> preintegrated(V3<R> F0, V3<R> wi) const {
+        return ggx_preintegrated(F0, std::sqrt(ax * ay), wi.z);
+    }
     template <class G> Sample<R> sample_eval(V3<R> wi, G& rng) const {
         if (wi.z < R(BSDF_MIN_COS)) return none<R>();
         const R r0 = rng.next_float(), r1 = rng.next_float();
@@ -388,6 +427,7 @@ template <class R> struct GGX {
 template <class R> struct Conductor {
     GGX<R> ggx;
     V3<R> f0;
+    V3<R> get_albedo(V3<R> wi) const { return ggx.preintegrated(f0, wi); } // :39-41
     V3<R> schlick(R c) const {
         const R t = schlick_term(c);
         return f0 + (mk(R(1), R(1), R(1)) - f0) * t;
@@ -410,6 +450,13 @@ template <class R> struct Conductor {
 template <class R> struct RoughDielectric {
     R alpha, eta;
     V3<R> tint;
+    // bsdf-rough-dielectric.slang:111-115
+    V3<R> get_albedo(V3<R> wi) const {
+        const R f = pow2((R(1) - eta) / (R(1) + eta));
+        const V3<R> spec = GGX<R>{alpha, alpha}.preintegrated(mk(f, f, f), wi);
+        const V3<R> one = mk(R(1), R(1), R(1));
+        return spec + (one - spec) * (pow2(eta) * tint);
+    }
     template <class G> Sample<R> sample_eval(V3<R> wi, G& rng) const {
         if (wi.z < R(BSDF_MIN_COS)) return none<R>();
         const R a2 = pow2(alpha);
@@ -500,6 +547,11 @@ template <class R> struct OpaqueDielectric {
     GGX<R> layer;
     Lambert<R> base;
     R f0;
+    // bsdf-fresnel-mix.slang:50-53
+    V3<R> get_albedo(V3<R> wi) const {
+        const V3<R> spec = layer.preintegrated(mk(f0, f0, f0), wi);
+        return spec + (mk(R(1), R(1), R(1)) - spec) * base.get_albedo(wi);
+    }
     R F(R c) const { return f0 + (R(1) - f0) * schlick_term(c); }
     V3<R> eval(V3<R> wi, V3<R> wo) const {
         const V3<R> h = normalize(wi + wo);
@@ -528,6 +580,8 @@ template <class R, class B0, class B1> struct Mix {
     B0 b0;
     B1 b1;
     R w;
+    // bsdf-mix.slang:51-54 (a plain lerp, also at weight 0 and 1)
+    V3<R> get_albedo(V3<R> wi) const { return lerp(b0.get_albedo(wi), b1.get_albedo(wi), w); }
     V3<R> eval(V3<R> wi, V3<R> wo) const {
         if (w == R(0)) return b0.eval(wi, wo);
         if (w == R(1)) return b1.eval(wi, wo);
@@ -574,6 +628,9 @@ template <class R> struct MaterialBSDF {
         return diffuse ? lambert.eval(wi, wo) : substrate.eval(wi, wo);
     }
     R pdf(V3<R> wi, V3<R> wo) const { return diffuse ? lambert.pdf(wi, wo) : substrate.pdf(wi, wo); }
+    V3<R> get_albedo(V3<R> wi) const {
+        return diffuse ? lambert.get_albedo(wi) : substrate.get_albedo(wi);
+    }
 };
 
 static constexpr float MIN_ROUGHNESS = 0.0316f; // material.slang:23
