@@ -91,11 +91,15 @@ typedef struct gbpt_material {
     uint32_t reserved[3];
 } gbpt_material;
 
-/* RGBA8 texture (sRGB is not applied: values are linear / 255). */
+/* RGBA8 texture (a material's base_color_texture), sampled bilinearly with repeat addressing at
+ * level 0 (merian's DefaultLODSampler); srgb = 1 decodes the colour channels from sRGB per texel
+ * before filtering (an R8G8B8A8_SRGB image), 0 reads them as UNORM. */
 typedef struct gbpt_texture {
-    const uint8_t* texels; /* width*height*4 bytes, row-major */
+    const uint8_t* texels; /* width*height*4 bytes, row-major, row 0 = v in [0, 1/height) */
     uint32_t width;
     uint32_t height;
+    uint32_t srgb;
+    uint32_t reserved;
 } gbpt_texture;
 
 /* Lat-long environment (merian LatLongMap, environment-map.slang:23-35): RGBA32F texels,
@@ -272,7 +276,7 @@ GBPT_API int gbpt_render_device(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera
  * fixed 64 MiB device array compiled into the library, held by each GPU that loads the library
  * until the process exits; this call allocates nothing. The scene must already be resident
  * (gbpt_scene_create, an earlier set-up step) and out_rgba_device is caller-owned device memory.
- * Limits: spp at most the paths one pass over the array holds (242,182), a pixel
+ * Limits: spp at most the paths one pass over the array holds (225,815), a pixel
  * subset of at most 65,536 entries; larger requests return GBPT_ERR_INVALID. The first call on a
  * device looks up the array's device address, so make it before any stream capture. All calls
  * share the array: calls that overlap on the GPU (other streams or threads) race on it. The call
@@ -307,6 +311,23 @@ GBPT_API int gbpt_render_batch(gbpt_ctx* ctx, const gbpt_request* requests, uint
 /* gbpt_render_batch replays each tick from a captured CUDA graph (one per path length and
  * estimator) when enabled (1), or launches the kernels one by one (0, the default). */
 GBPT_API int gbpt_set_graphs(gbpt_ctx* ctx, int enable);
+
+/* The schedule of gbpt_render, gbpt_render_device and gbpt_render_batch. Outputs are the same
+ * under every tuning, bit for bit: only the time changes. */
+typedef struct gbpt_tuning {
+    uint64_t wave_paths;    /* paths per tick: 0 = default (2^23), else in [1024, 2^24] */
+    int32_t sort_materials; /* -1: as each request's params ask; 0 / 1: force off / on */
+    int32_t use_graphs;     /* gbpt_render_batch replays ticks from CUDA graphs */
+} gbpt_tuning;
+
+GBPT_API int gbpt_set_tuning(gbpt_ctx* ctx, const gbpt_tuning* tuning);
+GBPT_API int gbpt_get_tuning(gbpt_ctx* ctx, gbpt_tuning* tuning);
+/* Autotuner: renders the frame (camera, params: a whole frame, no pixel list) under each
+ * candidate tick size (2^21 .. 2^24 paths) with material sorting off and on, keeps the fastest as
+ * the context's tuning and returns it. ms_out, when non-NULL, receives the time of each candidate
+ * (up to 8, ordered tick size major, sorting minor). Outputs are discarded. */
+GBPT_API int gbpt_autotune(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
+                           const gbpt_render_params* params, gbpt_tuning* out, double* ms_out);
 
 /* The request server: one host thread per context admits submitted requests in arrival order
  * while their outputs fit a device arena reserved from free HBM at start, and renders the
@@ -454,6 +475,12 @@ GBPT_API int gbpt_gen_soup(uint64_t seed, uint32_t n_triangles, uint32_t n_geome
                            gbpt_packed_vertex* vertices, uint32_t* indices,
                            gbpt_geometry* geometries, gbpt_material* materials);
 GBPT_API int gbpt_gen_env(uint64_t seed, uint32_t width, uint32_t height, float* texels);
+/* A closed bumpy sphere for the instanced configuration: (n_u + 1) * n_v vertices (uv from the
+ * latitude-longitude grid, smooth normals) and 2 * n_u * (n_v - 1) triangles. */
+GBPT_API int gbpt_gen_blob(uint64_t seed, uint32_t n_u, uint32_t n_v, gbpt_packed_vertex* vertices,
+                           uint32_t* indices);
+/* A tileable sRGB value-noise RGBA8 texture, width * height * 4 bytes. */
+GBPT_API int gbpt_gen_noise_texture(uint64_t seed, uint32_t width, uint32_t height, uint8_t* rgba);
 
 #ifdef __cplusplus
 }

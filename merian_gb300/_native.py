@@ -48,6 +48,9 @@ HIT_DTYPE = np.dtype([("instance_id", "<u4"), ("instance_index", "<u4"), ("primi
                       ("reserved", "<u4")])
 RAY_DTYPE = np.dtype([("origin", "<f4", 3), ("tmin", "<f4"), ("direction", "<f4", 3),
                       ("tmax", "<f4")])
+INSTANCE_DTYPE = np.dtype([("blas", "<u4"), ("mask", "<u4"), ("object_to_world", "<f4", 12)])
+BLAS_DTYPE = np.dtype([("first_geometry", "<u4"), ("geometry_count", "<u4")])
+assert INSTANCE_DTYPE.itemsize == 56
 GBUFFER_DTYPE = np.dtype([("encoded_normal", "<u4"), ("grad_z", "<u4"), ("instance_id", "<u4"),
                           ("primitive_id", "<u4"), ("geometry_index", "<u2"),
                           ("instance_index", "<u2"), ("barycentrics", "<u4"),
@@ -88,7 +91,8 @@ class EnvMap(C.Structure):
 
 
 class Texture(C.Structure):
-    _fields_ = [("texels", C.POINTER(C.c_uint8)), ("width", C.c_uint32), ("height", C.c_uint32)]
+    _fields_ = [("texels", C.POINTER(C.c_uint8)), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("srgb", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class SceneDesc(C.Structure):
@@ -123,6 +127,11 @@ class ServerStats(C.Structure):
                 ("arena_bytes", C.c_uint64), ("wave_paths", C.c_uint64)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("wave_paths", C.c_uint64), ("sort_materials", C.c_int32),
+                ("use_graphs", C.c_int32)]
+
+
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
 
 # (name, restype, argtypes) of every exported entry point declared in include/gbpt.h
@@ -130,6 +139,10 @@ EXPORTS = [
     ("gbpt_render_batch", C.c_int, [C.c_void_p, C.POINTER(Request), C.c_uint32,
                                     C.POINTER(RenderStats)]),
     ("gbpt_set_graphs", C.c_int, [C.c_void_p, C.c_int]),
+    ("gbpt_set_tuning", C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    ("gbpt_get_tuning", C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    ("gbpt_autotune", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.POINTER(RenderParams),
+                                C.POINTER(Tuning), C.POINTER(C.c_double)]),
     ("gbpt_clock", C.c_double, []),
     ("gbpt_server_start", C.c_int, [C.c_void_p, C.POINTER(ServerConfig)]),
     ("gbpt_server_stop", C.c_int, [C.c_void_p]),
@@ -195,6 +208,8 @@ EXPORTS = [
                                         C.c_void_p, C.c_void_p]),
     ("gbpt_gen_soup", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                                 C.c_void_p, C.c_void_p]),
+    ("gbpt_gen_blob", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("gbpt_gen_noise_texture", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p]),
     ("gbpt_gen_env", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p]),
 ]
 

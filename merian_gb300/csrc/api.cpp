@@ -69,9 +69,30 @@ int upload(void** dst, const void* src, size_t bytes, uint64_t& total) {
     return GBPT_OK;
 }
 
+// Inverse of a row-major 3x4 affine transform (double); false when singular.
+bool invert_affine(const float* m, double* inv) {
+    const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9],
+                 i = m[10];
+    const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
+    const double det = a * A + b * B + c * C;
+    if (!(std::fabs(det) > 1e-30) || !std::isfinite(det)) return false;
+    const double r[9] = {A / det, -(b * i - c * h) / det, (b * f - c * e) / det,
+                         B / det, (a * i - c * g) / det,  -(a * f - c * d) / det,
+                         C / det, -(a * h - b * g) / det, (a * e - b * d) / det};
+    const double t[3] = {m[3], m[7], m[11]};
+    for (int row = 0; row < 3; ++row) {
+        inv[4 * row + 0] = r[3 * row + 0];
+        inv[4 * row + 1] = r[3 * row + 1];
+        inv[4 * row + 2] = r[3 * row + 2];
+        inv[4 * row + 3] = -(r[3 * row + 0] * t[0] + r[3 * row + 1] * t[1] + r[3 * row + 2] * t[2]);
+    }
+    return true;
+}
+
 void free_scene(SceneGPU& s) {
-    void* ptrs[] = {s.nodes,    s.tris,     s.verts,    s.idx,      s.geoms,      s.mats,
-                    s.env,      s.env_marg, s.env_cond, s.env_func, s.light_tris, s.light_cdf};
+    void* ptrs[] = {s.nodes,    s.tris,     s.verts,      s.idx,       s.geoms,    s.mats,
+                    s.env,      s.env_marg, s.env_cond,   s.env_func,  s.light_tris, s.light_cdf,
+                    s.inst,     s.tex,      s.tex_info,   s.srgb_lut};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     s = SceneGPU{};
@@ -202,9 +223,39 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
         set_error("gbpt_scene_create: null pointer in scene description");
         return GBPT_ERR_INVALID;
     }
-    if (d->instance_count != 0) {
-        set_error("gbpt_scene_create: two-level (instanced) scenes are not supported yet");
-        return GBPT_ERR_INVALID;
+    const bool two_level = d->instance_count != 0;
+    if (two_level) {
+        if (!d->instances || !d->blas_ranges || d->blas_count == 0) {
+            set_error("gbpt_scene_create: instances need BLAS ranges");
+            return GBPT_ERR_INVALID;
+        }
+        for (uint32_t b = 0; b < d->blas_count; ++b) {
+            const gbpt_blas_range& r = d->blas_ranges[b];
+            if (r.geometry_count == 0 ||
+                (uint64_t)r.first_geometry + r.geometry_count > d->geometry_count) {
+                set_error("gbpt_scene_create: BLAS " + std::to_string(b) + " geometry range out of bounds");
+                return GBPT_ERR_INVALID;
+            }
+        }
+        for (uint32_t i = 0; i < d->instance_count; ++i) {
+            const gbpt_instance& in = d->instances[i];
+            bool finite = in.blas < d->blas_count;
+            for (float x : in.object_to_world) finite = finite && std::isfinite(x);
+            double inv[12];
+            if (!finite || !invert_affine(in.object_to_world, inv)) {
+                set_error("gbpt_scene_create: instance " + std::to_string(i) +
+                          " has a bad BLAS index or a singular / non-finite transform");
+                return GBPT_ERR_INVALID;
+            }
+        }
+    }
+    for (uint32_t t = 0; t < d->texture_count; ++t) {
+        const gbpt_texture& tx = d->textures[t];
+        if (!tx.texels || tx.width == 0 || tx.height == 0 ||
+            (uint64_t)tx.width * tx.height > (1ull << 28)) {
+            set_error("gbpt_scene_create: texture " + std::to_string(t) + " is empty or too large");
+            return GBPT_ERR_INVALID;
+        }
     }
     // validate geometry ranges and gather world-space triangles
     BuildInput bi;
@@ -231,40 +282,121 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
             return GBPT_ERR_INVALID;
         }
     }
-    bi.v.reserve(9 * total_tris);
-    bi.prim.reserve(total_tris);
-    bi.geom.reserve(total_tris);
-    bi.flags.reserve(total_tris);
-    for (uint32_t g = 0; g < d->geometry_count; ++g) {
-        const gbpt_geometry& geo = d->geometries[g];
-        const uint32_t tf = (geo.instance_mask & 0xFFu) |
-                            ((geo.flags & GBPT_MESH_TWO_SIDED) ? (1u << 8) : 0u) |
-                            ((geo.flags & GBPT_MESH_FLIP_FACING) ? (1u << 9) : 0u);
-        for (uint32_t k = 0; k < geo.triangle_count; ++k) {
-            const uint64_t tri = (uint64_t)geo.first_triangle + k;
-            for (int c = 0; c < 3; ++c) {
-                const uint64_t vi = (uint64_t)geo.first_vertex + d->indices[3 * tri + c];
-                if (vi >= d->vertex_count) {
-                    set_error("gbpt_scene_create: vertex index out of bounds in geometry " +
-                              std::to_string(g));
-                    return GBPT_ERR_INVALID;
+    // triangles of the given geometries (object space for a BLAS), vertex indices checked
+    auto gather = [&](uint32_t g_first, uint32_t g_count, BuildInput& in) -> int {
+        for (uint32_t g = g_first; g < g_first + g_count; ++g) {
+            const gbpt_geometry& geo = d->geometries[g];
+            const uint32_t tf = (geo.instance_mask & 0xFFu) |
+                                ((geo.flags & GBPT_MESH_TWO_SIDED) ? (1u << 8) : 0u) |
+                                ((geo.flags & GBPT_MESH_FLIP_FACING) ? (1u << 9) : 0u);
+            for (uint32_t k = 0; k < geo.triangle_count; ++k) {
+                const uint64_t tri = (uint64_t)geo.first_triangle + k;
+                for (int c = 0; c < 3; ++c) {
+                    const uint64_t vi = (uint64_t)geo.first_vertex + d->indices[3 * tri + c];
+                    if (vi >= d->vertex_count) {
+                        set_error("gbpt_scene_create: vertex index out of bounds in geometry " +
+                                  std::to_string(g));
+                        return GBPT_ERR_INVALID;
+                    }
+                    const float* p = d->vertices[vi].position;
+                    if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(p[2])) {
+                        set_error("gbpt_scene_create: non-finite vertex position");
+                        return GBPT_ERR_INVALID;
+                    }
+                    in.v.insert(in.v.end(), p, p + 3);
                 }
-                const float* p = d->vertices[vi].position;
-                if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(p[2])) {
-                    set_error("gbpt_scene_create: non-finite vertex position");
-                    return GBPT_ERR_INVALID;
-                }
-                bi.v.insert(bi.v.end(), p, p + 3);
+                in.prim.push_back(k);
+                in.geom.push_back(g);
+                in.flags.push_back(tf);
             }
-            bi.prim.push_back(k);
-            bi.geom.push_back(g);
-            bi.flags.push_back(tf);
+        }
+        return GBPT_OK;
+    };
+    CwBvh bvh;
+    std::vector<float> inst_rec; // 28 floats per instance
+    if (!two_level) {
+        bi.v.reserve(9 * total_tris);
+        bi.prim.reserve(total_tris);
+        bi.geom.reserve(total_tris);
+        bi.flags.reserve(total_tris);
+        if ((rc = gather(0, d->geometry_count, bi))) return rc;
+        // each tree level puts at most one node group and one postponed triangle group on the
+        // 48-entry traversal stack
+        if (!build_cwbvh(bi, bvh, 24)) return GBPT_ERR_INVALID;
+    } else {
+        // one CWBVH per BLAS in object space, a top-level CWBVH over the instances' world boxes
+        // (a leaf record per instance: its index and mask), concatenated top level first; the
+        // stack holds both levels, so their depths share the 24 levels
+        std::vector<CwBvh> blas(d->blas_count);
+        for (uint32_t b = 0; b < d->blas_count; ++b) {
+            BuildInput in;
+            if ((rc = gather(d->blas_ranges[b].first_geometry, d->blas_ranges[b].geometry_count, in)))
+                return rc;
+            if (in.prim.empty()) {
+                set_error("gbpt_scene_create: BLAS " + std::to_string(b) + " has no triangles");
+                return GBPT_ERR_INVALID;
+            }
+            if (!build_cwbvh(in, blas[b], 16)) return GBPT_ERR_INVALID;
+        }
+        BuildInput top;
+        for (uint32_t i = 0; i < d->instance_count; ++i) {
+            const gbpt_instance& in = d->instances[i];
+            const CwBvh& b = blas[in.blas];
+            double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (int c = 0; c < 8; ++c) {
+                const double p[3] = {(c & 1) ? b.hi[0] : b.lo[0], (c & 2) ? b.hi[1] : b.lo[1],
+                                     (c & 4) ? b.hi[2] : b.lo[2]};
+                for (int a = 0; a < 3; ++a) {
+                    const float* r = in.object_to_world + 4 * a;
+                    const double w = (double)r[0] * p[0] + (double)r[1] * p[1] +
+                                     (double)r[2] * p[2] + (double)r[3];
+                    lo[a] = std::min(lo[a], w);
+                    hi[a] = std::max(hi[a], w);
+                }
+            }
+            // a degenerate triangle spanning the box (its bounds are the box, its centroid the
+            // box centre); rounded outward to float
+            float flo[3], fhi[3], fc[3];
+            for (int a = 0; a < 3; ++a) {
+                flo[a] = std::nextafter((float)lo[a], -INFINITY);
+                fhi[a] = std::nextafter((float)hi[a], INFINITY);
+                fc[a] = 0.5f * (flo[a] + fhi[a]);
+            }
+            top.v.insert(top.v.end(), flo, flo + 3);
+            top.v.insert(top.v.end(), fhi, fhi + 3);
+            top.v.insert(top.v.end(), fc, fc + 3);
+            top.prim.push_back(i);
+            top.geom.push_back(0);
+            top.flags.push_back(in.mask & 0xFFu);
+        }
+        if (!build_cwbvh(top, bvh, 8)) return GBPT_ERR_INVALID;
+        uint32_t max_blas_depth = 0;
+        std::vector<uint32_t> root(d->blas_count);
+        for (uint32_t b = 0; b < d->blas_count; ++b) {
+            const uint32_t node_off = (uint32_t)bvh.nodes.size(), tri_off = (uint32_t)bvh.tris.size();
+            root[b] = node_off;
+            for (CwNode nd : blas[b].nodes) {
+                nd.w[4] += node_off; // child base
+                nd.w[5] += tri_off;  // triangle base
+                bvh.nodes.push_back(nd);
+            }
+            bvh.tris.insert(bvh.tris.end(), blas[b].tris.begin(), blas[b].tris.end());
+            max_blas_depth = std::max(max_blas_depth, blas[b].depth);
+        }
+        bvh.depth += max_blas_depth;
+        for (uint32_t i = 0; i < d->instance_count; ++i) {
+            const gbpt_instance& in = d->instances[i];
+            double inv[12];
+            invert_affine(in.object_to_world, inv);
+            float rec[28];
+            for (int k = 0; k < 12; ++k) rec[k] = in.object_to_world[k];
+            for (int k = 0; k < 12; ++k) rec[12 + k] = (float)inv[k];
+            const uint32_t bits[4] = {root[in.blas], in.mask & 0xFFu,
+                                      d->blas_ranges[in.blas].first_geometry, 0u};
+            std::memcpy(&rec[24], bits, 16);
+            inst_rec.insert(inst_rec.end(), rec, rec + 28);
         }
     }
-    CwBvh bvh;
-    // each tree level puts at most one node group and one postponed triangle group on the
-    // 48-entry traversal stack
-    if (!build_cwbvh(bi, bvh, 24)) return GBPT_ERR_INVALID;
 
     SceneGPU s;
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -283,6 +415,10 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
                  d->geometries[g].material_id, d->geometries[g].flags};
     if ((rc = upload(&s.geoms, gh.data(), gh.size() * sizeof(GeomHost), bytes))) return fail(rc);
     if ((rc = upload(&s.mats, d->materials, d->material_count * sizeof(gbpt_material), bytes))) return fail(rc);
+    if (two_level) {
+        if ((rc = upload(&s.inst, inst_rec.data(), inst_rec.size() * sizeof(float), bytes))) return fail(rc);
+        s.n_inst = d->instance_count;
+    }
     s.n_nodes = bvh.nodes.size();
     s.n_tris = bvh.tris.size();
     s.n_verts = d->vertex_count;
@@ -294,7 +430,20 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
     {
         std::vector<float> lt;
         std::vector<double> pw;
-        for (uint32_t g = 0; g < d->geometry_count; ++g) {
+        // every placement of a geometry: once in a single-level scene, once per instance of
+        // its BLAS (world-space copies) in a two-level scene
+        std::vector<std::pair<uint32_t, const float*>> placements;
+        if (!two_level) {
+            for (uint32_t g = 0; g < d->geometry_count; ++g) placements.push_back({g, nullptr});
+        } else {
+            for (uint32_t i = 0; i < d->instance_count; ++i) {
+                const gbpt_blas_range& r = d->blas_ranges[d->instances[i].blas];
+                for (uint32_t g = r.first_geometry; g < r.first_geometry + r.geometry_count; ++g)
+                    placements.push_back({g, d->instances[i].object_to_world});
+            }
+        }
+        for (const auto& pl : placements) {
+            const uint32_t g = pl.first;
             const gbpt_geometry& geo = d->geometries[g];
             const gbpt_material& m = d->materials[geo.material_id];
             if (m.model == GBPT_MATERIAL_DIFFUSE) continue;
@@ -302,9 +451,21 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
             if (!(lum > 0.0)) continue;
             for (uint32_t k = 0; k < geo.triangle_count; ++k) {
                 const uint64_t tri = (uint64_t)geo.first_triangle + k;
+                float pw_[3][3];
                 const float* p[3];
-                for (int c = 0; c < 3; ++c)
-                    p[c] = d->vertices[geo.first_vertex + d->indices[3 * tri + c]].position;
+                for (int c = 0; c < 3; ++c) {
+                    const float* q = d->vertices[geo.first_vertex + d->indices[3 * tri + c]].position;
+                    if (pl.second) { // to world space
+                        for (int a = 0; a < 3; ++a) {
+                            const float* r = pl.second + 4 * a;
+                            pw_[c][a] = (float)((double)r[0] * q[0] + (double)r[1] * q[1] +
+                                                (double)r[2] * q[2] + (double)r[3]);
+                        }
+                        p[c] = pw_[c];
+                    } else {
+                        p[c] = q;
+                    }
+                }
                 const double e1[3] = {(double)p[1][0] - p[0][0], (double)p[1][1] - p[0][1], (double)p[1][2] - p[0][2]};
                 const double e2[3] = {(double)p[2][0] - p[0][0], (double)p[2][1] - p[0][1], (double)p[2][2] - p[0][2]};
                 const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
@@ -391,6 +552,36 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
         if ((rc = upload(&s.env_func, ffunc.data(), ffunc.size() * sizeof(float), bytes))) return fail(rc);
         if ((rc = upload(&s.env_cond, cond.data(), cond.size() * sizeof(float), bytes))) return fail(rc);
         if ((rc = upload(&s.env_marg, marg.data(), marg.size() * sizeof(float), bytes))) return fail(rc);
+    }
+    // RGBA8 textures, concatenated, with (first texel, width, height, sRGB) per texture and the
+    // sRGB decoding table (IEC 61966-2-1), evaluated in double and rounded once
+    if (d->texture_count) {
+        std::vector<uint32_t> info;
+        uint64_t total = 0;
+        for (uint32_t t = 0; t < d->texture_count; ++t) {
+            const gbpt_texture& tx = d->textures[t];
+            info.insert(info.end(), {(uint32_t)total, tx.width, tx.height, tx.srgb ? 1u : 0u});
+            total += (uint64_t)tx.width * tx.height;
+        }
+        if (total >= (1ull << 32)) {
+            set_error("gbpt_scene_create: textures too large");
+            return fail(GBPT_ERR_INVALID);
+        }
+        std::vector<uint8_t> texels(total * 4);
+        for (uint32_t t = 0; t < d->texture_count; ++t) {
+            const gbpt_texture& tx = d->textures[t];
+            std::memcpy(texels.data() + (size_t)info[4 * t] * 4, tx.texels,
+                        (size_t)tx.width * tx.height * 4);
+        }
+        float lut[256];
+        for (int i = 0; i < 256; ++i) {
+            const double c = i / 255.0;
+            lut[i] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+        }
+        if ((rc = upload(&s.tex, texels.data(), texels.size(), bytes))) return fail(rc);
+        if ((rc = upload(&s.tex_info, info.data(), info.size() * 4, bytes))) return fail(rc);
+        if ((rc = upload(&s.srgb_lut, lut, sizeof(lut), bytes))) return fail(rc);
+        s.n_tex = d->texture_count;
     }
     s.bytes = bytes;
     const uint32_t id = ctx->next_scene++;
@@ -486,6 +677,7 @@ static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
     RenderArgs a;
     a.camera = *cam;
     a.params = *p;
+    if (ctx->tuning.sort_materials >= 0) a.params.sort_materials = ctx->tuning.sort_materials;
     a.pixel_count = n_pix;
     a.pixels_device = nullptr;
     if (p->pixel_count) {
@@ -523,7 +715,11 @@ static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
         GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev0, ctx->stream));
         if (prof) prof->reset();
     }
-    rc = render_frame(it->second, w, a, ctx->stream, &launches, prof, ctx->d_misc);
+    // a tuned tick holds at least one whole pixel
+    const uint64_t wave = ctx->tuning.wave_paths
+                              ? std::max<uint64_t>(ctx->tuning.wave_paths, (uint64_t)p->spp)
+                              : 0;
+    rc = render_frame(it->second, w, a, ctx->stream, &launches, prof, ctx->d_misc, wave);
     if (rc != GBPT_OK) {
         set_error(rc == GBPT_ERR_NO_MEMORY ? "render: work buffer allocation failed"
                                            : "render: kernel launch failed: " +
@@ -691,6 +887,8 @@ GBPT_API int gbpt_render_batch(gbpt_ctx* ctx, const gbpt_request* reqs, uint32_t
         const uint32_t np = p.pixel_count ? p.pixel_count : p.width * p.height;
         items[i].camera = reqs[i].camera;
         items[i].params = reqs[i].params;
+        if (ctx->tuning.sort_materials >= 0)
+            items[i].params.sort_materials = ctx->tuning.sort_materials;
         items[i].pixel_count = np;
         items[i].pixels_device = nullptr;
         if (p.pixel_count) {
@@ -743,7 +941,111 @@ GBPT_API int gbpt_set_graphs(gbpt_ctx* ctx, int enable) {
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->batch.use_graphs = enable != 0;
+    ctx->tuning.use_graphs = enable != 0;
     if (!enable) ctx->batch.release();
+    return GBPT_OK;
+}
+
+static int check_tuning(const gbpt_tuning* t) {
+    if (!t || t->wave_paths > (1ull << 24) || (t->wave_paths && t->wave_paths < 1024) ||
+        t->sort_materials < -1 || t->sort_materials > 1) {
+        set_error("tuning: wave_paths must be 0 or in [1024, 2^24], sort_materials in {-1, 0, 1}");
+        return GBPT_ERR_INVALID;
+    }
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_set_tuning(gbpt_ctx* ctx, const gbpt_tuning* t) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if ((rc = check_tuning(t))) return rc;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->tuning = *t;
+    ctx->batch.wave = t->wave_paths ? t->wave_paths : kWavePaths;
+    ctx->batch.use_graphs = t->use_graphs != 0;
+    ctx->batch.release();
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_get_tuning(gbpt_ctx* ctx, gbpt_tuning* t) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!t) {
+        set_error("gbpt_get_tuning: null output");
+        return GBPT_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    *t = ctx->tuning;
+    return GBPT_OK;
+}
+
+// The autotuner: the candidate tunings rendered on one representative request and the fastest
+// kept. Outputs do not depend on the tuning (tick size and shading order only change the
+// schedule), so only time is compared.
+GBPT_API int gbpt_autotune(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
+                           const gbpt_render_params* p, gbpt_tuning* out, double* ms_out) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if ((rc = validate_params(camera, p))) return rc;
+    if (p->pixel_count) {
+        set_error("gbpt_autotune: tune on a whole frame (no pixel list)");
+        return GBPT_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->scenes.find(scene);
+    if (it == ctx->scenes.end()) {
+        set_error("gbpt_autotune: unknown scene id");
+        return GBPT_ERR_NOT_FOUND;
+    }
+    Work& w = ctx->work;
+    const uint32_t n_pix = p->width * p->height;
+    if (n_pix > w.out_cap) {
+        if (w.out) cudaFree(w.out);
+        w.out = nullptr;
+        w.out_cap = 0;
+        GBPT_CUDA_CHECK(cudaMalloc((void**)&w.out, (size_t)n_pix * sizeof(float4)));
+        w.out_cap = n_pix;
+    }
+    const uint64_t waves[4] = {1ull << 21, 1ull << 22, 1ull << 23, 1ull << 24};
+    gbpt_tuning best{};
+    double best_ms = 1e300;
+    int idx = 0;
+    for (uint64_t wave : waves) {
+        if (wave < (uint64_t)p->spp) continue;
+        for (int sort = 0; sort < 2; ++sort, ++idx) {
+            RenderArgs a;
+            a.camera = *camera;
+            a.params = *p;
+            a.params.sort_materials = sort;
+            a.pixel_count = n_pix;
+            a.pixels_device = nullptr;
+            a.out_device = w.out;
+            float ms = 0.f;
+            for (int rep = 0; rep < 2; ++rep) { // the first run allocates and warms the caches
+                GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev0, ctx->stream));
+                rc = render_frame(it->second, w, a, ctx->stream, nullptr, nullptr, nullptr, wave);
+                if (rc != GBPT_OK) {
+                    set_error("gbpt_autotune: render failed");
+                    return rc;
+                }
+                GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev1, ctx->stream));
+                GBPT_CUDA_CHECK(cudaEventSynchronize(ctx->ev1));
+                GBPT_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+            }
+            if (ms_out && idx < 8) ms_out[idx] = ms;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best.wave_paths = wave;
+                best.sort_materials = sort;
+            }
+        }
+    }
+    if ((rc = check_device_error(ctx))) return rc;
+    best.use_graphs = ctx->tuning.use_graphs;
+    ctx->tuning = best;
+    ctx->batch.wave = best.wave_paths;
+    ctx->batch.release();
+    if (out) *out = best;
     return GBPT_OK;
 }
 

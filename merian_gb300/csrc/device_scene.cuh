@@ -44,11 +44,21 @@ struct DevScene {
     uint32_t n_lights;
     float light_total; // sum of area x luminance
     float p_env;       // probability of choosing the environment in NEE
+    // two-level scenes: instance records (7 float4 each), n_inst = 0 for single-level scenes
+    const float4* __restrict__ inst;
+    uint32_t n_inst;
+    // RGBA8 textures: texels of all textures, (first texel, width, height, sRGB) per texture and
+    // the sRGB-to-linear table
+    const uchar4* __restrict__ tex;
+    const uint4* __restrict__ tex_info;
+    uint32_t n_tex;
+    const float* __restrict__ srgb_lut;
 };
 
 struct Hit {
     float t, u, v;
-    uint32_t prim, geom; // geom = 0xFFFFFFFF on miss
+    uint32_t prim, geom; // geom = 0xFFFFFFFF on miss (the scene-global geometry index)
+    uint32_t inst;       // instance index of two-level scenes, 0xFFFFFFFF otherwise
 };
 
 // ---- watertight test (Woop, Benthin, Wald 2013) -------------------------------------------------
@@ -128,6 +138,7 @@ GBPT_DI bool intersect_tri(const RayPre& p, float4 a4, float4 b4, float4 c4, uin
 
 // ---- CWBVH traversal ----------------------------------------------------------------------------
 constexpr int kStackSize = 48;
+constexpr uint32_t kNoInst = 0xFFFFFFFFu;
 
 struct TraceCounters {
     uint32_t nodes, tris;
@@ -138,152 +149,32 @@ GBPT_DI float safe_rcp(float d) {
     return __fdiv_rn(1.0f, fabsf(d) > m ? d : copysignf(m, d));
 }
 
-// Closest hit (ANY = false) or first hit (ANY = true) of a ray against the scene. Sets *err when
-// the traversal stack would overflow (the builder bounds the depth, so this does not happen for
-// trees it accepted).
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ Hit trace_ray(const DevScene& sc, float3 o, float3 d, float tmin,
-                                         float tmax, uint32_t ray_mask, TraceCounters* ctr,
-                                         uint32_t* err) {
-    Hit best;
-    best.t = tmax;
-    best.u = best.v = 0.0f;
-    best.prim = 0xFFFFFFFFu;
-    best.geom = 0xFFFFFFFFu;
-    uint32_t best_geom_key = 0xFFFFFFFFu, best_prim_key = 0xFFFFFFFFu;
-    const RayPre pre = ray_pre(o, d);
-    const float3 inv = f3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
-    const uint32_t oct = (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) |
-                         ((__float_as_uint(d.z) >> 31) << 2);
-    const uint32_t oct_inv = 7u - oct;
-    const uint32_t oct_inv4 = oct_inv * 0x01010101u;
-    const bool negx = d.x < 0.0f || (d.x == 0.0f && signbit(d.x));
-    const bool negy = d.y < 0.0f || (d.y == 0.0f && signbit(d.y));
-    const bool negz = d.z < 0.0f || (d.z == 0.0f && signbit(d.z));
-    const float kErr = 1.0f / 1048576.0f; // 2^-20 relative slack on dequantised plane distances
-
-    uint2 stack[kStackSize];
-    int sp = 0;
-    uint2 ngroup = make_uint2(0u, 0x80000000u);
-    bool found = false;
-    while (true) {
-        uint2 tgroup = make_uint2(0u, 0u);
-        {
-            // descend into the nearest remaining child of the current node group
-            const uint32_t hits = ngroup.y;
-            const uint32_t bit = 31u - __clz(hits & 0xFF000000u);
-            ngroup.y &= ~(1u << bit);
-            if (ngroup.y > 0x00FFFFFFu) {
-                if (sp >= kStackSize) {
-                    atomicOr(err, 1u);
-                    break;
-                }
-                stack[sp++] = ngroup;
-            }
-            const uint32_t slot = (bit - 24u) ^ oct_inv;
-            const uint32_t imask_parent = hits & 0xFFu;
-            const uint32_t rel = __popc(imask_parent & ((1u << slot) - 1u));
-            const uint32_t ni = ngroup.x + rel;
-            if (COUNT) ctr->nodes++;
-            const uint4 n0 = __ldg(&sc.nodes[5 * ni + 0]);
-            const uint4 n1 = __ldg(&sc.nodes[5 * ni + 1]);
-            const uint4 n2 = __ldg(&sc.nodes[5 * ni + 2]);
-            const uint4 n3 = __ldg(&sc.nodes[5 * ni + 3]);
-            const uint4 n4 = __ldg(&sc.nodes[5 * ni + 4]);
-            const float px = __uint_as_float(n0.x), py = __uint_as_float(n0.y),
-                        pz = __uint_as_float(n0.z);
-            const float sx = __uint_as_float((n0.w & 0xFFu) << 23);
-            const float sy = __uint_as_float(((n0.w >> 8) & 0xFFu) << 23);
-            const float sz = __uint_as_float(((n0.w >> 16) & 0xFFu) << 23);
-            const uint32_t imask = n0.w >> 24;
-            const float aix = sx * inv.x, aiy = sy * inv.y, aiz = sz * inv.z;
-            const float aox = (px - o.x) * inv.x, aoy = (py - o.y) * inv.y, aoz = (pz - o.z) * inv.z;
-            const float ex = (fabsf(aox) + 255.0f * fabsf(aix)) * kErr;
-            const float ey = (fabsf(aoy) + 255.0f * fabsf(aiy)) * kErr;
-            const float ez = (fabsf(aoz) + 255.0f * fabsf(aiz)) * kErr;
-            const float nox = aox - ex, fox = aox + ex;
-            const float noy = aoy - ey, foy = aoy + ey;
-            const float noz = aoz - ez, foz = aoz + ez;
-            uint32_t hitmask = 0;
-#pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const uint32_t meta4 = half ? n1.w : n1.z;
-                const uint32_t is_inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
-                const uint32_t inner_mask4 = (is_inner4 >> 4) * 0xFFu;
-                const uint32_t bit_index4 = (meta4 ^ (oct_inv4 & inner_mask4)) & 0x1F1F1F1Fu;
-                const uint32_t child_bits4 = (meta4 >> 5) & 0x07070707u;
-                const uint32_t qlx = half ? n2.y : n2.x, qly = half ? n2.w : n2.z;
-                const uint32_t qlz = half ? n3.y : n3.x, qhx = half ? n3.w : n3.z;
-                const uint32_t qhy = half ? n4.y : n4.x, qhz = half ? n4.w : n4.z;
-                const uint32_t nqx = negx ? qhx : qlx, fqx = negx ? qlx : qhx;
-                const uint32_t nqy = negy ? qhy : qly, fqy = negy ? qly : qhy;
-                const uint32_t nqz = negz ? qhz : qlz, fqz = negz ? qlz : qhz;
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const uint32_t sh = 8u * j;
-                    const float tnx = fmaf((float)((nqx >> sh) & 0xFFu), aix, nox);
-                    const float tny = fmaf((float)((nqy >> sh) & 0xFFu), aiy, noy);
-                    const float tnz = fmaf((float)((nqz >> sh) & 0xFFu), aiz, noz);
-                    const float tfx = fmaf((float)((fqx >> sh) & 0xFFu), aix, fox);
-                    const float tfy = fmaf((float)((fqy >> sh) & 0xFFu), aiy, foy);
-                    const float tfz = fmaf((float)((fqz >> sh) & 0xFFu), aiz, foz);
-                    const float cmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-                    const float cmax = fminf(fminf(tfx, tfy), fminf(tfz, best.t));
-                    if (cmin <= cmax) {
-                        const uint32_t cb = (child_bits4 >> sh) & 7u;
-                        const uint32_t bi = (bit_index4 >> sh) & 31u;
-                        hitmask |= cb << bi;
-                    }
-                }
-            }
-            ngroup = make_uint2(n1.x, (hitmask & 0xFF000000u) | imask);
-            tgroup = make_uint2(n1.y, hitmask & 0x00FFFFFFu);
-        }
-        while (tgroup.y != 0u) {
-            const uint32_t b = __ffs(tgroup.y) - 1u;
-            tgroup.y &= tgroup.y - 1u;
-            const uint32_t ti = tgroup.x + b;
-            const float4 r0 = __ldg(&sc.tris[3 * ti + 0]);
-            const float4 r1 = __ldg(&sc.tris[3 * ti + 1]);
-            const float4 r2 = __ldg(&sc.tris[3 * ti + 2]);
-            const uint32_t tfl = __float_as_uint(r2.w);
-            if (((tfl & 0xFFu) & ray_mask) == 0u) continue;
-            if (COUNT) ctr->tris++;
-            float t, u, v;
-            if (!intersect_tri(pre, r0, r1, r2, tfl, tmin, best.t, t, u, v)) continue;
-            const uint32_t prim = __float_as_uint(r0.w), geom = __float_as_uint(r1.w);
-            if (t < best.t || geom < best_geom_key ||
-                (geom == best_geom_key && prim < best_prim_key)) {
-                best.t = t;
-                best.u = u;
-                best.v = v;
-                best.prim = prim;
-                best.geom = geom;
-                best_geom_key = geom;
-                best_prim_key = prim;
-                found = true;
-                if (ANY) return best;
-            }
-        }
-        if (ngroup.y <= 0x00FFFFFFu) {
-            if (sp == 0) break;
-            ngroup = stack[--sp];
-        }
-    }
-    if (!found) {
-        best.geom = 0xFFFFFFFFu;
-        best.prim = 0xFFFFFFFFu;
-    }
-    return best;
+// Instance records of two-level scenes, 7 float4 each: object-to-world rows (0..2), world-to-
+// object rows (3..5), then (BLAS root node, mask, first geometry of the BLAS, 0) as bits. The
+// transforms are evaluated with explicit round-to-nearest operations in a fixed order, as the
+// oracle does, so transformed rays (and therefore hits) are bit-identical to the host's.
+GBPT_DI float xform_row(float4 r, float3 p, float w) {
+    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(r.x, p.x), __fmul_rn(r.y, p.y)),
+                               __fmul_rn(r.z, p.z)),
+                     __fmul_rn(r.w, w));
+}
+GBPT_DI float3 xform_point(float4 r0, float4 r1, float4 r2, float3 p) {
+    return f3(xform_row(r0, p, 1.0f), xform_row(r1, p, 1.0f), xform_row(r2, p, 1.0f));
+}
+GBPT_DI float3 xform_vector(float4 r0, float4 r1, float4 r2, float3 v) {
+    return f3(xform_row(r0, v, 0.0f), xform_row(r1, v, 0.0f), xform_row(r2, v, 0.0f));
 }
 
-// ---- persistent traversal -------------------------------------------------------------------------
-// Warps stay resident and pull rays from a global counter. A lane whose ray finished takes a new
-// one (one atomic per warp for all idle lanes); a warp leaves its inner loop to refill once fewer
-// than kRefillLanes lanes are still busy, and a lane postpones its pending triangle tests (pushes
-// the triangle group onto its stack) when fewer than kPostponeLanes lanes of the warp have
-// triangles to test, so node steps and triangle steps stay in lockstep across the warp. The
-// closest-hit result and the tie rule are the same as trace_ray's: only the visit order changes.
+// ---- traversal state and loop ------------------------------------------------------------------
+// One loop serves the per-thread queries (trace_ray) and the persistent warps (trace_persistent).
+// In the persistent form a lane postpones its pending triangle tests (pushes the triangle group
+// onto its stack) when fewer than kPostponeLanes lanes of the warp have triangles to test, so node
+// steps and triangle steps stay in lockstep across the warp, and the warp leaves the loop to refill
+// idle lanes once fewer than kRefillLanes lanes are busy. Two-level scenes: a top-level leaf is an
+// instance; entering it pushes what is left of the top level, transforms the ray to object space
+// (t is unchanged: the direction is not renormalised) and continues from the BLAS root; when the
+// stack drops back to the entry depth the world ray is restored. The closest hit and the tie rule
+// (equal t: smallest geometry, primitive, instance) do not depend on the visit order.
 #ifndef GBPT_SMEM_STACK
 #define GBPT_SMEM_STACK 0
 #endif
@@ -299,8 +190,9 @@ constexpr int kPostponeLanes = GBPT_POSTPONE_LANES;
 struct TraceState {
     const uint4* nodes;  // the ray's scene (rays of one launch may belong to different scenes)
     const float4* tris;
+    const float4* insts; // instance records; nullptr for single-level scenes
     uint32_t mask;       // instance mask of the ray
-    float3 o, d, inv;
+    float3 o, d, inv;    // the ray in the current space (object space inside an instance)
     float tmin;
     uint32_t oct_inv, oct_inv4;
     bool negx, negy, negz;
@@ -309,13 +201,15 @@ struct TraceState {
     int sp;
     Hit best;
     bool found;
+    float3 wo, wd; // the world ray
+    uint32_t inst; // instance being traversed, kNoInst at the top level
+    int inst_sp;   // stack depth at which it was entered
 };
 
-GBPT_DI void trace_init(TraceState& s, float3 o, float3 d, float tmin, float tmax) {
+GBPT_DI void set_ray(TraceState& s, float3 o, float3 d) {
     s.o = o;
     s.d = d;
     s.inv = f3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
-    s.tmin = tmin;
     const uint32_t oct = (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) |
                          ((__float_as_uint(d.z) >> 31) << 2);
     s.oct_inv = 7u - oct;
@@ -324,14 +218,37 @@ GBPT_DI void trace_init(TraceState& s, float3 o, float3 d, float tmin, float tma
     s.negy = (__float_as_uint(d.y) >> 31) != 0u;
     s.negz = (__float_as_uint(d.z) >> 31) != 0u;
     s.pre = ray_pre(o, d);
+}
+
+GBPT_DI void trace_init(TraceState& s, float3 o, float3 d, float tmin, float tmax) {
+    set_ray(s, o, d);
+    s.wo = o;
+    s.wd = d;
+    s.tmin = tmin;
     s.ngroup = make_uint2(0u, 0x80000000u);
     s.tgroup = make_uint2(0u, 0u);
     s.sp = 0;
     s.best.t = tmax;
     s.best.u = s.best.v = 0.0f;
-    s.best.prim = 0xFFFFFFFFu;
-    s.best.geom = 0xFFFFFFFFu;
+    s.best.prim = s.best.geom = s.best.inst = kNoInst;
     s.found = false;
+    s.inst = kNoInst;
+    s.inst_sp = -1;
+}
+
+GBPT_DI void enter_instance(TraceState& s, uint32_t ii) {
+    const float4* r = s.insts + 7ull * ii;
+    const float4 w0 = __ldg(r + 3), w1 = __ldg(r + 4), w2 = __ldg(r + 5);
+    set_ray(s, xform_point(w0, w1, w2, s.wo), xform_vector(w0, w1, w2, s.wd));
+    s.inst = ii;
+    s.inst_sp = s.sp;
+    s.ngroup = make_uint2(__float_as_uint(__ldg(r + 6).x), 0x80000000u);
+}
+
+GBPT_DI void exit_instance(TraceState& s) {
+    set_ray(s, s.wo, s.wd);
+    s.inst = kNoInst;
+    s.inst_sp = -1;
 }
 
 // Byte j of w as a float. With GBPT_BOX_PRMT the byte is placed in the mantissa of 2^23 with
@@ -350,6 +267,8 @@ GBPT_DI float qbyte(uint32_t w, int j) {
 
 // Intersects the 8 children of node `ni`; returns the hit mask (inner children in bits 24..31 in
 // traversal order, triangles in bits 0..23) and the node's child / triangle bases and imask.
+// The quantised planes are dequantised with a per-axis slack of 2^-20 of the plane distance
+// magnitude, so rounding never loses a child the exact box would keep.
 template <bool COUNT>
 GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& child_base,
                                 uint32_t& tri_base, uint32_t& imask, TraceCounters* ctr) {
@@ -406,11 +325,130 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
     return hitmask;
 }
 
-// Runs the traversal of every ray i < n, pulling indices from *fetch (zero before the launch).
-// load(i, state) sets ray i's scene (nodes, tris), mask and calls trace_init; store(i, hit)
-// receives its result (geom == 0xFFFFFFFF on miss; with ANY, the first hit found). Must be called
-// by all 32 lanes of every warp.
-template <bool ANY, bool COUNT, class Load, class Store>
+// Runs the traversal of the ray in s until it is finished (returns true; result in s.best, geom
+// = kNoInst on a miss; with ANY the first hit found) or, with WARP, until the warp should refill
+// its idle lanes (returns false; s keeps the state). `st(i)` is stack entry i. A stack overflow
+// raises *err and finishes the ray with what it found.
+template <bool ANY, bool COUNT, bool TWO_LEVEL, bool WARP, class StackRef>
+GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32_t* err,
+                        bool pool_empty) {
+    while (true) {
+        if (s.ngroup.y > 0x00FFFFFFu) {
+            const uint32_t hits = s.ngroup.y;
+            const uint32_t bit = 31u - __clz(hits & 0xFF000000u);
+            s.ngroup.y &= ~(1u << bit);
+            if (s.ngroup.y > 0x00FFFFFFu) {
+                if (s.sp >= kStackSize) {
+                    atomicOr(err, 1u);
+                    s.sp = 0;
+                    s.ngroup.y = 0;
+                    s.tgroup.y = 0;
+                    s.inst = kNoInst;
+                    break;
+                }
+                st(s.sp++) = s.ngroup;
+            }
+            const uint32_t slot = (bit - 24u) ^ s.oct_inv;
+            const uint32_t ni = s.ngroup.x + __popc((hits & 0xFFu) & ((1u << slot) - 1u));
+            uint32_t cb, tb, im;
+            const uint32_t hm = intersect_node<COUNT>(s, ni, cb, tb, im, ctr);
+            s.ngroup = make_uint2(cb, (hm & 0xFF000000u) | im);
+            s.tgroup = make_uint2(tb, hm & 0x00FFFFFFu);
+        } else {
+            // a postponed triangle group (or the rest of a top-level instance group) came off
+            // the stack
+            s.tgroup = s.ngroup;
+            s.ngroup = make_uint2(0u, 0u);
+        }
+        bool done_any = false;
+        // only groups followed by node work are postponed (a group popped back is tested)
+        const bool may_postpone = WARP && s.ngroup.y > 0x00FFFFFFu;
+        while (s.tgroup.y != 0u) {
+            if (may_postpone && s.sp < kStackSize && __popc(__activemask()) < kPostponeLanes) {
+                st(s.sp++) = s.tgroup;
+                s.tgroup.y = 0u;
+                break;
+            }
+            const uint32_t b = __ffs(s.tgroup.y) - 1u;
+            s.tgroup.y &= s.tgroup.y - 1u;
+            const uint32_t ti = s.tgroup.x + b;
+            if (TWO_LEVEL && s.insts != nullptr && s.inst == kNoInst) {
+                // a top-level leaf: an instance (record: instance index, mask in the flag word)
+                const uint32_t fl = __float_as_uint(__ldg(&s.tris[3 * ti + 2]).w);
+                if (((fl & 0xFFu) & s.mask) == 0u) continue;
+                if (s.sp + 2 > kStackSize) {
+                    atomicOr(err, 1u);
+                    s.tgroup.y = 0u;
+                    continue;
+                }
+                if (s.ngroup.y > 0x00FFFFFFu) st(s.sp++) = s.ngroup;
+                if (s.tgroup.y != 0u) st(s.sp++) = s.tgroup;
+                s.tgroup.y = 0u;
+                enter_instance(s, __float_as_uint(__ldg(&s.tris[3 * ti]).w));
+                break;
+            }
+            const float4 r0 = __ldg(&s.tris[3 * ti + 0]);
+            const float4 r1 = __ldg(&s.tris[3 * ti + 1]);
+            const float4 r2 = __ldg(&s.tris[3 * ti + 2]);
+            const uint32_t tfl = __float_as_uint(r2.w);
+            if (((tfl & 0xFFu) & s.mask) == 0u) continue;
+            if (COUNT) ctr->tris++;
+            float t, u, v;
+            if (!intersect_tri(s.pre, r0, r1, r2, tfl, s.tmin, s.best.t, t, u, v)) continue;
+            const uint32_t prim = __float_as_uint(r0.w), geom = __float_as_uint(r1.w);
+            if (t < s.best.t || geom < s.best.geom ||
+                (geom == s.best.geom &&
+                 (prim < s.best.prim || (prim == s.best.prim && s.inst < s.best.inst)))) {
+                s.best.t = t;
+                s.best.u = u;
+                s.best.v = v;
+                s.best.prim = prim;
+                s.best.geom = geom;
+                s.best.inst = s.inst;
+                s.found = true;
+                if (ANY) {
+                    done_any = true;
+                    break;
+                }
+            }
+        }
+        bool done = done_any;
+        if (!done && s.ngroup.y <= 0x00FFFFFFu) {
+            if (TWO_LEVEL && s.inst != kNoInst && s.sp == s.inst_sp) exit_instance(s);
+            if (s.sp == 0) done = true;
+            else s.ngroup = st(--s.sp);
+        }
+        if (done) break;
+        if (WARP && !pool_empty && __popc(__activemask()) < kRefillLanes) return false;
+    }
+    if (!s.found) s.best.geom = s.best.prim = s.best.inst = kNoInst;
+    return true;
+}
+
+// Closest hit (ANY = false) or first hit (ANY = true) of one ray, per thread. Sets *err when the
+// traversal stack would overflow (the builder bounds the depth, so this does not happen for
+// trees it accepted).
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ Hit trace_ray(const DevScene& sc, float3 o, float3 d, float tmin,
+                                         float tmax, uint32_t ray_mask, TraceCounters* ctr,
+                                         uint32_t* err) {
+    TraceState s;
+    s.nodes = sc.nodes;
+    s.tris = sc.tris;
+    s.insts = sc.n_inst ? sc.inst : nullptr;
+    s.mask = ray_mask;
+    trace_init(s, o, d, tmin, tmax);
+    uint2 stack[kStackSize];
+    trace_loop<ANY, COUNT, true, false>(s, [&](int i) -> uint2& { return stack[i]; }, ctr, err,
+                                        true);
+    return s.best;
+}
+
+// Runs the traversal of every ray i < n with persistent warps that pull ray indices from *fetch
+// (zero before the launch; one atomic per warp for all idle lanes). load(i, state) sets ray i's
+// scene (nodes, tris, insts), mask and calls trace_init; store(i, hit) receives its result. Must
+// be called by all 32 lanes of every warp.
+template <bool ANY, bool COUNT, bool TWO_LEVEL, class Load, class Store>
 __device__ __forceinline__ void trace_persistent(uint32_t n, uint32_t* fetch, Load load,
                                                  Store store, TraceCounters* ctr, uint32_t* err) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -450,87 +488,12 @@ __device__ __forceinline__ void trace_persistent(uint32_t n, uint32_t* fetch, Lo
             }
         }
         if (__ballot_sync(0xFFFFFFFFu, active) == 0u) break;
-        // once a lane found the pool empty, leaving the inner loop to refill gains nothing
+        // once a lane found the pool empty, leaving the loop to refill gains nothing
         const bool pool_empty = __ballot_sync(0xFFFFFFFFu, exhausted) != 0u;
         if (!active) continue;
-        // inner loop: node step, then (possibly postponed) triangle steps
-        while (true) {
-            if (s.ngroup.y > 0x00FFFFFFu) {
-                const uint32_t hits = s.ngroup.y;
-                const uint32_t bit = 31u - __clz(hits & 0xFF000000u);
-                s.ngroup.y &= ~(1u << bit);
-                if (s.ngroup.y > 0x00FFFFFFu) {
-                    if (s.sp >= kStackSize) {
-                        atomicOr(err, 1u);
-                        s.sp = 0;
-                        s.ngroup.y = 0;
-                        s.tgroup.y = 0;
-                        break;
-                    }
-                    st_ref(s.sp++) = s.ngroup;
-                }
-                const uint32_t slot = (bit - 24u) ^ s.oct_inv;
-                const uint32_t ni = s.ngroup.x + __popc((hits & 0xFFu) & ((1u << slot) - 1u));
-                uint32_t cb, tb, im;
-                const uint32_t hm = intersect_node<COUNT>(s, ni, cb, tb, im, ctr);
-                s.ngroup = make_uint2(cb, (hm & 0xFF000000u) | im);
-                s.tgroup = make_uint2(tb, hm & 0x00FFFFFFu);
-            } else {
-                // a postponed triangle group came off the stack
-                s.tgroup = s.ngroup;
-                s.ngroup = make_uint2(0u, 0u);
-            }
-            bool done_any = false;
-            // only groups followed by node work are postponed (a group popped back is tested)
-            const bool may_postpone = s.ngroup.y > 0x00FFFFFFu;
-            while (s.tgroup.y != 0u) {
-                if (may_postpone && s.sp < kStackSize &&
-                    __popc(__activemask()) < kPostponeLanes) {
-                    st_ref(s.sp++) = s.tgroup;
-                    s.tgroup.y = 0u;
-                    break;
-                }
-                const uint32_t b = __ffs(s.tgroup.y) - 1u;
-                s.tgroup.y &= s.tgroup.y - 1u;
-                const uint32_t ti = s.tgroup.x + b;
-                const float4 r0 = __ldg(&s.tris[3 * ti + 0]);
-                const float4 r1 = __ldg(&s.tris[3 * ti + 1]);
-                const float4 r2 = __ldg(&s.tris[3 * ti + 2]);
-                const uint32_t tfl = __float_as_uint(r2.w);
-                if (((tfl & 0xFFu) & s.mask) == 0u) continue;
-                if (COUNT) ctr->tris++;
-                float t, u, v;
-                if (!intersect_tri(s.pre, r0, r1, r2, tfl, s.tmin, s.best.t, t, u, v)) continue;
-                const uint32_t prim = __float_as_uint(r0.w), geom = __float_as_uint(r1.w);
-                if (t < s.best.t || geom < s.best.geom ||
-                    (geom == s.best.geom && prim < s.best.prim)) {
-                    s.best.t = t;
-                    s.best.u = u;
-                    s.best.v = v;
-                    s.best.prim = prim;
-                    s.best.geom = geom;
-                    s.found = true;
-                    if (ANY) {
-                        done_any = true;
-                        break;
-                    }
-                }
-            }
-            bool done = done_any;
-            if (!done && s.ngroup.y <= 0x00FFFFFFu) {
-                if (s.sp == 0) done = true;
-                else s.ngroup = st_ref(--s.sp);
-            }
-            if (done) {
-                if (!s.found) {
-                    s.best.geom = 0xFFFFFFFFu;
-                    s.best.prim = 0xFFFFFFFFu;
-                }
-                store(ray, s.best);
-                active = false;
-                break;
-            }
-            if (!pool_empty && __popc(__activemask()) < kRefillLanes) break;
+        if (trace_loop<ANY, COUNT, TWO_LEVEL, true>(s, st_ref, ctr, err, pool_empty)) {
+            store(ray, s.best);
+            active = false;
         }
     }
 }

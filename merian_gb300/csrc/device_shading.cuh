@@ -30,7 +30,44 @@ inline DevScene make_dev_scene(const SceneGPU& s) {
     d.n_lights = s.n_lights;
     d.light_total = s.light_total;
     d.p_env = d.ew ? (s.n_lights ? 0.5f : 1.0f) : 0.0f;
+    d.inst = (const float4*)s.inst;
+    d.n_inst = s.n_inst;
+    d.tex = (const uchar4*)s.tex;
+    d.tex_info = (const uint4*)s.tex_info;
+    d.n_tex = s.n_tex;
+    d.srgb_lut = (const float*)s.srgb_lut;
     return d;
+}
+
+// Bilinear lookup with repeat addressing at level 0 (merian's DefaultLODSampler = LOD0Sampler,
+// textures.slang:338-423, on a linear/repeat sampler): texel centres at (i + 0.5) / size; an sRGB
+// texture is decoded per texel before filtering, as the hardware does for sRGB formats.
+GBPT_DI float4 texture_sample(const DevScene& sc, uint32_t t, float u, float v) {
+    const uint4 info = __ldg(&sc.tex_info[t]);
+    const int w = (int)info.y, h = (int)info.z;
+    const float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
+    const float fx = floorf(x), fy = floorf(y);
+    const float a = x - fx, b = y - fy;
+    const int ix = (int)fx, iy = (int)fy;
+    const int x0 = ((ix % w) + w) % w, x1 = (((ix + 1) % w) + w) % w;
+    const int y0 = ((iy % h) + h) % h, y1 = (((iy + 1) % h) + h) % h;
+    const uchar4* base = sc.tex + info.x;
+    auto texel = [&](int xx, int yy) {
+        const uchar4 c = __ldg(&base[(size_t)yy * w + xx]);
+        if (info.w)
+            return make_float4(__ldg(&sc.srgb_lut[c.x]), __ldg(&sc.srgb_lut[c.y]),
+                               __ldg(&sc.srgb_lut[c.z]), (float)c.w * (1.0f / 255.0f));
+        return make_float4((float)c.x * (1.0f / 255.0f), (float)c.y * (1.0f / 255.0f),
+                           (float)c.z * (1.0f / 255.0f), (float)c.w * (1.0f / 255.0f));
+    };
+    const float4 t00 = texel(x0, y0), t10 = texel(x1, y0), t01 = texel(x0, y1), t11 = texel(x1, y1);
+    auto mix = [&](float c00, float c10, float c01, float c11) {
+        const float top = c00 * (1.0f - a) + c10 * a;
+        const float bot = c01 * (1.0f - a) + c11 * a;
+        return top * (1.0f - b) + bot * b;
+    };
+    return make_float4(mix(t00.x, t10.x, t01.x, t11.x), mix(t00.y, t10.y, t01.y, t11.y),
+                       mix(t00.z, t10.z, t01.z, t11.z), mix(t00.w, t10.w, t01.w, t11.w));
 }
 
 // Appends one entry per lane that wants one; one atomic per warp. All 32 lanes must call it.
@@ -48,6 +85,7 @@ GBPT_DI uint32_t warp_append(uint32_t* counter, bool want) {
 // ---- shading points (scene.slang:312-498) -----------------------------------------------------------
 struct SPd {
     float3 pos;
+    float3 tex_color; // base colour texture at the hit (1 without a texture)
     uint32_t enc_fn;
     float3 fn;        // exact face normal (FlipFacing applied), for light pdfs
     float3 emission;
@@ -67,6 +105,7 @@ GBPT_DI SPd env_sp(const DevScene& sc, float3 o, float3 d) {
     sp.fn = -d;
     sp.emission = env_eval(sc, d);
     sp.frame = frame_from_normal(-d);
+    sp.tex_color = f3(1.f, 1.f, 1.f);
     sp.mat = 0;
     sp.has_material = false;
     sp.front = true;
@@ -87,8 +126,11 @@ GBPT_DI void load_vertex(const DevScene& sc, uint32_t vi, float3& p, uint32_t& e
 
 // get_triangle_hit + get_surface + get_shading_point (scene.slang:312-456), material instantiated
 // later by the scatter step
+// A two-level hit (inst != kNoInst) is transformed to world space as scene.slang:235-259 does:
+// position by the object-to-world transform, edges and tangents by its linear part, the
+// interpolated normal by the inverse transpose (renormalised).
 GBPT_DI SPd surface_sp(const DevScene& sc, float3 o, float3 d, uint32_t geom, uint32_t prim,
-                       float bu, float bv) {
+                       float bu, float bv, uint32_t inst = kNoInst) {
     const GeomGPU g = sc.geoms[geom];
     if (g.flags & GBPT_MESH_USE_ENV_MAP) return env_sp(sc, o, d);
     const uint32_t tri = g.first_triangle + prim;
@@ -101,8 +143,24 @@ GBPT_DI SPd surface_sp(const DevScene& sc, float3 o, float3 d, uint32_t geom, ui
     load_vertex(sc, i1, p1, n1, uv1, t1);
     load_vertex(sc, i2, p2, n2, uv2, t2);
     const float b0 = 1.0f - bu - bv, b1 = bu, b2 = bv;
-    const float3 pos = (b0 * p0 + b1 * p1) + b2 * p2;
-    const float3 e01 = p1 - p0, e02 = p2 - p0;
+    const bool xf = inst != kNoInst;
+    float4 x0, x1, x2, w0r, w1r, w2r;
+    if (xf) {
+        const float4* r = sc.inst + 7ull * inst;
+        x0 = __ldg(r + 0);
+        x1 = __ldg(r + 1);
+        x2 = __ldg(r + 2);
+        w0r = __ldg(r + 3);
+        w1r = __ldg(r + 4);
+        w2r = __ldg(r + 5);
+    }
+    float3 pos = (b0 * p0 + b1 * p1) + b2 * p2;
+    float3 e01 = p1 - p0, e02 = p2 - p0;
+    if (xf) {
+        pos = xform_point(x0, x1, x2, pos);
+        e01 = xform_vector(x0, x1, x2, e01);
+        e02 = xform_vector(x0, x1, x2, e02);
+    }
     float3 fn = normalize(cross(e01, e02));
     if (g.flags & GBPT_MESH_FLIP_FACING) fn = -fn;
     float3 vn;
@@ -110,6 +168,11 @@ GBPT_DI SPd surface_sp(const DevScene& sc, float3 o, float3 d, uint32_t geom, ui
         vn = fn;
     } else {
         vn = normalize((b0 * decode_normal(n0) + b1 * decode_normal(n1)) + b2 * decode_normal(n2));
+        if (xf) { // inverse transpose: the columns of the world-to-object rows
+            vn = normalize(f3(w0r.x * vn.x + w1r.x * vn.y + w2r.x * vn.z,
+                              w0r.y * vn.x + w1r.y * vn.y + w2r.y * vn.z,
+                              w0r.z * vn.x + w1r.z * vn.y + w2r.z * vn.z));
+        }
     }
     Frame frame;
     if (g.flags & GBPT_MESH_HAS_TANGENTS) {
@@ -118,7 +181,9 @@ GBPT_DI SPd surface_sp(const DevScene& sc, float3 o, float3 d, uint32_t geom, ui
         const float3 t = (b0 * decode_normal(t0 & ~1u) + b1 * decode_normal(t1 & ~1u)) +
                          b2 * decode_normal(t2 & ~1u);
         const float tw = (b0 * w0 + b1 * w1) + b2 * w2;
-        frame = frame_from_tangent(vn, normalize(t), signf(tw));
+        float3 tn = normalize(t);
+        if (xf) tn = xform_vector(x0, x1, x2, tn);
+        frame = frame_from_tangent(vn, tn, signf(tw));
     } else {
         const float d1x = half_lo(uv1) - half_lo(uv0), d1y = half_hi(uv1) - half_hi(uv0);
         const float d2x = half_lo(uv2) - half_lo(uv0), d2y = half_hi(uv2) - half_hi(uv0);
@@ -141,6 +206,16 @@ GBPT_DI SPd surface_sp(const DevScene& sc, float3 o, float3 d, uint32_t geom, ui
     sp.enc_fn = encode_normal(fn);
     sp.fn = fn;
     sp.mat = g.material;
+    sp.tex_color = f3(1.f, 1.f, 1.f);
+    if (sc.n_tex) { // the base colour texture (the material header's alpha texture)
+        const int tex = (int)__float_as_uint(__ldg(&sc.mats[5 * g.material + 4]).x);
+        if (tex >= 0 && (uint32_t)tex < sc.n_tex) {
+            const float u = (b0 * half_lo(uv0) + b1 * half_lo(uv1)) + b2 * half_lo(uv2);
+            const float v = (b0 * half_hi(uv0) + b1 * half_hi(uv1)) + b2 * half_hi(uv2);
+            const float4 c = texture_sample(sc, (uint32_t)tex, u, v);
+            sp.tex_color = f3(c.x, c.y, c.z);
+        }
+    }
     sp.front = front;
     sp.env = false;
     const float4 m0 = __ldg(&sc.mats[5 * g.material + 0]);
@@ -155,10 +230,15 @@ GBPT_DI SPd surface_sp(const DevScene& sc, float3 o, float3 d, uint32_t geom, ui
 }
 
 // OpenPBRMaterial::get_sample / DiffuseMaterial::get_sample for this shading point
-GBPT_DI Material load_material(const DevScene& sc, uint32_t mid, bool front, float ior) {
-    return material_from_record(__ldg(&sc.mats[5 * mid + 0]), __ldg(&sc.mats[5 * mid + 1]),
-                                __ldg(&sc.mats[5 * mid + 2]), __ldg(&sc.mats[5 * mid + 3]), front,
-                                ior);
+// tex: the base colour texture at the shading point, multiplying base_color
+// (diffuse-material.slang:25-29, openpbr-material.slang:114-116)
+GBPT_DI Material load_material(const DevScene& sc, uint32_t mid, bool front, float ior,
+                               float3 tex = f3(1.f, 1.f, 1.f)) {
+    Material m = material_from_record(__ldg(&sc.mats[5 * mid + 0]), __ldg(&sc.mats[5 * mid + 1]),
+                                      __ldg(&sc.mats[5 * mid + 2]), __ldg(&sc.mats[5 * mid + 3]),
+                                      front, ior);
+    m.base = m.base * tex;
+    return m;
 }
 
 // ---- lights (next-event estimation; not in the reference, same expectation) ---------------------------

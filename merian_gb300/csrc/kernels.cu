@@ -15,6 +15,24 @@ std::string cuda_error_string(cudaError_t e) { return std::string(cudaGetErrorSt
 
 namespace {
 
+// merian's Hit (hit.slang:25-65): for two-level hits the custom index of the instance (the first
+// geometry of its BLAS), the TLAS instance and the geometry within the BLAS; misses all ~0.
+GBPT_DI gbpt_hit to_hit(const DevScene& sc, const Hit& h) {
+    gbpt_hit out;
+    const bool ok = h.geom != kNoInst;
+    uint32_t first = 0;
+    if (ok && h.inst != kNoInst) first = __float_as_uint(__ldg(&sc.inst[7ull * h.inst + 6]).z);
+    out.instance_id = ok ? first : kNoInst;
+    out.instance_index = ok ? (h.inst == kNoInst ? 0u : h.inst) : kNoInst;
+    out.primitive_id = h.prim;
+    out.geometry_index = ok ? h.geom - first : kNoInst;
+    out.barycentrics[0] = ok ? h.u : 0.f;
+    out.barycentrics[1] = ok ? h.v : 0.f;
+    out.t = ok ? h.t : -1.0f;
+    out.reserved = 0;
+    return out;
+}
+
 // The caller's rays through the persistent traversal (the closest hit or, with ANY, any hit).
 template <bool ANY>
 __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
@@ -25,24 +43,13 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
         const gbpt_ray r = rays[i];
         s.nodes = sc.nodes;
         s.tris = sc.tris;
+        s.insts = sc.n_inst ? sc.inst : nullptr;
         s.mask = mask;
         trace_init(s, f3(r.origin[0], r.origin[1], r.origin[2]),
                    f3(r.direction[0], r.direction[1], r.direction[2]), r.tmin, r.tmax);
     };
-    auto store = [&](uint32_t i, const Hit& h) {
-        gbpt_hit out;
-        const bool ok = h.geom != 0xFFFFFFFFu;
-        out.instance_id = ok ? 0u : 0xFFFFFFFFu;
-        out.instance_index = ok ? 0u : 0xFFFFFFFFu;
-        out.primitive_id = h.prim;
-        out.geometry_index = h.geom;
-        out.barycentrics[0] = ok ? h.u : 0.f;
-        out.barycentrics[1] = ok ? h.v : 0.f;
-        out.t = ok ? h.t : -1.0f;
-        out.reserved = 0;
-        hits[i] = out;
-    };
-    trace_persistent<ANY, true>(n, fetch, load, store, &ctr, err);
+    auto store = [&](uint32_t i, const Hit& h) { hits[i] = to_hit(sc, h); };
+    trace_persistent<ANY, true, true>(n, fetch, load, store, &ctr, err);
     if (work_ctr) {
         atomicAdd(work_ctr + 0, (unsigned long long)ctr.nodes);
         atomicAdd(work_ctr + 1, (unsigned long long)ctr.tris);
@@ -57,18 +64,7 @@ __global__ void k_trace_primary(DevScene sc, CamGPU cam, uint32_t w, uint32_t h,
     float3 o, d;
     float tmin, tmax;
     camera_ray(cam, i % w, i / w, w, h, o, d, tmin, tmax);
-    const Hit ht = trace_ray<false, false>(sc, o, d, tmin, tmax, mask, nullptr, err);
-    gbpt_hit out;
-    const bool ok = ht.geom != 0xFFFFFFFFu;
-    out.instance_id = ok ? 0u : 0xFFFFFFFFu;
-    out.instance_index = ok ? 0u : 0xFFFFFFFFu;
-    out.primitive_id = ht.prim;
-    out.geometry_index = ht.geom;
-    out.barycentrics[0] = ok ? ht.u : 0.f;
-    out.barycentrics[1] = ok ? ht.v : 0.f;
-    out.t = ok ? ht.t : -1.0f;
-    out.reserved = 0;
-    hits[i] = out;
+    hits[i] = to_hit(sc, trace_ray<false, false>(sc, o, d, tmin, tmax, mask, nullptr, err));
 }
 
 GBPT_DI uint32_t pack_half2_rn(float lo, float hi) {
@@ -98,17 +94,18 @@ __global__ void k_gbuffer(DevScene sc, CamGPU cam, uint32_t w, uint32_t h, uint3
     const Hit ht = trace_ray<false, false>(sc, o, d, tmin, tmax, mask, nullptr, err);
     gbpt_gbuffer_texel t;
     const bool hit = ht.geom != 0xFFFFFFFFu;
-    t.instance_id = hit ? 0u : 0xFFFFFFFFu;
-    t.primitive_id = ht.prim;
-    t.geometry_index = (uint16_t)ht.geom;
-    t.instance_index = hit ? (uint16_t)0 : (uint16_t)0xFFFFu;
+    const gbpt_hit ph = to_hit(sc, ht);
+    t.instance_id = ph.instance_id;
+    t.primitive_id = ph.primitive_id;
+    t.geometry_index = (uint16_t)ph.geometry_index;
+    t.instance_index = (uint16_t)ph.instance_index;
     t.barycentrics = hit ? pack_half2_rn(ht.u, ht.v) : 0u;
     t.motion[0] = t.motion[1] = 0.0f;
     t.grad_z = 0u;
     t.delta_z = 0.0f;
     SPd sp;
     if (!hit || ht.geom >= sc.geom_count) sp = env_sp(sc, o, d);
-    else sp = surface_sp(sc, o, d, ht.geom, ht.prim, ht.u, ht.v);
+    else sp = surface_sp(sc, o, d, ht.geom, ht.prim, ht.u, ht.v, ht.inst);
     const float lz = length(sp.pos - o);
     t.linear_z = fminf(lz, 65504.0f);
     t.encoded_normal = encode_normal(sp.frame.n);
@@ -120,7 +117,7 @@ __global__ void k_gbuffer(DevScene sc, CamGPU cam, uint32_t w, uint32_t h, uint3
         const float gy = n_dot_oo / dot(sp.fn, pinhole_direction(cam, px, py + 1, w, h)) - lz;
         t.grad_z = pack_half2_rn(gx, gy);
         t.delta_z = length(sp.pos - cam.pos) - lz;
-        const Material m = load_material(sc, sp.mat, sp.front, 1.0f);
+        const Material m = load_material(sc, sp.mat, sp.front, 1.0f, sp.tex_color);
         albedo = material_albedo(m, sp.frame.to_local(-d));
     }
     t.albedo[0] = albedo.x;
@@ -192,9 +189,12 @@ static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBy
 namespace {
 constexpr uint64_t kStaticCounterBytes = 256; // 16 counters + 8 stats words, padded
 constexpr uint64_t kStaticPixelBytes = (uint64_t)kStaticMaxPixelList * 4;
-// per path: throughput, radiance (16 + 16), rng (4), two ray queues (2 x 36), hits (20),
-// shadow queue (52); plus a 96-byte primary point per pixel, budgeted as one pixel per path
-constexpr uint64_t kStaticBytesPerPath = 16 + 16 + 4 + 2 * (32 + 4) + (16 + 4) + (32 + 16 + 4) + 96;
+// per path: throughput, radiance (16 + 16), rng (4), two ray queues (2 x 36), hits (24),
+// shadow queue (52); plus a 112-byte primary point per pixel, budgeted as one pixel per path
+constexpr uint64_t kStaticBytesPerPath =
+    16 + 16 + 4 + 2 * (32 + 4) + (16 + 4 + 4) + (32 + 16 + 4) + 16 * kPixFloat4;
+// alignment padding of the carved arrays, and the tick tables of a one-request render
+constexpr uint64_t kStaticSlackBytes = 16 * 256 + 1024;
 
 std::mutex g_static_mu;
 void* g_static_ptr[64] = {};
@@ -215,8 +215,8 @@ int static_scratch_address(int dev, unsigned char** out) {
 } // namespace
 
 uint64_t static_scratch_paths() {
-    // 16 x 256 bytes of slack for the alignment of the carved arrays and the request tables
-    return (kStaticScratchBytes - kStaticCounterBytes - kStaticPixelBytes - 16 * 256) /
+    // kStaticSlackBytes for the alignment of the carved arrays and the tick tables
+    return (kStaticScratchBytes - kStaticCounterBytes - kStaticPixelBytes - kStaticSlackBytes) /
            kStaticBytesPerPath;
 }
 
@@ -270,10 +270,11 @@ int render_frame_static(const SceneGPU& scene, const RenderArgs& args, const uin
     carve(w.q_path[1], N);
     carve(w.hit_tuv, N);
     carve(w.hit_geom, N);
+    carve(w.hit_inst, N);
     carve(w.s_od, 2 * N);
     carve(w.s_contrib, N);
     carve(w.s_path, N);
-    carve(w.pix, 6 * N);
+    carve(w.pix, kPixFloat4 * N);
     const uint64_t used = (uint64_t)(p - base);
     if (used + tick_table_bytes(1) > kStaticScratchBytes) {
         err = "static scratch layout overflow";

@@ -34,6 +34,16 @@ struct SceneGPU {
     float env_func_int = 0.0f;
     uint32_t n_lights = 0;
     float light_total = 0.0f;
+    // two-level scenes: 7 float4 per instance (object-to-world and world-to-object rows, BLAS
+    // root / mask / first geometry); the TLAS is the first tree of `nodes`, its leaves the first
+    // records of `tris`
+    void* inst = nullptr;
+    uint32_t n_inst = 0;
+    // RGBA8 textures
+    void* tex = nullptr;
+    void* tex_info = nullptr; // uint4 per texture: first texel, width, height, sRGB
+    void* srgb_lut = nullptr; // 256 floats
+    uint32_t n_tex = 0;
     uint32_t depth = 0;
     uint64_t bytes = 0;
 };
@@ -54,17 +64,22 @@ struct Work {
     uint32_t* q_path[2] = {nullptr, nullptr};
     float4* hit_tuv = nullptr; // t, u, v, primitive bits
     uint32_t* hit_geom = nullptr;
+    uint32_t* hit_inst = nullptr; // instance of two-level hits, 0xFFFFFFFF otherwise
     // shadow queue
     float4* s_od = nullptr;     // 2 float4 per entry: (o, tmax), (d, 0)
     float4* s_contrib = nullptr;
     uint32_t* s_path = nullptr;
-    // per-pixel primary shading point cache (5 float4 per pixel)
+    // material-sorted shading: key per queue entry and the sorted order (absent in fixed Work)
+    uint8_t* keys = nullptr;
+    uint32_t* perm = nullptr;
+    // per-pixel primary shading point cache (kPixFloat4 float4 per pixel)
     float4* pix = nullptr;
     uint32_t* pix_id = nullptr; // pixel ids of the current request (device)
     uint64_t pix_id_cap = 0;
     float4* out = nullptr;      // device output staging for host-output renders
     uint64_t out_cap = 0;
-    // counters: [0],[1] queue counts, [2] shadow count, [3] error flags, [4],[5] fetch cursors
+    // counters: [0],[1] queue counts, [2] shadow count, [3] error flags, [4],[5] fetch cursors,
+    // [8..11] material-key counts, [12..15] their scatter cursors
     uint32_t* counters = nullptr;
     unsigned long long* stats = nullptr; // [0] rays, [1] shadow rays, [2] closest-hit rays
     // request, scene and tick tables of the batch being rendered
@@ -86,6 +101,10 @@ struct BatchItem {
 
 // Paths per wave: 8 Mi paths keep ~1.5 GB of path state and queues resident.
 constexpr uint64_t kWavePaths = 1ull << 23;
+// float4 per pixel of the primary shading point cache: position + encoded face normal, frame
+// (n + material, t + flags, b + demodulation r), emission + demodulation g, ray direction +
+// demodulation b, base colour texture
+constexpr uint64_t kPixFloat4 = 7;
 
 // Optional per-kernel timing (CUDA events around each launch) and traversal work counters.
 struct Profile {
@@ -148,8 +167,10 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
 // other items in the batch, bit for bit.
 int render_batch(TickEngine& e, const BatchItem* items, uint32_t n_items, uint64_t* launches,
                  Profile* prof, unsigned long long* work_ctr);
+// wave: paths per tick, 0 = kWavePaths
 int render_frame(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
-                 uint64_t* launches, Profile* prof, unsigned long long* work_ctr);
+                 uint64_t* launches, Profile* prof, unsigned long long* work_ctr,
+                 uint64_t wave = 0);
 int primary_points(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
                    float* out_device);
 // Bytes of tick tables for ticks of at most max_chunks requests.

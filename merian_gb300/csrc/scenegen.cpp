@@ -5,6 +5,7 @@
 #include "host_common.h"
 
 #include <cmath>
+#include <vector>
 
 namespace gbpt {
 namespace {
@@ -320,6 +321,147 @@ extern "C" GBPT_API int gbpt_gen_env(uint64_t seed, uint32_t width, uint32_t hei
             t[1] = (float)rgb[1];
             t[2] = (float)rgb[2];
             t[3] = 1.0f;
+        }
+    }
+    return GBPT_OK;
+}
+
+// ---- the instanced configuration: bumpy closed meshes and value-noise textures -------------------
+namespace gbpt {
+namespace {
+
+// integer lattice hash -> [0, 1)
+inline float lattice(uint32_t seed, int x, int y, int z) {
+    uint32_t h = seed ^ 0x9E3779B9u;
+    h = (h ^ (uint32_t)x) * 0x85EBCA6Bu;
+    h = (h ^ (uint32_t)y) * 0xC2B2AE35u;
+    h = (h ^ (uint32_t)z) * 0x27D4EB2Fu;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+inline float smooth(float t) { return t * t * (3.0f - 2.0f * t); }
+inline float lerpf(float a, float b, float t) { return a + (b - a) * t; }
+
+// trilinear value noise with smoothstep weights; coordinates wrap with `period` (0 = none)
+float value_noise(uint32_t seed, float x, float y, float z, int period) {
+    const float fx = std::floor(x), fy = std::floor(y), fz = std::floor(z);
+    int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+    const float tx = smooth(x - fx), ty = smooth(y - fy), tz = smooth(z - fz);
+    auto wrap = [&](int i) { return period > 0 ? ((i % period) + period) % period : i; };
+    float c[2][2][2];
+    for (int dz = 0; dz < 2; ++dz)
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx)
+                c[dz][dy][dx] = lattice(seed, wrap(ix + dx), wrap(iy + dy), wrap(iz + dz));
+    const float x00 = lerpf(c[0][0][0], c[0][0][1], tx), x01 = lerpf(c[0][1][0], c[0][1][1], tx);
+    const float x10 = lerpf(c[1][0][0], c[1][0][1], tx), x11 = lerpf(c[1][1][0], c[1][1][1], tx);
+    return lerpf(lerpf(x00, x01, ty), lerpf(x10, x11, ty), tz);
+}
+
+} // namespace
+} // namespace gbpt
+
+// A closed bumpy sphere: an (n_u + 1) x n_v latitude-longitude vertex grid (the seam column
+// duplicated for continuous uv, the pole rows collapsed), radius 1 + 0.35 * (two octaves of value
+// noise - 0.5), smooth per-vertex normals (area-weighted face normals), uv = (i / n_u,
+// j / (n_v - 1)); 2 n_u (n_v - 1) triangles, counter-clockwise seen from outside.
+extern "C" GBPT_API int gbpt_gen_blob(uint64_t seed, uint32_t n_u, uint32_t n_v,
+                                      gbpt_packed_vertex* vertices, uint32_t* indices) {
+    if (!vertices || !indices || n_u < 3 || n_v < 3 || (uint64_t)(n_u + 1) * n_v > (1u << 30)) {
+        set_error("gbpt_gen_blob: invalid arguments");
+        return GBPT_ERR_INVALID;
+    }
+    const uint32_t s32 = (uint32_t)(seed ^ (seed >> 32));
+    const uint32_t nvert = (n_u + 1) * n_v;
+    std::vector<V3> pos(nvert), nrm(nvert, v3(0, 0, 0));
+    for (uint32_t j = 0; j < n_v; ++j) {
+        const double theta = 3.14159265358979323846 * (double)j / (double)(n_v - 1);
+        double st, ct;
+        det::sincos(theta, st, ct);
+        for (uint32_t i = 0; i <= n_u; ++i) {
+            const double phi = 2.0 * 3.14159265358979323846 * (double)(i % n_u) / (double)n_u;
+            double sp, cp;
+            det::sincos(phi, sp, cp);
+            const V3 dir = v3((float)(st * cp), (float)ct, (float)(st * sp));
+            const float n1 = value_noise(s32, 2.0f * dir.x + 4.0f, 2.0f * dir.y + 4.0f, 2.0f * dir.z + 4.0f, 0);
+            const float n2 = value_noise(s32 ^ 0xA5A5u, 5.0f * dir.x + 8.0f, 5.0f * dir.y + 8.0f, 5.0f * dir.z + 8.0f, 0);
+            const float r = 1.0f + 0.35f * ((0.7f * n1 + 0.3f * n2) - 0.5f);
+            pos[j * (n_u + 1) + i] = r * dir;
+        }
+    }
+    uint32_t t = 0;
+    for (uint32_t j = 0; j + 1 < n_v; ++j) {
+        for (uint32_t i = 0; i < n_u; ++i) {
+            const uint32_t a = j * (n_u + 1) + i, b = a + 1, c = a + (n_u + 1), d = c + 1;
+            // (a, c, b) and (b, c, d) wind counter-clockwise seen from outside
+            const uint32_t tri[2][3] = {{a, c, b}, {b, c, d}};
+            for (int k = 0; k < 2; ++k) {
+                indices[3 * t + 0] = tri[k][0];
+                indices[3 * t + 1] = tri[k][1];
+                indices[3 * t + 2] = tri[k][2];
+                const V3 n = cross(pos[tri[k][1]] - pos[tri[k][0]], pos[tri[k][2]] - pos[tri[k][0]]);
+                for (int q = 0; q < 3; ++q) nrm[tri[k][q]] = nrm[tri[k][q]] + n;
+                ++t;
+            }
+        }
+    }
+    // the seam column shares its normals with column 0, the poles average their ring
+    for (uint32_t j = 0; j < n_v; ++j) {
+        V3& n0 = nrm[j * (n_u + 1)];
+        V3& n1 = nrm[j * (n_u + 1) + n_u];
+        const V3 s = n0 + n1;
+        n0 = s;
+        n1 = s;
+    }
+    for (uint32_t j : {0u, n_v - 1}) {
+        V3 s = v3(0, 0, 0);
+        for (uint32_t i = 0; i <= n_u; ++i) s = s + nrm[j * (n_u + 1) + i];
+        for (uint32_t i = 0; i <= n_u; ++i) nrm[j * (n_u + 1) + i] = s;
+    }
+    for (uint32_t j = 0; j < n_v; ++j) {
+        for (uint32_t i = 0; i <= n_u; ++i) {
+            const uint32_t k = j * (n_u + 1) + i;
+            gbpt_packed_vertex& v = vertices[k];
+            v.position[0] = pos[k].x;
+            v.position[1] = pos[k].y;
+            v.position[2] = pos[k].z;
+            const V3 n = dot(nrm[k], nrm[k]) > 0.0f ? normalize(nrm[k]) : normalize(pos[k]);
+            v.encoded_normal = encode_normal(n);
+            v.uv = pack_half2((float)i / (float)n_u, (float)j / (float)(n_v - 1));
+            v.encoded_tangent = 0;
+        }
+    }
+    return GBPT_OK;
+}
+
+// A tileable RGBA8 value-noise texture: two octaves of 2D value noise (period 8 and 16 lattice
+// cells) blending two seeded colours, sRGB-encoded, alpha 255.
+extern "C" GBPT_API int gbpt_gen_noise_texture(uint64_t seed, uint32_t width, uint32_t height,
+                                               uint8_t* rgba) {
+    if (!rgba || width == 0 || height == 0) {
+        set_error("gbpt_gen_noise_texture: invalid arguments");
+        return GBPT_ERR_INVALID;
+    }
+    Pcg32 rng(seed, 0x7E7u);
+    float c0[3], c1[3];
+    for (float& c : c0) c = 0.1f + 0.8f * rng.uniform();
+    for (float& c : c1) c = 0.1f + 0.8f * rng.uniform();
+    const uint32_t s32 = (uint32_t)(seed ^ (seed >> 32));
+    auto to_srgb8 = [](float x) {
+        x = std::fmin(std::fmax(x, 0.0f), 1.0f);
+        const double e = x <= 0.0031308 ? 12.92 * x : 1.055 * std::pow((double)x, 1.0 / 2.4) - 0.055;
+        return (uint8_t)std::lround(e * 255.0);
+    };
+    for (uint32_t y = 0; y < height; ++y) {
+        for (uint32_t x = 0; x < width; ++x) {
+            const float u = (float)x / (float)width, v = (float)y / (float)height;
+            const float n = 0.65f * value_noise(s32, 8.0f * u, 8.0f * v, 0.0f, 8) +
+                            0.35f * value_noise(s32 ^ 0x5Au, 16.0f * u, 16.0f * v, 0.0f, 16);
+            uint8_t* p = rgba + 4 * ((size_t)y * width + x);
+            for (int c = 0; c < 3; ++c) p[c] = to_srgb8(c0[c] + (c1[c] - c0[c]) * n);
+            p[3] = 255;
         }
     }
     return GBPT_OK;

@@ -32,6 +32,10 @@ constexpr uint32_t kMaxChunks = 256;
 constexpr uint64_t kMaxWavePaths = 1ull << kPathBits;
 static_assert(kWavePaths <= kMaxWavePaths, "path ids must fit the packed queue entry");
 
+// resident 128-thread blocks per SM the shading kernels are register-budgeted for
+// (65536 / (5 * 128) = 102 registers per thread)
+constexpr int kShadeBlocksPerSM = 5;
+
 constexpr uint32_t kReqEmission = 1u, kReqNee = 2u, kReqDemodulate = 4u;
 
 struct ReqGPU {
@@ -56,8 +60,10 @@ struct ChunkGPU {
     uint32_t mask;
     const uint4* nodes; // the scene's traversal data, for the trace kernels
     const float4* tris;
+    const float4* insts; // instance records of a two-level scene, else nullptr
+    uint64_t pad;
 };
-static_assert(sizeof(ChunkGPU) == 48, "chunk layout");
+static_assert(sizeof(ChunkGPU) == 64, "chunk layout");
 
 struct TickHeader {
     uint32_t n_chunks, n_pix, n_paths, pad;
@@ -112,9 +118,9 @@ __global__ void __launch_bounds__(128) k_primary(TickArgs t) {
         if (h.geom == 0xFFFFFFFFu || h.geom >= sc.geom_count) {
             sp = env_sp(sc, o, d);
         } else {
-            sp = surface_sp(sc, o, d, h.geom, h.prim, round_half(h.u), round_half(h.v));
+            sp = surface_sp(sc, o, d, h.geom, h.prim, round_half(h.u), round_half(h.v), h.inst);
         }
-        float4* pc = t.w.pix + 6ull * q;
+        float4* pc = t.w.pix + kPixFloat4 * q;
         pc[0] = make_float4(sp.pos.x, sp.pos.y, sp.pos.z, __uint_as_float(sp.enc_fn));
         pc[1] = make_float4(sp.frame.n.x, sp.frame.n.y, sp.frame.n.z, __uint_as_float(sp.mat));
         const uint32_t fl = (sp.has_material ? 1u : 0u) | (sp.front ? 2u : 0u);
@@ -125,9 +131,10 @@ __global__ void __launch_bounds__(128) k_primary(TickArgs t) {
         if (r.flags & kReqDemodulate) {
             float3 a = sp.emission;
             if (!sp.env) {
-                const SPd ex = surface_sp(sc, o, d, h.geom, h.prim, h.u, h.v);
+                const SPd ex = surface_sp(sc, o, d, h.geom, h.prim, h.u, h.v, h.inst);
                 a = ex.env ? ex.emission
-                           : material_albedo(load_material(sc, ex.mat, ex.front, 1.0f),
+                           : material_albedo(load_material(sc, ex.mat, ex.front, 1.0f,
+                                                           ex.tex_color),
                                              ex.frame.to_local(-d));
             }
             demod = f3(fmaxf(a.x, 1e-2f), fmaxf(a.y, 1e-2f), fmaxf(a.z, 1e-2f));
@@ -135,6 +142,7 @@ __global__ void __launch_bounds__(128) k_primary(TickArgs t) {
         pc[3] = make_float4(sp.frame.b.x, sp.frame.b.y, sp.frame.b.z, demod.x);
         pc[4] = make_float4(sp.emission.x, sp.emission.y, sp.emission.z, demod.y);
         pc[5] = make_float4(d.x, d.y, d.z, demod.z);
+        pc[6] = make_float4(sp.tex_color.x, sp.tex_color.y, sp.tex_color.z, 0.f);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(t.w.stats + 0, (unsigned long long)n);
 }
@@ -156,7 +164,7 @@ GBPT_DI bool scatter(const DevScene& sc, const ReqGPU& r, int k, const SPd& sp, 
         if (rng.next_float() >= q) return false;
         thr = thr / q;
     }
-    const Material m = load_material(sc, sp.mat, sp.front, ior);
+    const Material m = load_material(sc, sp.mat, sp.front, ior, sp.tex_color);
     const float3 wi_local = sp.frame.to_local(-ray_d);
     const float3 ng = decode_normal(sp.enc_fn);
     const float wi_ng = dot(-ray_d, ng);
@@ -196,7 +204,7 @@ GBPT_DI bool scatter(const DevScene& sc, const ReqGPU& r, int k, const SPd& sp, 
 }
 
 // Path start at the primary shading point (render_pt.slang:113-117) and the first scatter.
-__global__ void __launch_bounds__(128) k_shade_primary(TickArgs t) {
+__global__ void __launch_bounds__(128, kShadeBlocksPerSM) k_shade_primary(TickArgs t) {
     const uint32_t n = t.hdr->n_paths, nc = t.hdr->n_chunks;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_round = (n + 31u) & ~31u;
@@ -215,8 +223,9 @@ __global__ void __launch_bounds__(128) k_shade_primary(TickArgs t) {
             const uint32_t pid = pixel_id(r, c.pix_first + local / c.spp);
             const uint32_t px = pid % r.width, py = pid / r.width;
             Pcg rng{pcg4d16(px, py, r.frame, s)};
-            const float4* pc = t.w.pix + 6ull * slot;
+            const float4* pc = t.w.pix + kPixFloat4 * slot;
             const float4 c0 = pc[0], c1 = pc[1], c2 = pc[2], c3 = pc[3], c4 = pc[4], c5 = pc[5];
+            const float4 c6 = pc[6];
             SPd sp;
             sp.pos = f3(c0.x, c0.y, c0.z);
             sp.enc_fn = __float_as_uint(c0.w);
@@ -228,6 +237,7 @@ __global__ void __launch_bounds__(128) k_shade_primary(TickArgs t) {
             sp.front = (fl & 2u) != 0u;
             sp.frame.b = f3(c3.x, c3.y, c3.z);
             sp.emission = f3(c4.x, c4.y, c4.z);
+            sp.tex_color = f3(c6.x, c6.y, c6.z);
             const float3 d = f3(c5.x, c5.y, c5.z);
             float3 thr = f3(1.f, 1.f, 1.f);
             float ior = 1.0f, last_pdf = 0.f;
@@ -259,7 +269,7 @@ __global__ void __launch_bounds__(128) k_shade_primary(TickArgs t) {
 }
 
 // Closest hit for every entry of ray queue `qi` (persistent warps, counter w.counters[4]).
-template <bool COUNT>
+template <bool COUNT, bool TWO_LEVEL>
 __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
     k_trace(TickArgs t, int qi, unsigned long long* work_ctr) {
     const uint32_t n = t.w.counters[qi];
@@ -272,14 +282,17 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
         const float4 b = q[2 * i + 1];
         s.nodes = c.nodes;
         s.tris = c.tris;
+        s.insts = c.insts;
         s.mask = c.mask;
         trace_init(s, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w, b.w);
     };
     auto store = [&](uint32_t i, const Hit& h) {
         t.w.hit_tuv[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
         t.w.hit_geom[i] = h.geom;
+        t.w.hit_inst[i] = h.inst;
     };
-    trace_persistent<false, COUNT>(n, t.w.counters + 4, load, store, &ctr, t.w.counters + 3);
+    trace_persistent<false, COUNT, TWO_LEVEL>(n, t.w.counters + 4, load, store, &ctr,
+                                              t.w.counters + 3);
     if (COUNT) {
         atomicAdd(work_ctr + 0, (unsigned long long)ctr.nodes);
         atomicAdd(work_ctr + 1, (unsigned long long)ctr.tris);
@@ -291,16 +304,18 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
 }
 
 // Emission at the k-th path vertex, then scatter (k < L) into ray queue `qo`.
-__global__ void __launch_bounds__(128) k_shade(TickArgs t, int k, int qi, int qo) {
+__global__ void __launch_bounds__(128, kShadeBlocksPerSM)
+    k_shade(TickArgs t, int k, int qi, int qo, const uint32_t* __restrict__ perm) {
     const uint32_t n = t.w.counters[qi];
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_round = (n + 31u) & ~31u;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_round; j += stride) {
         bool want = false, want_shadow = false;
         float3 no, nd;
         float4 s_o, s_d, s_c;
         uint32_t tag = 0;
-        if (i < n) {
+        if (j < n) {
+            const uint32_t i = perm ? __ldg(&perm[j]) : j;
             tag = t.w.q_path[qi][i];
             const uint32_t p = tag & kPathMask;
             const ChunkGPU& c = t.chunks[tag >> kPathBits];
@@ -319,7 +334,8 @@ __global__ void __launch_bounds__(128) k_shade(TickArgs t, int k, int qi, int qo
             if (geom == 0xFFFFFFFFu || geom >= sc.geom_count) {
                 sp = env_sp(sc, o, d);
             } else {
-                sp = surface_sp(sc, o, d, geom, __float_as_uint(h.w), h.y, h.z);
+                sp = surface_sp(sc, o, d, geom, __float_as_uint(h.w), h.y, h.z,
+                                t.w.hit_inst[i]);
             }
             const bool scatters = k < (int)r.max_len;
             sp.has_material = sp.has_material && scatters;
@@ -356,8 +372,69 @@ __global__ void __launch_bounds__(128) k_shade(TickArgs t, int k, int qi, int qo
     }
 }
 
+// "shader execution reordering" (render_pt.cpp:160-161): the closest-hit queue is ordered by
+// material model before shading, so the warps of k_shade run one BSDF model at a time. Keys:
+// 0 environment (miss or UseEnvMap geometry), 1 diffuse, 2 OpenPBR, 3 OpenPBR with transmission.
+// Shading results do not depend on the order (each entry updates only its own path).
+constexpr int kSortKeys = 4;
+
+__global__ void __launch_bounds__(256) k_sort_keys(TickArgs t, int qi) {
+    const uint32_t n = t.w.counters[qi];
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t n_round = (n + 31u) & ~31u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
+        uint32_t key = 0xFFu;
+        if (i < n) {
+            key = 0u;
+            const uint32_t geom = t.w.hit_geom[i];
+            const ChunkGPU& c = t.chunks[__ldg(&t.w.q_path[qi][i]) >> kPathBits];
+            const DevScene& sc = t.scenes[c.scene];
+            if (geom < sc.geom_count) {
+                const GeomGPU g = sc.geoms[geom];
+                if (!(g.flags & GBPT_MESH_USE_ENV_MAP))
+                    key = 1u + min(__float_as_uint(__ldg(&sc.mats[5 * g.material]).x), 2u);
+            }
+            t.w.keys[i] = (uint8_t)key;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kSortKeys; ++k) {
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, key == k);
+            if (lane == 0 && m) atomicAdd(t.w.counters + 8 + k, (uint32_t)__popc(m));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sort_scatter(TickArgs t, int qi, uint32_t* perm) {
+    const uint32_t n = t.w.counters[qi];
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t base[kSortKeys];
+    uint32_t acc = 0;
+#pragma unroll
+    for (int k = 0; k < kSortKeys; ++k) {
+        base[k] = acc;
+        acc += t.w.counters[8 + k];
+    }
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t n_round = (n + 31u) & ~31u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
+        const uint32_t key = i < n ? t.w.keys[i] : 0xFFu;
+#pragma unroll
+        for (uint32_t k = 0; k < kSortKeys; ++k) {
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, key == k);
+            if (!m) continue;
+            const uint32_t leader = __ffs(m) - 1u;
+            uint32_t b = 0;
+            if (lane == leader) b = atomicAdd(t.w.counters + 12 + k, (uint32_t)__popc(m));
+            b = __shfl_sync(0xFFFFFFFFu, b, leader);
+            if (key == k) perm[base[k] + b + __popc(m & ((1u << lane) - 1u))] = i;
+        }
+    }
+}
+
 // Occlusion of the NEE queue; unoccluded contributions are added to their path (one shadow ray
 // per path per bounce, so no two lanes write the same path).
+template <bool TWO_LEVEL>
 __global__ void __launch_bounds__(128, kTraceBlocksPerSM) k_shadow(TickArgs t) {
     const uint32_t n = t.w.counters[2];
     auto load = [&](uint32_t i, TraceState& s) {
@@ -366,6 +443,7 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM) k_shadow(TickArgs t) {
         const float4 b = t.w.s_od[2 * i + 1];
         s.nodes = c.nodes;
         s.tris = c.tris;
+        s.insts = c.insts;
         s.mask = c.mask;
         trace_init(s, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), 0.0f, a.w);
     };
@@ -380,7 +458,8 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM) k_shadow(TickArgs t) {
             t.w.rad[p] = r;
         }
     };
-    trace_persistent<true, false>(n, t.w.counters + 5, load, store, nullptr, t.w.counters + 3);
+    trace_persistent<true, false, TWO_LEVEL>(n, t.w.counters + 5, load, store, nullptr,
+                                             t.w.counters + 3);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         atomicAdd(t.w.stats + 0, (unsigned long long)n);
         atomicAdd(t.w.stats + 1, (unsigned long long)n);
@@ -400,7 +479,7 @@ __global__ void __launch_bounds__(128) k_finalize(TickArgs t) {
         const uint64_t base = (uint64_t)c.path_base + (uint64_t)(q - c.slot_base) * S;
         float cr = 0.f, cg = 0.f, cb = 0.f, m = 0.f;
         // per-sample demodulation (render_pt.slang:105-116): 1 unless "demodulate albedo"
-        const float4* pc = t.w.pix + 6ull * q;
+        const float4* pc = t.w.pix + kPixFloat4 * q;
         const float ax = pc[3].w, ay = pc[4].w, az = pc[5].w;
         const bool demod = (r.flags & kReqDemodulate) != 0u;
         for (uint32_t s = lane; s < S; s += 32u) {
@@ -486,7 +565,8 @@ void work_free(Work& w) {
     }
     void* ptrs[] = {w.thr,     w.rad,       w.rng,    w.q_od[0], w.q_od[1],  w.q_path[0],
                     w.q_path[1], w.hit_tuv, w.hit_geom, w.s_od,  w.s_contrib, w.s_path,
-                    w.pix,     w.pix_id,    w.out,    w.counters, w.stats,    w.tables};
+                    w.pix,     w.pix_id,    w.out,    w.counters, w.stats,    w.tables,
+                    w.keys,    w.perm,      w.hit_inst};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     w = Work{};
@@ -504,7 +584,8 @@ int work_reserve(Work& w, uint64_t paths, uint64_t pixels) {
     }
     if (paths > w.path_cap) {
         void* old[] = {w.thr, w.rad, w.rng, w.q_od[0], w.q_od[1], w.q_path[0], w.q_path[1],
-                       w.hit_tuv, w.hit_geom, w.s_od, w.s_contrib, w.s_path};
+                       w.hit_tuv, w.hit_geom, w.hit_inst, w.s_od, w.s_contrib, w.s_path,
+                       w.keys, w.perm};
         for (void* p : old)
             if (p) cudaFree(p);
         uint64_t b = 0;
@@ -516,9 +597,11 @@ int work_reserve(Work& w, uint64_t paths, uint64_t pixels) {
                   alloc(w.q_path[1], paths, b) == cudaSuccess &&
                   alloc(w.hit_tuv, paths, b) == cudaSuccess &&
                   alloc(w.hit_geom, paths, b) == cudaSuccess &&
+                  alloc(w.hit_inst, paths, b) == cudaSuccess &&
                   alloc(w.s_od, 2 * paths, b) == cudaSuccess &&
                   alloc(w.s_contrib, paths, b) == cudaSuccess &&
-                  alloc(w.s_path, paths, b) == cudaSuccess;
+                  alloc(w.s_path, paths, b) == cudaSuccess &&
+                  alloc(w.keys, paths, b) == cudaSuccess && alloc(w.perm, paths, b) == cudaSuccess;
         if (!ok) {
             w.path_cap = 0;
             return GBPT_ERR_NO_MEMORY;
@@ -529,7 +612,7 @@ int work_reserve(Work& w, uint64_t paths, uint64_t pixels) {
     if (pixels > w.pixel_cap) {
         if (w.pix) cudaFree(w.pix);
         uint64_t b = 0;
-        if (alloc(w.pix, 6 * pixels, b) != cudaSuccess) return GBPT_ERR_NO_MEMORY;
+        if (alloc(w.pix, kPixFloat4 * pixels, b) != cudaSuccess) return GBPT_ERR_NO_MEMORY;
         w.pixel_cap = pixels;
         w.bytes += b;
     }
@@ -578,6 +661,8 @@ int tables_reserve(Work& w, uint64_t need) {
 struct TickPlan {
     uint32_t chunk_first, n_chunks, n_pix, n_paths, max_len;
     bool nee;
+    bool sort; // material-sorted shading (some request asked for it and the Work has the buffers)
+    bool two_level; // some chunk's scene is instanced: the two-level traversal variants
 };
 
 struct Grids {
@@ -589,9 +674,10 @@ struct Grids {
 Grids launch_grids() {
     Grids g;
     g.grid = num_sms() * 8;
-    g.trace = persistent_grid(k_trace<false>);
-    g.trace_c = persistent_grid(k_trace<true>);
-    g.shadow = persistent_grid(k_shadow);
+    // the two-level variants have the same launch bounds, hence the same residency
+    g.trace = persistent_grid(k_trace<false, false>);
+    g.trace_c = persistent_grid(k_trace<true, false>);
+    g.shadow = persistent_grid(k_shadow<false>);
     return g;
 }
 
@@ -621,7 +707,8 @@ uint64_t enqueue_tick(const TickArgs& ta, const TickPlan& tp, const Grids& g, cu
     if (nee) {
         cudaMemsetAsync(ctr + 5, 0, sizeof(uint32_t), st);
         ev = prof->begin(st, 2);
-        k_shadow<<<g.shadow, 128, 0, st>>>(ta);
+        if (tp.two_level) k_shadow<true><<<g.shadow, 128, 0, st>>>(ta);
+        else k_shadow<false><<<g.shadow, 128, 0, st>>>(ta);
         prof->end(st, ev);
         cudaMemsetAsync(ctr + 2, 0, sizeof(uint32_t), st);
         nl += 1;
@@ -631,18 +718,31 @@ uint64_t enqueue_tick(const TickArgs& ta, const TickPlan& tp, const Grids& g, cu
         const int qo = qi ^ 1;
         cudaMemsetAsync(ctr + 4, 0, sizeof(uint32_t), st);
         ev = prof->begin(st, 0);
-        if (work_ctr) k_trace<true><<<g.trace_c, 128, 0, st>>>(ta, qi, work_ctr);
-        else k_trace<false><<<g.trace, 128, 0, st>>>(ta, qi, nullptr);
+        if (work_ctr && tp.two_level) k_trace<true, true><<<g.trace_c, 128, 0, st>>>(ta, qi, work_ctr);
+        else if (work_ctr) k_trace<true, false><<<g.trace_c, 128, 0, st>>>(ta, qi, work_ctr);
+        else if (tp.two_level) k_trace<false, true><<<g.trace, 128, 0, st>>>(ta, qi, nullptr);
+        else k_trace<false, false><<<g.trace, 128, 0, st>>>(ta, qi, nullptr);
         prof->end(st, ev);
+        const uint32_t* perm = nullptr;
+        if (tp.sort) {
+            cudaMemsetAsync(ctr + 8, 0, 8 * sizeof(uint32_t), st);
+            ev = prof->begin(st, 1);
+            k_sort_keys<<<g.grid / 2, 256, 0, st>>>(ta, qi);
+            k_sort_scatter<<<g.grid / 2, 256, 0, st>>>(ta, qi, ta.w.perm);
+            prof->end(st, ev);
+            perm = ta.w.perm;
+            nl += 2;
+        }
         cudaMemsetAsync(ctr + qo, 0, sizeof(uint32_t), st);
         ev = prof->begin(st, 1);
-        k_shade<<<g.grid, 128, 0, st>>>(ta, (int)k, qi, qo);
+        k_shade<<<g.grid, 128, 0, st>>>(ta, (int)k, qi, qo, perm);
         prof->end(st, ev);
         nl += 2;
         if (nee && k < L) {
             cudaMemsetAsync(ctr + 5, 0, sizeof(uint32_t), st);
             ev = prof->begin(st, 2);
-            k_shadow<<<g.shadow, 128, 0, st>>>(ta);
+            if (tp.two_level) k_shadow<true><<<g.shadow, 128, 0, st>>>(ta);
+        else k_shadow<false><<<g.shadow, 128, 0, st>>>(ta);
             prof->end(st, ev);
             cudaMemsetAsync(ctr + 2, 0, sizeof(uint32_t), st);
             nl += 1;
@@ -716,7 +816,7 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
     DevScene* scenes = (DevScene*)(sb + lay.scenes);
     ChunkGPU* chunks = (ChunkGPU*)(sb + lay.chunks);
     e.scene_ptrs.clear();
-    TickPlan tp{0, 0, 0, 0, 1, false};
+    TickPlan tp{0, 0, 0, 0, 1, false, false, false};
     uint64_t paths = 0, pix = 0;
     for (uint32_t i = 0; i < n_items && tp.n_chunks < cap; ++i) {
         TickItem& it = *items[i];
@@ -744,11 +844,14 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
         c.mask = reqs[ri].mask;
         c.nodes = scenes[si].nodes;
         c.tris = scenes[si].tris;
+        c.insts = scenes[si].n_inst ? scenes[si].inst : nullptr;
+        tp.two_level |= scenes[si].n_inst != 0u;
         ++tp.n_chunks;
         paths += fit * S;
         pix += fit;
         tp.max_len = std::max(tp.max_len, reqs[ri].max_len);
         tp.nee |= (reqs[ri].flags & kReqNee) != 0u;
+        tp.sort |= it.params.sort_materials != 0;
         it.cursor += (uint32_t)fit;
         if (done && it.cursor == it.pixel_count) done->push_back(i);
     }
@@ -760,6 +863,7 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
     // work buffers: a whole wave when graphs replay the tick (their pointers must not move)
     bool graph = e.use_graphs && prof->level == 0;
     if ((rc = work_reserve(w, graph ? wave : paths, graph ? wave : pix)) != GBPT_OK) return rc;
+    tp.sort = tp.sort && w.perm != nullptr;
     unsigned char* tb = (unsigned char*)w.tables;
     if (cudaMemcpyAsync(tb, sb, lay.chunks + tp.n_chunks * sizeof(ChunkGPU), cudaMemcpyHostToDevice,
                         st) != cudaSuccess)
@@ -785,7 +889,8 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
             e.graph_work = w.thr;
             e.graph_tables = w.tables;
         }
-        const uint32_t shape = tp.max_len * 2u + (tp.nee ? 1u : 0u);
+        const uint32_t shape =
+            tp.max_len * 8u + (tp.nee ? 1u : 0u) + (tp.sort ? 2u : 0u) + (tp.two_level ? 4u : 0u);
         const TickEngine::Graph* found = nullptr;
         for (const auto& g : e.graphs)
             if (g.shape == shape) found = &g;
@@ -834,7 +939,7 @@ int render_batch(TickEngine& e, const BatchItem* items, uint32_t n_items, uint64
 }
 
 int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStream_t st,
-                 uint64_t* launches, Profile* prof, unsigned long long* work_ctr) {
+                 uint64_t* launches, Profile* prof, unsigned long long* work_ctr, uint64_t wave) {
     BatchItem it;
     it.scene = &scene;
     it.camera = args.camera;
@@ -845,6 +950,7 @@ int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStr
     TickEngine e;
     e.work = &w;
     e.stream = st;
+    if (wave) e.wave = wave;
     const int rc = render_batch(e, &it, 1, launches, prof, work_ctr);
     e.release();
     return rc;
@@ -892,8 +998,9 @@ int primary_points(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaS
     ta.hdr = d_hdr;
     ta.w = w;
     k_primary<<<(P + 127) / 128, 128, 0, st>>>(ta);
-    if (cudaMemcpyAsync(out_device, w.pix, (size_t)P * 6 * sizeof(float4), cudaMemcpyDeviceToDevice,
-                        st) != cudaSuccess)
+    // the first 6 float4 of every cached point: the gbpt_debug_primary_points layout
+    if (cudaMemcpy2DAsync(out_device, 6 * sizeof(float4), w.pix, kPixFloat4 * sizeof(float4),
+                          6 * sizeof(float4), P, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
         return GBPT_ERR_CUDA;
     return cudaGetLastError() == cudaSuccess ? GBPT_OK : GBPT_ERR_CUDA;
 }

@@ -74,9 +74,6 @@ class RenderPT:
         if spp < 0 or not 1 <= L <= 64:
             raise ValueError(f"{self.TYPE}: samples per pixel must be >= 0 and max path length "
                              f"in [1, 64]")
-        if self.props["demodulate albedo"]:
-            raise ValueError(f"{self.TYPE}: 'demodulate albedo' needs the GBuffer albedo, which "
-                             f"this build does not produce yet")
         return flags
 
     def instance_mask(self) -> int:
@@ -96,6 +93,7 @@ class RenderPT:
                                nee=bool(self.props["next event estimation"]),
                                rr_depth=int(self.props["russian roulette depth"]),
                                sort_materials=bool(self.props["shader execution reordering"]),
+                               demodulate_albedo=bool(self.props["demodulate albedo"]),
                                pixels=pixels)
 
     def process(self, scene_id: int, camera: N.Camera, iteration: int, out=None):

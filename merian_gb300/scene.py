@@ -26,6 +26,11 @@ class SceneData:
     env: np.ndarray | None = None          # (h, w, 4) float32
     env_to_local: np.ndarray = field(default_factory=lambda: np.eye(3, dtype=np.float32))
     env_intensity: float = 1.0
+    # two-level scenes: BLAS geometry ranges (BLAS_DTYPE) and instances (INSTANCE_DTYPE)
+    blas_ranges: np.ndarray | None = None
+    instances: np.ndarray | None = None
+    # RGBA8 textures: (height, width, 4) uint8 arrays and whether each is sRGB-encoded
+    textures: list = field(default_factory=list)
 
     @property
     def triangle_count(self) -> int:
@@ -55,6 +60,25 @@ class SceneData:
         d.materials = N.ptr(self.materials)
         d.material_count = len(self.materials)
         d.env = env_p
+        if self.textures:
+            arr = (N.Texture * len(self.textures))()
+            for i, (tex, srgb) in enumerate(self.textures):
+                t = np.ascontiguousarray(tex, dtype=np.uint8)
+                keep.append(t)
+                arr[i].texels = t.ctypes.data_as(C.POINTER(C.c_uint8))
+                arr[i].height, arr[i].width = int(t.shape[0]), int(t.shape[1])
+                arr[i].srgb = int(bool(srgb))
+            keep.append(arr)
+            d.textures = C.cast(arr, C.POINTER(N.Texture))
+            d.texture_count = len(self.textures)
+        if self.instances is not None and len(self.instances):
+            b = np.ascontiguousarray(self.blas_ranges, dtype=N.BLAS_DTYPE)
+            ins = np.ascontiguousarray(self.instances, dtype=N.INSTANCE_DTYPE)
+            keep += [b, ins]
+            d.blas_ranges = N.ptr(b)
+            d.blas_count = len(b)
+            d.instances = N.ptr(ins)
+            d.instance_count = len(ins)
         return d, keep
 
 
@@ -72,6 +96,22 @@ def cornell(seed: int = BASE_SEED, tess: int = 1) -> SceneData:
     else:
         N.check(lib.gbpt_gen_cornell_tess(seed, tess, N.ptr(v), N.ptr(i), N.ptr(g), N.ptr(m)))
     return SceneData(v, i, g, m)
+
+
+def blob(seed: int, n_u: int = 250, n_v: int = 101):
+    """(vertices, indices) of a bumpy closed sphere (gbpt_gen_blob), 2 n_u (n_v - 1) triangles."""
+    lib = N.load()
+    v = np.zeros((n_u + 1) * n_v, N.VERTEX_DTYPE)
+    i = np.zeros((2 * n_u * (n_v - 1), 3), np.uint32)
+    N.check(lib.gbpt_gen_blob(seed, n_u, n_v, N.ptr(v), N.ptr(i)))
+    return v, i
+
+
+def noise_texture(seed: int, width: int = 512, height: int = 512) -> np.ndarray:
+    lib = N.load()
+    t = np.zeros((height, width, 4), np.uint8)
+    N.check(lib.gbpt_gen_noise_texture(seed, width, height, N.ptr(t)))
+    return t
 
 
 def env_lobes(seed: int, width: int = 2048, height: int = 1024) -> np.ndarray:
@@ -110,7 +150,8 @@ def look_at(position, target, up=(0.0, 1.0, 0.0), vfov_deg: float = 40.0, aspect
 def render_params(width: int, height: int, spp: int, max_path_length: int, *,
                   emission_on_primary: bool = True, instance_mask: int = 0xFF,
                   frame: int = 0, nee: bool = False, rr_depth: int = 0,
-                  sort_materials: bool = False, pixels: np.ndarray | None = None):
+                  sort_materials: bool = False, demodulate_albedo: bool = False,
+                  pixels: np.ndarray | None = None):
     p = N.RenderParams()
     p.width, p.height, p.spp, p.max_path_length = width, height, spp, max_path_length
     p.emission_on_primary = int(emission_on_primary)
@@ -119,6 +160,7 @@ def render_params(width: int, height: int, spp: int, max_path_length: int, *,
     p.nee = int(nee)
     p.rr_depth = rr_depth
     p.sort_materials = int(sort_materials)
+    p.demodulate_albedo = int(demodulate_albedo)
     keep = None
     if pixels is not None and len(pixels):
         keep = np.ascontiguousarray(pixels, dtype=np.uint32)
@@ -271,6 +313,25 @@ class Context:
 
     def set_graphs(self, enable: bool) -> None:
         N.check(self.lib.gbpt_set_graphs(self.handle, int(enable)))
+
+    def set_tuning(self, wave_paths: int = 0, sort_materials: int = -1,
+                   use_graphs: bool = False) -> None:
+        t = N.Tuning(wave_paths, sort_materials, int(use_graphs))
+        N.check(self.lib.gbpt_set_tuning(self.handle, C.byref(t)))
+
+    def get_tuning(self) -> N.Tuning:
+        t = N.Tuning()
+        N.check(self.lib.gbpt_get_tuning(self.handle, C.byref(t)))
+        return t
+
+    def autotune(self, sid: int, camera: N.Camera, params: N.RenderParams):
+        """Times the candidate schedules on one frame and keeps the fastest; returns the chosen
+        tuning and the candidates' times (ms, tick size major, sorting minor)."""
+        t = N.Tuning()
+        ms = (C.c_double * 8)(*([float("nan")] * 8))
+        N.check(self.lib.gbpt_autotune(self.handle, sid, C.byref(camera), C.byref(params),
+                                       C.byref(t), ms))
+        return t, [v for v in ms if v == v]
 
     def clock(self) -> float:
         return self.lib.gbpt_clock()

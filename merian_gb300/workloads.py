@@ -15,6 +15,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
+from . import _native as N
 from . import scene as S
 
 BATCH_RESOLUTIONS = ((256, 256), (512, 512), (1024, 1024))
@@ -109,3 +110,77 @@ def upload_all(ctx: S.Context, specs, threads: int = 16):
         return ctx.upload(spec.build())
     with ThreadPoolExecutor(max_workers=threads) as ex:
         return list(ex.map(one, specs))
+
+
+def _rotation(rng: np.random.Generator) -> np.ndarray:
+    """A uniformly distributed rotation (unit quaternion from a normal 4-vector)."""
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def instanced_scene(seed: int = S.BASE_SEED, n_meshes: int = 50, n_u: int = 250, n_v: int = 101,
+                    n_instances: int = 1000, n_textures: int = 256, tex_size: int = 512,
+                    bands: int = 6, box: float = 100.0, env_size=(1024, 512)) -> S.SceneData:
+    """The instanced configuration: n_meshes bumpy closed meshes of 2 n_u (n_v - 1) triangles
+    (50 x 50,000 by default), each split into `bands` latitude bands with their own material and
+    albedo texture (n_textures sRGB value-noise RGBA8 textures, tex_size^2), placed by n_instances
+    instances under random affine transforms (uniform rotation, scale in [0.5, 2], translation in
+    a box^3 cube), lit by a Gaussian-lobe environment. Materials: 60 % Lambert, 40 % the OpenPBR
+    GGX/Lambert Fresnel mix with roughness in [0.1, 0.6]."""
+    rng = np.random.default_rng(seed)
+    textures = [(S.noise_texture(seed * 7919 + 17 + t, tex_size, tex_size), True)
+                for t in range(n_textures)]
+    verts, idx, geoms, mats, blas = [], [], [], [], []
+    v_off = t_off = 0
+    for m in range(n_meshes):
+        v, i = S.blob(seed * 104729 + 1000 + m, n_u, n_v)
+        rows = n_v - 1
+        first_geom = len(geoms)
+        for b in range(bands):
+            r0, r1 = b * rows // bands, (b + 1) * rows // bands
+            g = np.zeros(1, N.GEOMETRY_DTYPE)
+            g["first_vertex"] = v_off
+            g["first_triangle"] = t_off + 2 * n_u * r0
+            g["triangle_count"] = 2 * n_u * (r1 - r0)
+            g["material_id"] = len(mats)
+            g["flags"] = 0
+            g["instance_mask"] = 0xFF
+            geoms.append(g)
+            mat = np.zeros(1, N.MATERIAL_DTYPE)
+            lambert = rng.uniform() < 0.6
+            tint = rng.uniform(0.7, 1.0, size=3)
+            roughness = rng.uniform(0.1, 0.6)
+            mat["model"] = N.MATERIAL_DIFFUSE if lambert else N.MATERIAL_OPENPBR
+            mat["base_color"] = tint
+            mat["specular_alpha"] = roughness * roughness
+            mat["specular_weight"] = 0.0 if lambert else 1.0
+            mat["specular_ior"] = 1.5
+            mat["transmission_color"] = 1.0
+            mat["base_color_texture"] = (m * bands + b) % n_textures
+            mats.append(mat)
+        blas.append((first_geom, bands))
+        verts.append(v)
+        idx.append(i)
+        v_off += len(v)
+        t_off += len(i)
+    inst = np.zeros(n_instances, N.INSTANCE_DTYPE)
+    for k in range(n_instances):
+        M = _rotation(rng) * rng.uniform(0.5, 2.0)
+        t = rng.uniform(0.0, box, size=3)
+        inst[k]["blas"] = rng.integers(n_meshes)
+        inst[k]["mask"] = 0xFF
+        inst[k]["object_to_world"] = np.concatenate([M, t[:, None]], axis=1).reshape(12)
+    b = np.array(blas, dtype=np.uint32).view(N.BLAS_DTYPE).reshape(-1)
+    env = S.env_lobes(seed ^ 0x5E, *env_size) if env_size else None
+    return S.SceneData(np.concatenate(verts), np.concatenate(idx), np.concatenate(geoms),
+                       np.concatenate(mats), env, blas_ranges=b, instances=inst,
+                       textures=textures)
+
+
+def instanced_camera(width: int, height: int, box: float = 100.0):
+    c = 0.5 * box
+    return S.look_at((c, c, -0.45 * box), (c, c, c), (0.0, 1.0, 0.0), 60.0, width / height)

@@ -41,6 +41,8 @@ def load() -> C.CDLL:
         lib.oracle_render.argtypes = [vp, vp, vp, i32, i32, vp, vp, vp]
         lib.oracle_num_threads.restype = i32
         lib.oracle_gbuffer.argtypes = [vp, vp, u32, u32, u32, vp]
+        lib.oracle_scene_set_instances.argtypes = [vp, vp, u32, vp, u32]
+        lib.oracle_scene_set_textures.argtypes = [vp, vp, u32]
         lib.oracle_bsdf_check.argtypes = [i32, vp, vp, f32, f32, vp, f32, f32, u32, u32, vp]
         lib.oracle_material_samples.argtypes = [vp, i32, f32, vp, u32, u32, vp]
         _lib = lib
@@ -66,6 +68,14 @@ class OracleScene:
             _p(scene.geometries), len(scene.geometries), _p(scene.materials),
             len(scene.materials), _p(env), 0 if env is None else env.shape[1],
             0 if env is None else env.shape[0], _p(m), float(scene.env_intensity))
+        d, self._desc_keep = scene.desc()
+        if getattr(scene, "textures", None):
+            lib.oracle_scene_set_textures(self.h, C.cast(d.textures, C.c_void_p).value,
+                                          d.texture_count)
+        if getattr(scene, "instances", None) is not None and len(scene.instances):
+            if lib.oracle_scene_set_instances(self.h, d.blas_ranges, d.blas_count, d.instances,
+                                              d.instance_count) != 0:
+                raise ValueError("oracle: bad instances")
 
     def close(self):
         if self.h:

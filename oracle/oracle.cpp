@@ -25,7 +25,30 @@
 
 namespace oracle {
 
-struct Scene {
+constexpr uint32_t kNoInst = 0xFFFFFFFFu;
+
+// Triangles and their binary BVH: a whole single-level scene, or one BLAS in object space.
+struct TriSet {
+    std::vector<float> tv;        // 9 per triangle
+    std::vector<uint32_t> tgeom;  // geometry of each triangle
+    std::vector<uint32_t> tprim;  // primitive id within the geometry
+    struct Node {
+        float lo[3], hi[3];
+        uint32_t left_or_first, count; // count > 0: leaf over perm[first, first+count)
+    };
+    std::vector<Node> nodes;
+    std::vector<uint32_t> perm;
+};
+
+// A TLAS instance: row-major 3x4 transforms (world-to-object computed in double, rounded once,
+// exactly as the library computes it), BLAS, mask, first geometry and world bounds.
+struct Instance {
+    float o2w[12], w2o[12];
+    uint32_t blas, mask, first_geom;
+    double lo[3], hi[3];
+};
+
+struct Scene : TriSet {
     std::vector<gbpt_packed_vertex> verts;
     std::vector<uint32_t> idx;
     std::vector<gbpt_geometry> geoms;
@@ -34,20 +57,19 @@ struct Scene {
     uint32_t ew = 0, eh = 0;
     float env_to_local[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     float env_intensity = 1.0f;
-    // flattened triangles (in the order of `idx`)
-    std::vector<float> tv;        // 9 per triangle
-    std::vector<uint32_t> tgeom;  // geometry of each triangle
-    std::vector<uint32_t> tprim;  // primitive id within the geometry
+    // the flattened triangles (TriSet, in the order of `idx`) of a single-level scene
     std::vector<uint32_t> geom_tri_base; // first flattened triangle of each geometry
-    // BVH2
-    struct Node {
-        float lo[3], hi[3];
-        uint32_t left_or_first, count; // count > 0: leaf over perm[first, first+count)
-    };
-    std::vector<Node> nodes;
-    std::vector<uint32_t> perm;
-    // emissive triangles for next-event estimation
-    std::vector<uint32_t> light_tri;
+    // two-level scenes
+    std::vector<TriSet> blas;
+    std::vector<Instance> insts;
+    // RGBA8 textures: texels, (first texel, width, height, sRGB) per texture, sRGB decode table
+    std::vector<uint8_t> tex;
+    std::vector<uint32_t> tex_info;
+    float srgb_lut[256] = {};
+    // emissive triangles for next-event estimation, in world space (one copy per instance)
+    std::vector<float> light_tv;       // 9 per light
+    std::vector<uint32_t> light_geom;
+    std::vector<uint32_t> light_tri;   // light index (kept for the selection count)
     std::vector<double> light_cdf; // inclusive prefix of power, normalised to 1
     double light_total = 0.0;
     // environment importance sampling
@@ -58,7 +80,7 @@ struct Scene {
 };
 
 // ---- BVH2 build (binned SAH, 16 bins) ---------------------------------------------------------
-static void build_bvh(Scene& s) {
+static void build_bvh(TriSet& s) {
     const size_t n = s.tgeom.size();
     s.perm.resize(n);
     for (size_t i = 0; i < n; ++i) s.perm[i] = (uint32_t)i;
@@ -193,6 +215,7 @@ struct HitRec {
     double t;
     float u, v;
     uint32_t geom, prim;
+    uint32_t inst; // instance of a two-level hit, kNoInst otherwise
     bool valid;
 };
 // Returns true and the distance / barycentrics when the triangle is hit within [tmin, tmax].
@@ -237,12 +260,13 @@ inline bool intersect(const RayPre<R>& p, const float* tv, uint32_t flags, R tmi
     return true;
 }
 
+// Closest (or any) hit of r against one triangle set, updating best / tbest; returns true when an
+// any-hit query found its hit. Ties at equal t go to the smallest (geometry, primitive, instance).
 template <class R>
-static HitRec trace(const Scene& s, const Ray<R>& r, uint32_t mask, bool any_hit,
-                    uint64_t* node_count = nullptr, uint64_t* tri_count = nullptr) {
-    HitRec best{};
-    best.valid = false;
-    if (s.nodes.empty() || s.tgeom.empty()) return best;
+static bool trace_set(const Scene& s, const TriSet& ts, const Ray<R>& r, uint32_t mask,
+                      bool any_hit, uint32_t inst, HitRec& best, R& tbest, uint64_t* node_count,
+                      uint64_t* tri_count) {
+    if (ts.nodes.empty() || ts.tgeom.empty()) return false;
     const RayPre<R> pre = ray_pre(r);
     V3<R> inv;
     auto safe_inv = [](R d) {
@@ -250,15 +274,13 @@ static HitRec trace(const Scene& s, const Ray<R>& r, uint32_t mask, bool any_hit
         return R(1) / (std::fabs(d) > m ? d : std::copysign(m, d));
     };
     inv = mk(safe_inv(r.d.x), safe_inv(r.d.y), safe_inv(r.d.z));
-    R tbest = r.tmax;
-    uint64_t key_best = ~0ull;
     uint32_t stack[128];
     int sp = 0;
     stack[sp++] = 0;
     const R eps = sizeof(R) == 4 ? R(1.0 / (1 << 20)) : R(0);
     while (sp > 0) {
         const uint32_t ni = stack[--sp];
-        const Scene::Node& nd = s.nodes[ni];
+        const TriSet::Node& nd = ts.nodes[ni];
         if (node_count) ++*node_count;
         // slab test, conservative by a relative epsilon in float mode
         R t0 = r.tmin, t1 = tbest;
@@ -276,37 +298,93 @@ static HitRec trace(const Scene& s, const Ray<R>& r, uint32_t mask, bool any_hit
         if (miss) continue;
         if (nd.count > 0) {
             for (uint32_t k = 0; k < nd.count; ++k) {
-                const uint32_t tri = s.perm[nd.left_or_first + k];
-                const uint32_t g = s.tgeom[tri];
+                const uint32_t tri = ts.perm[nd.left_or_first + k];
+                const uint32_t g = ts.tgeom[tri];
                 const gbpt_geometry& geo = s.geoms[g];
                 if (((geo.instance_mask & 0xFFu) & mask) == 0) continue;
                 if (tri_count) ++*tri_count;
                 R t, u, v;
-                if (!intersect(pre, &s.tv[9 * tri], geo.flags, r.tmin, tbest, t, u, v)) continue;
-                const uint64_t key = ((uint64_t)g << 32) | s.tprim[tri];
-                if (t < tbest || key < key_best) {
+                if (!intersect(pre, &ts.tv[9 * tri], geo.flags, r.tmin, tbest, t, u, v)) continue;
+                const uint32_t prim = ts.tprim[tri];
+                if (!best.valid || t < tbest || g < best.geom ||
+                    (g == best.geom && (prim < best.prim || (prim == best.prim && inst < best.inst)))) {
                     tbest = t;
-                    key_best = key;
                     best.t = (double)t;
                     best.u = (float)u;
                     best.v = (float)v;
                     best.geom = g;
-                    best.prim = s.tprim[tri];
+                    best.prim = prim;
+                    best.inst = inst;
                     best.valid = true;
-                    if (any_hit) return best;
+                    if (any_hit) return true;
                 }
             }
         } else {
             // visit the nearer child first
             const uint32_t l = nd.left_or_first, rr = l + 1;
-            const Scene::Node &a = s.nodes[l], &b = s.nodes[rr];
+            const TriSet::Node &a = ts.nodes[l], &b = ts.nodes[rr];
             const int ax = pre.kz;
             const R ca = (R)a.lo[ax] + (R)a.hi[ax], cb = (R)b.lo[ax] + (R)b.hi[ax];
             const bool a_first = (comp(r.d, ax) >= R(0)) ? (ca <= cb) : (ca > cb);
-            if (sp + 2 > 128) return best; // depth guard (never reached by the SAH build)
+            if (sp + 2 > 128) return false; // depth guard (never reached by the SAH build)
             stack[sp++] = a_first ? rr : l;
             stack[sp++] = a_first ? l : rr;
         }
+    }
+    return false;
+}
+
+// One row of an affine transform applied with one rounding per operation in the order the
+// library's kernels use: ((m0 x + m1 y) + m2 z) + m3 w.
+template <class R> inline R xform_row(const float* m, V3<R> p, R w) {
+    return (((R)m[0] * p.x + (R)m[1] * p.y) + (R)m[2] * p.z) + (R)m[3] * w;
+}
+template <class R> inline V3<R> xform_point(const float* m, V3<R> p) {
+    return mk(xform_row(m, p, R(1)), xform_row(m + 4, p, R(1)), xform_row(m + 8, p, R(1)));
+}
+template <class R> inline V3<R> xform_vector(const float* m, V3<R> v) {
+    return mk(xform_row(m, v, R(0)), xform_row(m + 4, v, R(0)), xform_row(m + 8, v, R(0)));
+}
+
+template <class R>
+static HitRec trace(const Scene& s, const Ray<R>& r, uint32_t mask, bool any_hit,
+                    uint64_t* node_count = nullptr, uint64_t* tri_count = nullptr) {
+    HitRec best{};
+    best.valid = false;
+    best.inst = kNoInst;
+    R tbest = r.tmax;
+    if (s.insts.empty()) {
+        trace_set(s, s, r, mask, any_hit, kNoInst, best, tbest, node_count, tri_count);
+        return best;
+    }
+    // two-level: every instance whose mask and world box the ray meets, in object space (the
+    // direction is not renormalised, so t is the world parameter)
+    for (uint32_t i = 0; i < (uint32_t)s.insts.size(); ++i) {
+        const Instance& in = s.insts[i];
+        if ((in.mask & mask) == 0u) continue;
+        double t0 = (double)r.tmin, t1 = (double)tbest;
+        bool miss = false;
+        for (int a = 0; a < 3 && !miss; ++a) {
+            const double o = (double)comp(r.o, a), d = (double)comp(r.d, a);
+            if (d == 0.0) {
+                if (o < in.lo[a] || o > in.hi[a]) miss = true;
+                continue;
+            }
+            double ta = (in.lo[a] - o) / d, tb = (in.hi[a] - o) / d;
+            if (ta > tb) std::swap(ta, tb);
+            t0 = std::max(t0, ta - 1e-9 * std::fabs(ta));
+            t1 = std::min(t1, tb + 1e-9 * std::fabs(tb));
+            if (t0 > t1) miss = true;
+        }
+        if (miss) continue;
+        Ray<R> ro;
+        ro.o = xform_point<R>(in.w2o, r.o);
+        ro.d = xform_vector<R>(in.w2o, r.d);
+        ro.tmin = r.tmin;
+        ro.tmax = r.tmax;
+        if (trace_set(s, s.blas[in.blas], ro, mask, any_hit, i, best, tbest, node_count,
+                      tri_count))
+            return best;
     }
     return best;
 }
@@ -314,6 +392,7 @@ static HitRec trace(const Scene& s, const Ray<R>& r, uint32_t mask, bool any_hit
 // ---- shading point (scene.slang:312-469, hit.slang) ---------------------------------------------
 template <class R> struct SP {
     V3<R> pos;
+    V3<R> tex_color; // base colour texture at the hit (1 without one)
     uint32_t enc_face_normal;
     V3<R> emission;
     Frame<R> frame;
@@ -371,9 +450,33 @@ template <class R> SP<R> env_sp(const Scene& s, const Ray<R>& ray) {
 }
 
 // get_shading_point(ray, hit) with a valid triangle hit; bary are the Hit barycentrics
+// Bilinear lookup with repeat addressing at level 0 (LOD0Sampler, textures.slang:338-423), sRGB
+// textures decoded per texel before filtering; returns rgb.
+template <class R> inline V3<R> texture_sample(const Scene& s, uint32_t t, R u, R v) {
+    const uint32_t* info = &s.tex_info[4 * t];
+    const int w = (int)info[1], h = (int)info[2];
+    const R x = u * (R)w - R(0.5), y = v * (R)h - R(0.5);
+    const R fx = std::floor(x), fy = std::floor(y);
+    const R a = x - fx, b = y - fy;
+    const int ix = (int)fx, iy = (int)fy;
+    auto wrap = [](int i, int n) { return ((i % n) + n) % n; };
+    const int x0 = wrap(ix, w), x1 = wrap(ix + 1, w), y0 = wrap(iy, h), y1 = wrap(iy + 1, h);
+    auto texel = [&](int xx, int yy) {
+        const uint8_t* c = &s.tex[4 * ((size_t)info[0] + (size_t)yy * w + xx)];
+        if (info[3]) return mk<R>(s.srgb_lut[c[0]], s.srgb_lut[c[1]], s.srgb_lut[c[2]]);
+        return mk<R>((R)c[0] * R(1.0f / 255.0f), (R)c[1] * R(1.0f / 255.0f),
+                     (R)c[2] * R(1.0f / 255.0f));
+    };
+    const V3<R> top = texel(x0, y0) * (R(1) - a) + texel(x1, y0) * a;
+    const V3<R> bot = texel(x0, y1) * (R(1) - a) + texel(x1, y1) * a;
+    return top * (R(1) - b) + bot * b;
+}
+
+// inst: the instance of a two-level hit (position by its object-to-world transform, edges and
+// tangents by the linear part, the normal by the inverse transpose; scene.slang:235-259)
 template <class R>
 SP<R> surface_sp(const Scene& s, const Ray<R>& ray, uint32_t g, uint32_t prim, R bu, R bv, R ior,
-                 bool with_material) {
+                 bool with_material, uint32_t inst = kNoInst) {
     const gbpt_geometry& geo = s.geoms[g];
     if (geo.flags & GBPT_MESH_USE_ENV_MAP) return env_sp(s, ray);
     const uint32_t tri = geo.first_triangle + prim;
@@ -383,8 +486,15 @@ SP<R> surface_sp(const Scene& s, const Ray<R>& ray, uint32_t g, uint32_t prim, R
     const gbpt_packed_vertex &v0 = s.verts[i0], &v1 = s.verts[i1], &v2 = s.verts[i2];
     const R b0 = R(1) - bu - bv, b1 = bu, b2 = bv;
     const V3<R> p0 = fetch_pos<R>(s, i0), p1 = fetch_pos<R>(s, i1), p2 = fetch_pos<R>(s, i2);
-    const V3<R> pos = (b0 * p0 + b1 * p1) + b2 * p2;
-    const V3<R> e01 = p1 - p0, e02 = p2 - p0;
+    V3<R> pos = (b0 * p0 + b1 * p1) + b2 * p2;
+    V3<R> e01 = p1 - p0, e02 = p2 - p0;
+    const float* o2w = inst == kNoInst ? nullptr : s.insts[inst].o2w;
+    const float* w2o = inst == kNoInst ? nullptr : s.insts[inst].w2o;
+    if (o2w) {
+        pos = xform_point<R>(o2w, pos);
+        e01 = xform_vector<R>(o2w, e01);
+        e02 = xform_vector<R>(o2w, e02);
+    }
     V3<R> fn = normalize(cross(e01, e02));
     if (geo.flags & GBPT_MESH_FLIP_FACING) fn = -fn;
     V3<R> vn;
@@ -394,6 +504,10 @@ SP<R> surface_sp(const Scene& s, const Ray<R>& ray, uint32_t g, uint32_t prim, R
         vn = normalize((b0 * decode_normal<R>(v0.encoded_normal) +
                         b1 * decode_normal<R>(v1.encoded_normal)) +
                        b2 * decode_normal<R>(v2.encoded_normal));
+        if (w2o) // inverse transpose: the columns of the world-to-object rows
+            vn = normalize(mk<R>((R)w2o[0] * vn.x + (R)w2o[4] * vn.y + (R)w2o[8] * vn.z,
+                                 (R)w2o[1] * vn.x + (R)w2o[5] * vn.y + (R)w2o[9] * vn.z,
+                                 (R)w2o[2] * vn.x + (R)w2o[6] * vn.y + (R)w2o[10] * vn.z));
     }
     // tangent: per-vertex, or the UV-derived (Lengyel) fallback
     Frame<R> frame;
@@ -410,7 +524,9 @@ SP<R> surface_sp(const Scene& s, const Ray<R>& ray, uint32_t g, uint32_t prim, R
                     t2 = dec_t(v2.encoded_tangent, w2);
         const V3<R> t = (b0 * t0 + b1 * t1) + b2 * t2;
         const R tw = (b0 * w0 + b1 * w1) + b2 * w2;
-        frame = frame_from_tangent(vn, normalize(t), signr(tw));
+        V3<R> tn = normalize(t);
+        if (o2w) tn = xform_vector<R>(o2w, tn);
+        frame = frame_from_tangent(vn, tn, signr(tw));
     } else {
         const R d1x = uv1x - uv0x, d1y = uv1y - uv0y, d2x = uv2x - uv0x, d2y = uv2y - uv0y;
         const R det = d1x * d2y - d2x * d1y;
@@ -452,7 +568,14 @@ SP<R> surface_sp(const Scene& s, const Ray<R>& ray, uint32_t g, uint32_t prim, R
     } else {
         sp.frame = frame;
     }
-    if (with_material) sp.bsdf = make_material<R>(m, mk(R(1), R(1), R(1)), ior, front);
+    sp.tex_color = mk(R(1), R(1), R(1));
+    if (!s.tex_info.empty() && m.base_color_texture >= 0 &&
+        (size_t)m.base_color_texture < s.tex_info.size() / 4) {
+        const R u = (b0 * uv0x + b1 * uv1x) + b2 * uv2x;
+        const R v = (b0 * uv0y + b1 * uv1y) + b2 * uv2y;
+        sp.tex_color = texture_sample<R>(s, (uint32_t)m.base_color_texture, u, v);
+    }
+    if (with_material) sp.bsdf = make_material<R>(m, sp.tex_color, ior, front);
     return sp;
 }
 
@@ -466,7 +589,7 @@ SP<R> shading_point(const Scene& s, const Ray<R>& ray, const HitRec& h, R ior, b
         bu = (R)half_to_float(float_to_half(h.u));
         bv = (R)half_to_float(float_to_half(h.v));
     }
-    return surface_sp(s, ray, h.geom, h.prim, bu, bv, ior, with_material);
+    return surface_sp(s, ray, h.geom, h.prim, bu, bv, ior, with_material, h.inst);
 }
 
 // ---- lights for next-event estimation (new in the GB300 build; the reference has none) -------
@@ -479,18 +602,46 @@ template <class R> inline R tri_area(const Scene& s, uint32_t tri) {
 static void build_lights(Scene& s) {
     s.light_tri.clear();
     s.light_cdf.clear();
+    s.light_tv.clear();
+    s.light_geom.clear();
     double acc = 0.0;
-    for (uint32_t t = 0; t < s.tgeom.size(); ++t) {
-        const gbpt_geometry& g = s.geoms[s.tgeom[t]];
-        const gbpt_material& m = s.mats[g.material_id];
-        if (m.model == GBPT_MATERIAL_DIFFUSE) continue;
+    // every placement of an emissive triangle in world space: the flattened triangles of a
+    // single-level scene, or each instance's copy of its BLAS triangles
+    auto add = [&](const float* tv, uint32_t g, const float* o2w) {
+        const gbpt_material& m = s.mats[s.geoms[g].material_id];
+        if (m.model == GBPT_MATERIAL_DIFFUSE) return;
         const double lum = 0.299 * m.emission[0] + 0.587 * m.emission[1] + 0.114 * m.emission[2];
-        if (!(lum > 0.0)) continue;
-        const double p = tri_area<double>(s, t) * lum;
-        if (!(p > 0.0)) continue;
+        if (!(lum > 0.0)) return;
+        float w[9];
+        for (int c = 0; c < 3; ++c)
+            for (int a = 0; a < 3; ++a) {
+                if (!o2w) {
+                    w[3 * c + a] = tv[3 * c + a];
+                } else {
+                    const float* r = o2w + 4 * a;
+                    w[3 * c + a] = (float)((double)r[0] * tv[3 * c] + (double)r[1] * tv[3 * c + 1] +
+                                           (double)r[2] * tv[3 * c + 2] + (double)r[3]);
+                }
+            }
+        const double e1[3] = {(double)w[3] - w[0], (double)w[4] - w[1], (double)w[5] - w[2]};
+        const double e2[3] = {(double)w[6] - w[0], (double)w[7] - w[1], (double)w[8] - w[2]};
+        const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                     cz = e1[0] * e2[1] - e1[1] * e2[0];
+        const double p = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz) * lum;
+        if (!(p > 0.0)) return;
         acc += p;
-        s.light_tri.push_back(t);
+        s.light_tri.push_back((uint32_t)s.light_geom.size());
+        s.light_geom.push_back(g);
+        s.light_tv.insert(s.light_tv.end(), w, w + 9);
         s.light_cdf.push_back(acc);
+    };
+    if (s.insts.empty()) {
+        for (uint32_t t = 0; t < s.tgeom.size(); ++t) add(&s.tv[9 * t], s.tgeom[t], nullptr);
+    } else {
+        for (const Instance& in : s.insts) {
+            const TriSet& b = s.blas[in.blas];
+            for (uint32_t t = 0; t < b.tgeom.size(); ++t) add(&b.tv[9 * t], b.tgeom[t], in.o2w);
+        }
     }
     s.light_total = acc;
     for (double& c : s.light_cdf) c /= acc;
@@ -568,13 +719,105 @@ ORACLE_API void* oracle_scene_create(const gbpt_packed_vertex* v, uint64_t nv, c
 
 ORACLE_API void oracle_scene_destroy(void* s) { delete (Scene*)s; }
 
+// Makes the scene two-level: one BVH per BLAS in object space and the instances (world-to-object
+// transforms inverted in double and rounded once, as the library does). Returns -1 on a bad
+// range, index or a singular transform.
+ORACLE_API int oracle_scene_set_instances(void* sp, const gbpt_blas_range* br, uint32_t nb,
+                                          const gbpt_instance* in, uint32_t ni) {
+    Scene& s = *(Scene*)sp;
+    s.blas.assign(nb, TriSet{});
+    for (uint32_t b = 0; b < nb; ++b) {
+        if ((uint64_t)br[b].first_geometry + br[b].geometry_count > s.geoms.size()) return -1;
+        TriSet& ts = s.blas[b];
+        for (uint32_t gi = br[b].first_geometry; gi < br[b].first_geometry + br[b].geometry_count; ++gi) {
+            const gbpt_geometry& g = s.geoms[gi];
+            for (uint32_t k = 0; k < g.triangle_count; ++k) {
+                const uint32_t tri = g.first_triangle + k;
+                for (int c = 0; c < 3; ++c) {
+                    const gbpt_packed_vertex& vv = s.verts[g.first_vertex + s.idx[3 * tri + c]];
+                    for (int a = 0; a < 3; ++a) ts.tv.push_back(vv.position[a]);
+                }
+                ts.tgeom.push_back(gi);
+                ts.tprim.push_back(k);
+            }
+        }
+        build_bvh(ts);
+    }
+    s.insts.clear();
+    for (uint32_t i = 0; i < ni; ++i) {
+        Instance x{};
+        if (in[i].blas >= nb) return -1;
+        std::memcpy(x.o2w, in[i].object_to_world, sizeof(x.o2w));
+        const float* m = in[i].object_to_world;
+        const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8],
+                     h = m[9], k = m[10];
+        const double A = e * k - f * h, B = -(d * k - f * g), Cc = d * h - e * g;
+        const double det = a * A + b * B + c * Cc;
+        if (!(std::fabs(det) > 1e-30)) return -1;
+        const double r[9] = {A / det, -(b * k - c * h) / det, (b * f - c * e) / det,
+                             B / det, (a * k - c * g) / det,  -(a * f - c * d) / det,
+                             Cc / det, -(a * h - b * g) / det, (a * e - b * d) / det};
+        const double t[3] = {m[3], m[7], m[11]};
+        for (int row = 0; row < 3; ++row) {
+            for (int col = 0; col < 3; ++col) x.w2o[4 * row + col] = (float)r[3 * row + col];
+            x.w2o[4 * row + 3] = (float)(-(r[3 * row] * t[0] + r[3 * row + 1] * t[1] +
+                                           r[3 * row + 2] * t[2]));
+        }
+        x.blas = in[i].blas;
+        x.mask = in[i].mask & 0xFFu;
+        x.first_geom = br[in[i].blas].first_geometry;
+        for (int q = 0; q < 3; ++q) {
+            x.lo[q] = INFINITY;
+            x.hi[q] = -INFINITY;
+        }
+        const TriSet& ts = s.blas[in[i].blas];
+        for (size_t v = 0; v < ts.tv.size() / 3; ++v)
+            for (int q = 0; q < 3; ++q) {
+                const double w = (double)m[4 * q] * ts.tv[3 * v] + (double)m[4 * q + 1] * ts.tv[3 * v + 1] +
+                                 (double)m[4 * q + 2] * ts.tv[3 * v + 2] + (double)m[4 * q + 3];
+                x.lo[q] = std::min(x.lo[q], w);
+                x.hi[q] = std::max(x.hi[q], w);
+            }
+        for (int q = 0; q < 3; ++q) { // cover the float rounding of transformed positions
+            const double pad = 1e-6 * (std::fabs(x.lo[q]) + std::fabs(x.hi[q]) + 1.0);
+            x.lo[q] -= pad;
+            x.hi[q] += pad;
+        }
+        s.insts.push_back(x);
+    }
+    build_lights(s);
+    return 0;
+}
+
+// RGBA8 textures and the sRGB decoding table (IEC 61966-2-1, in double, rounded once).
+ORACLE_API int oracle_scene_set_textures(void* sp, const gbpt_texture* t, uint32_t n) {
+    Scene& s = *(Scene*)sp;
+    s.tex.clear();
+    s.tex_info.clear();
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        s.tex_info.insert(s.tex_info.end(), {(uint32_t)total, t[i].width, t[i].height,
+                                             t[i].srgb ? 1u : 0u});
+        s.tex.insert(s.tex.end(), t[i].texels, t[i].texels + 4ull * t[i].width * t[i].height);
+        total += (uint64_t)t[i].width * t[i].height;
+    }
+    for (int i = 0; i < 256; ++i) {
+        const double c = i / 255.0;
+        s.srgb_lut[i] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+    }
+    return 0;
+}
+
+// merian's Hit: for a two-level hit the instance's custom index (the first geometry of its
+// BLAS), the TLAS instance and the geometry within the BLAS
 template <class R>
-static void fill_hit(const HitRec& h, gbpt_hit& o) {
+static void fill_hit(const Scene& s, const HitRec& h, gbpt_hit& o) {
     if (h.valid) {
-        o.instance_id = 0;
-        o.instance_index = 0;
+        const uint32_t first = h.inst == kNoInst ? 0u : s.insts[h.inst].first_geom;
+        o.instance_id = first;
+        o.instance_index = h.inst == kNoInst ? 0u : h.inst;
         o.primitive_id = h.prim;
-        o.geometry_index = h.geom;
+        o.geometry_index = h.geom - first;
         o.barycentrics[0] = h.u;
         o.barycentrics[1] = h.v;
         o.t = (float)h.t;
@@ -600,7 +843,7 @@ ORACLE_API int oracle_trace_primary(void* sp, const gbpt_camera* cam, uint32_t w
         } else {
             hr = trace<float>(s, camera_ray<float>(*cam, px, py, w, h), mask, false);
         }
-        fill_hit<float>(hr, out[i]);
+        fill_hit<float>(s, hr, out[i]);
         if (out_t64) out_t64[i] = hr.valid ? hr.t : -1.0;
     }
     return 0;
@@ -628,7 +871,7 @@ ORACLE_API int oracle_trace_rays(void* sp, const gbpt_ray* rays, uint32_t n, uin
                          rays[i].tmin, rays[i].tmax};
             hr = trace<float>(s, r, mask, any_hit != 0, &a, &b);
         }
-        fill_hit<float>(hr, out[i]);
+        fill_hit<float>(s, hr, out[i]);
         nn += a;
         nt += b;
     }
@@ -686,17 +929,36 @@ inline uint32_t global_tri(const Scene& s, uint32_t geom, uint32_t prim) {
     return s.geom_tri_base[geom] + prim;
 }
 
-// solid-angle pdf of reaching a point of an emissive triangle at squared distance dist2 along
-// direction dir (from the shading point towards the light)
-template <class R> inline R tri_light_pdf(const Scene& s, uint32_t tri_global, R dist2, V3<R> dir) {
-    const gbpt_geometry& g = s.geoms[s.tgeom[tri_global]];
-    const float* tv = &s.tv[9 * tri_global];
-    const V3<R> n = normalize(cross(mk<R>(tv[3] - tv[0], tv[4] - tv[1], tv[5] - tv[2]),
-                                    mk<R>(tv[6] - tv[0], tv[7] - tv[1], tv[8] - tv[2])));
+// World-space vertices of a hit triangle (object vertices placed by the hit's instance).
+template <class R>
+inline void world_tri(const Scene& s, uint32_t geom, uint32_t prim, uint32_t inst, V3<R> v[3]) {
+    const gbpt_geometry& g = s.geoms[geom];
+    const uint32_t tri = g.first_triangle + prim;
+    for (int c = 0; c < 3; ++c) {
+        const float* p = s.verts[g.first_vertex + s.idx[3 * tri + c]].position;
+        if (inst == kNoInst) {
+            v[c] = mk<R>(p[0], p[1], p[2]);
+        } else {
+            const float* r = s.insts[inst].o2w;
+            float w[3];
+            for (int a = 0; a < 3; ++a)
+                w[a] = (float)((double)r[4 * a] * p[0] + (double)r[4 * a + 1] * p[1] +
+                               (double)r[4 * a + 2] * p[2] + (double)r[4 * a + 3]);
+            v[c] = mk<R>(w[0], w[1], w[2]);
+        }
+    }
+}
+
+// solid-angle pdf of reaching a point of the emissive world-space triangle (a, b, c) of geometry
+// geom at squared distance dist2 along dir (from the shading point towards the light)
+template <class R>
+inline R tri_light_pdf(const Scene& s, const V3<R> tri[3], uint32_t geom, R dist2, V3<R> dir) {
+    const gbpt_geometry& g = s.geoms[geom];
+    const V3<R> n = normalize(cross(tri[1] - tri[0], tri[2] - tri[0]));
     const R cos_l = dot(dir, n);
     const gbpt_material& m = s.mats[g.material_id];
     const R lum = (R)(0.299 * m.emission[0] + 0.587 * m.emission[1] + 0.114 * m.emission[2]);
-    const R area = tri_area<R>(s, tri_global);
+    const R area = R(0.5) * length(cross(tri[1] - tri[0], tri[2] - tri[0]));
     const R pmf = area * lum / (R)s.light_total;
     return (R(1) - env_select_prob<R>(s)) * pmf / area * dist2 / std::fabs(cos_l);
 }
@@ -745,12 +1007,13 @@ LightSample<R> sample_light(const Scene& s, V3<R> pos, G& rng) {
     const uint32_t tri = s.light_tri[k];
     const R x = std::sqrt(u1);
     const R b0 = R(1) - x, b1 = x * (R(1) - u2), b2 = x * u2;
-    const V3<R> a = mk<R>(s.tv[9 * tri], s.tv[9 * tri + 1], s.tv[9 * tri + 2]);
-    const V3<R> b = mk<R>(s.tv[9 * tri + 3], s.tv[9 * tri + 4], s.tv[9 * tri + 5]);
-    const V3<R> c = mk<R>(s.tv[9 * tri + 6], s.tv[9 * tri + 7], s.tv[9 * tri + 8]);
+    const float* lt = &s.light_tv[9 * (size_t)tri];
+    const V3<R> a = mk<R>(lt[0], lt[1], lt[2]);
+    const V3<R> b = mk<R>(lt[3], lt[4], lt[5]);
+    const V3<R> c = mk<R>(lt[6], lt[7], lt[8]);
     const V3<R> pl = (b0 * a + b1 * b) + b2 * c;
     V3<R> n = normalize(cross(b - a, c - a));
-    const gbpt_geometry& g = s.geoms[s.tgeom[tri]];
+    const gbpt_geometry& g = s.geoms[s.light_geom[tri]];
     if (g.flags & GBPT_MESH_FLIP_FACING) n = -n;
     const V3<R> d = pl - pos;
     const R dist2 = dot(d, d);
@@ -761,7 +1024,8 @@ LightSample<R> sample_light(const Scene& s, V3<R> pos, G& rng) {
     const gbpt_material& m = s.mats[g.material_id];
     ls.le = mk<R>(m.emission[0], m.emission[1], m.emission[2]);
     ls.dist = dist * R(1 - 1e-4f);
-    ls.pdf = tri_light_pdf<R>(s, tri, dist2, ls.dir);
+    const V3<R> wt[3] = {a, b, c};
+    ls.pdf = tri_light_pdf<R>(s, wt, s.light_geom[tri], dist2, ls.dir);
     ls.valid = ls.pdf > R(0);
     return ls;
 }
@@ -835,8 +1099,9 @@ V3<R> trace_path(const Scene& s, const PathCfg& cfg, Ray<R> ray, SP<R> sp, Pcg& 
             if (!h.valid || (s.geoms[h.geom].flags & GBPT_MESH_USE_ENV_MAP)) {
                 pl = env_select_prob<R>(s) * env_pdf(s, ray.d);
             } else if (sp.emissive_tri) {
-                const uint32_t tri = global_tri(s, h.geom, h.prim);
-                pl = tri_light_pdf<R>(s, tri, pow2((R)h.t), ray.d);
+                V3<R> wt[3];
+                world_tri<R>(s, h.geom, h.prim, h.inst, wt);
+                pl = tri_light_pdf<R>(s, wt, h.geom, pow2((R)h.t), ray.d);
             }
             e = e * power_heuristic(bs.pdf, pl);
         }
@@ -975,10 +1240,12 @@ ORACLE_API int oracle_gbuffer(void* sp, const gbpt_camera* cam, uint32_t w, uint
         const Ray<R> r = camera_ray<R>(*cam, px, py, w, h);
         const HitRec hr = trace<R>(s, r, mask & 0xFFu, false);
         gbpt_gbuffer_texel t{};
-        t.instance_id = hr.valid ? 0u : 0xFFFFFFFFu;
-        t.primitive_id = hr.valid ? hr.prim : 0xFFFFFFFFu;
-        t.geometry_index = (uint16_t)(hr.valid ? hr.geom : 0xFFFFFFFFu);
-        t.instance_index = (uint16_t)(hr.valid ? 0u : 0xFFFFFFFFu);
+        gbpt_hit ph;
+        fill_hit<float>(s, hr, ph);
+        t.instance_id = ph.instance_id;
+        t.primitive_id = ph.primitive_id;
+        t.geometry_index = (uint16_t)ph.geometry_index;
+        t.instance_index = (uint16_t)ph.instance_index;
         t.barycentrics = hr.valid ? ((uint32_t)float_to_half(hr.v) << 16) | float_to_half(hr.u) : 0u;
         const bool env = !hr.valid || (s.geoms[hr.geom].flags & GBPT_MESH_USE_ENV_MAP);
         if (env) {
@@ -993,10 +1260,15 @@ ORACLE_API int oracle_gbuffer(void* sp, const gbpt_camera* cam, uint32_t w, uint
             const SP<R> q = shading_point<R>(s, r, hr, R(1), true, false);
             const gbpt_geometry& g = s.geoms[hr.geom];
             const uint32_t tri = g.first_triangle + hr.prim;
-            const V3<R> p0 = fetch_pos<R>(s, g.first_vertex + s.idx[3 * tri + 0]);
-            const V3<R> p1 = fetch_pos<R>(s, g.first_vertex + s.idx[3 * tri + 1]);
-            const V3<R> p2 = fetch_pos<R>(s, g.first_vertex + s.idx[3 * tri + 2]);
-            V3<R> fn = normalize(cross(p1 - p0, p2 - p0));
+            V3<R> p0 = fetch_pos<R>(s, g.first_vertex + s.idx[3 * tri + 0]);
+            V3<R> p1 = fetch_pos<R>(s, g.first_vertex + s.idx[3 * tri + 1]);
+            V3<R> p2 = fetch_pos<R>(s, g.first_vertex + s.idx[3 * tri + 2]);
+            V3<R> e1 = p1 - p0, e2 = p2 - p0;
+            if (hr.inst != kNoInst) {
+                e1 = xform_vector<R>(s.insts[hr.inst].o2w, e1);
+                e2 = xform_vector<R>(s.insts[hr.inst].o2w, e2);
+            }
+            V3<R> fn = normalize(cross(e1, e2));
             if (g.flags & GBPT_MESH_FLIP_FACING) fn = -fn;
             const R lz = length(q.pos - r.o);
             // Surface::compute_grad_z (hit.slang:99-103)

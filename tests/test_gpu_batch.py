@@ -230,3 +230,45 @@ def test_server_stop_cancels_queued(gpu_ctx, scenes):
     assert gpu_ctx.lib.gbpt_server_poll(gpu_ctx.handle, ts[0], None) == N.GBPT_ERR_INVALID
     sid = gpu_ctx.upload(S.cornell())
     gpu_ctx.destroy_scene(sid)
+
+
+def test_material_sorted_shading_same_result(gpu_ctx, scenes):
+    """'shader execution reordering' (sort_materials) only changes the order in which queue
+    entries are shaded: every output is bit-identical, alone and in a batch."""
+    from merian_gb300 import scene as S
+    jobs = _jobs(scenes, S)
+    ref = _alone(gpu_ctx, jobs)
+    for _, _, p, _ in jobs:
+        p.sort_materials = 1
+    assert all(_same(a, b) for a, b in zip(ref, _alone(gpu_ctx, jobs)))
+    outs = gpu_ctx.render_batch([(s, c, p) for s, c, p, _ in jobs])
+    assert all(_same(a, b) for a, b in zip(ref, outs))
+
+
+def test_tuning_and_autotune_same_result(gpu_ctx, scenes):
+    """The context's tuning (tick size, forced material sort, graphs) and the autotuner's choice
+    change only the schedule: every output is bit-identical to the default schedule's."""
+    from merian_gb300 import scene as S
+    jobs = _jobs(scenes, S)
+    ref = _alone(gpu_ctx, jobs)
+    corn, soup, cams = scenes
+    try:
+        for wave, sort, graphs in ((1 << 12, 1, False), (1 << 20, 0, True), (1 << 24, -1, False)):
+            gpu_ctx.set_tuning(wave, sort, graphs)
+            t = gpu_ctx.get_tuning()
+            assert (t.wave_paths, t.sort_materials, t.use_graphs) == (wave, sort, int(graphs))
+            assert all(_same(a, b) for a, b in zip(ref, _alone(gpu_ctx, jobs)))
+            outs = gpu_ctx.render_batch([(s, c, p) for s, c, p, _ in jobs if p.spp <= wave])
+            kept = [r for r, j in zip(ref, jobs) if j[2].spp <= wave]
+            assert all(_same(a, b) for a, b in zip(kept, outs))
+        with pytest.raises(N.GbptError):
+            gpu_ctx.set_tuning(100, 0, False)  # below the smallest tick
+        p, _ = S.render_params(320, 180, 16, 8, nee=True, rr_depth=3, frame=1)
+        t, ms = gpu_ctx.autotune(soup, cams[soup], p)
+        assert len(ms) == 8 and all(m > 0 for m in ms)
+        assert t.wave_paths in (1 << 21, 1 << 22, 1 << 23, 1 << 24) and t.sort_materials in (0, 1)
+        got = gpu_ctx.get_tuning()
+        assert (got.wave_paths, got.sort_materials) == (t.wave_paths, t.sort_materials)
+        assert all(_same(a, b) for a, b in zip(ref, _alone(gpu_ctx, jobs)))
+    finally:
+        gpu_ctx.set_tuning(0, -1, False)

@@ -69,7 +69,7 @@ def test_gbuffer_matches_oracle(gpu_ctx, scene):
     for k in ("instance_id", "primitive_id", "geometry_index", "instance_index", "barycentrics"):
         assert np.array_equal(g[k], o[k]), k
     hit = g["instance_id"] == 0
-    assert hit.mean() > 0.5
+    assert hit.mean() > (0.9 if name == "cornell" else 0.3)
     assert np.allclose(g["linear_z"], o["linear_z"], rtol=1e-6)
     assert np.all(g["linear_z"][~hit] == 65504.0)
     dots = np.sum(decode_normal(g["encoded_normal"]) * decode_normal(o["encoded_normal"]), -1)
