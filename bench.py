@@ -43,6 +43,9 @@ def parse():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default schedule instead of gbpt_autotune's choice of tick "
+                         "size and material sorting (made before the warm-up, untimed)")
     # the mixed workloads (--workload batch-256 | served-stream)
     ap.add_argument("--scenes", type=int, default=None, help="scenes of a mixed workload")
     ap.add_argument("--requests", type=int, default=96, help="requests per served-stream rate")
@@ -252,6 +255,11 @@ def run_gbpt(args):
         return p
 
     frame_base = 1_000_000 * rank
+    tuning = None
+    if not args.no_autotune:
+        t, cand_ms = ctx.autotune(sid, cam, params(frame_base + 998))
+        tuning = {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials,
+                  "candidates_ms": [round(m, 2) for m in cand_ms]}
     for i in range(args.warmup):
         ctx.render_device(sid, cam, params(frame_base + i), out.data_ptr())
     torch.cuda.synchronize()
@@ -356,6 +364,8 @@ def run_gbpt(args):
                          "trace_rays_per_step": trace_rays // max(args.steps, 1),
                          "trace_share_of_step": round(trace_ms / args.steps / ms, 4)},
         }
+        if tuning is not None:
+            line["config"]["tuning"] = tuning
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(sc, cam, w, args.cpu_seconds)
         print(json.dumps(line), flush=True)

@@ -48,6 +48,11 @@ extern "C" {
 #define GBPT_MESH_HAS_TANGENTS 0x20u /* per-vertex tangents are meaningful */
 #define GBPT_MESH_FLAT_SHADING 0x40u /* shading normal = face normal */
 #define GBPT_MESH_USE_ENV_MAP 0x80u  /* hits shade as the environment along the ray */
+/* Non-opaque geometry (merian: IsOpaque = 0x4 cleared, scene.hpp:46): every candidate hit runs the
+ * material's alpha test (material-system.slang:28-38, scene.slang:500-519) and is skipped when the
+ * alpha texture's alpha at the hit's uv is below 0.5. Off by default: geometry is opaque, as in
+ * merian's ForceOpaque instances (scene.cpp:1849-1850). */
+#define GBPT_MESH_ALPHA_TEST 0x100u
 
 /* ---- material models (merian MaterialSystem type ids, material-system.slang:51-56) --------- */
 #define GBPT_MATERIAL_DIFFUSE 0u              /* DiffuseMaterial (diffuse-material.slang) */
@@ -88,7 +93,8 @@ typedef struct gbpt_material {
     float transmission_weight;
     float transmission_color[3];
     int32_t base_color_texture; /* -1 = none */
-    uint32_t reserved[3];
+    int32_t alpha_texture;      /* -1 = none; its alpha channel is the alpha test's mask */
+    uint32_t reserved[2];
 } gbpt_material;
 
 /* RGBA8 texture (a material's base_color_texture), sampled bilinearly with repeat addressing at
@@ -481,6 +487,31 @@ GBPT_API int gbpt_gen_blob(uint64_t seed, uint32_t n_u, uint32_t n_v, gbpt_packe
                            uint32_t* indices);
 /* A tileable sRGB value-noise RGBA8 texture, width * height * 4 bytes. */
 GBPT_API int gbpt_gen_noise_texture(uint64_t seed, uint32_t width, uint32_t height, uint8_t* rgba);
+
+/* ---- scene loader (merian PBRTScene, src/merian-shaders/scene/pbrt_scene.cpp) ----------------
+ * gbpt_load_pbrt parses a pbrt-v4 scene file (Include/Import followed) into host arrays that
+ * gbpt_loaded_scene_info exposes as a gbpt_scene_desc for gbpt_scene_create, with the file's
+ * camera and film size. Shapes: trianglemesh, loopsubdiv (unsubdivided), plymesh (ASCII and
+ * binary PLY), sphere, disk; materials: diffuse, coateddiffuse, conductor, coatedconductor,
+ * dielectric, thindielectric, mix (the more probable side), others approximated as diffuse, as
+ * merian converts them; diffuse area lights as emission; ObjectBegin/ObjectInstance as TLAS
+ * instances; a constant infinite light as a uniform environment. Features it skips (image
+ * textures and environments, other lights, media) are listed by gbpt_loaded_scene_warning. */
+typedef struct gbpt_loaded_scene gbpt_loaded_scene;
+typedef struct gbpt_loaded_info {
+    gbpt_scene_desc desc; /* arrays owned by the loaded scene, valid until it is freed */
+    gbpt_camera camera;   /* pbrt's perspective camera (fov on the shorter image axis) */
+    uint32_t width;       /* Film xresolution (default 1280) */
+    uint32_t height;      /* Film yresolution (default 720) */
+    uint32_t warning_count;
+    uint32_t reserved;
+} gbpt_loaded_info;
+
+GBPT_API int gbpt_load_pbrt(const char* path, gbpt_loaded_scene** out);
+GBPT_API int gbpt_loaded_scene_info(const gbpt_loaded_scene* scene, gbpt_loaded_info* info);
+/* Warning i (0 <= i < warning_count) of the load, or NULL. */
+GBPT_API const char* gbpt_loaded_scene_warning(const gbpt_loaded_scene* scene, uint32_t i);
+GBPT_API void gbpt_loaded_scene_free(gbpt_loaded_scene* scene);
 
 #ifdef __cplusplus
 }

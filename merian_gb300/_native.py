@@ -28,6 +28,7 @@ MESH_TWO_SIDED = 0x10
 MESH_HAS_TANGENTS = 0x20
 MESH_FLAT_SHADING = 0x40
 MESH_USE_ENV_MAP = 0x80
+MESH_ALPHA_TEST = 0x100
 
 MATERIAL_DIFFUSE = 0
 MATERIAL_OPENPBR = 1
@@ -42,7 +43,8 @@ MATERIAL_DTYPE = np.dtype([("model", "<u4"), ("base_color", "<f4", 3), ("metalne
                            ("specular_alpha", "<f4", 2), ("specular_weight", "<f4"),
                            ("specular_ior", "<f4"), ("emission", "<f4", 3),
                            ("transmission_weight", "<f4"), ("transmission_color", "<f4", 3),
-                           ("base_color_texture", "<i4"), ("reserved", "<u4", 3)])
+                           ("base_color_texture", "<i4"), ("alpha_texture", "<i4"),
+                           ("reserved", "<u4", 2)])
 HIT_DTYPE = np.dtype([("instance_id", "<u4"), ("instance_index", "<u4"), ("primitive_id", "<u4"),
                       ("geometry_index", "<u4"), ("barycentrics", "<f4", 2), ("t", "<f4"),
                       ("reserved", "<u4")])
@@ -104,6 +106,11 @@ class SceneDesc(C.Structure):
                 ("texture_count", C.c_uint32), ("blas_ranges", C.c_void_p),
                 ("blas_count", C.c_uint32), ("instances", C.c_void_p),
                 ("instance_count", C.c_uint32)]
+
+
+class LoadedInfo(C.Structure):
+    _fields_ = [("desc", SceneDesc), ("camera", Camera), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("warning_count", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class Request(C.Structure):
@@ -210,6 +217,10 @@ EXPORTS = [
                                 C.c_void_p, C.c_void_p]),
     ("gbpt_gen_blob", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("gbpt_gen_noise_texture", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p]),
+    ("gbpt_load_pbrt", C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    ("gbpt_loaded_scene_info", C.c_int, [C.c_void_p, C.POINTER(LoadedInfo)]),
+    ("gbpt_loaded_scene_warning", C.c_char_p, [C.c_void_p, C.c_uint32]),
+    ("gbpt_loaded_scene_free", None, [C.c_void_p]),
     ("gbpt_gen_env", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p]),
 ]
 

@@ -288,7 +288,8 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
             const gbpt_geometry& geo = d->geometries[g];
             const uint32_t tf = (geo.instance_mask & 0xFFu) |
                                 ((geo.flags & GBPT_MESH_TWO_SIDED) ? (1u << 8) : 0u) |
-                                ((geo.flags & GBPT_MESH_FLIP_FACING) ? (1u << 9) : 0u);
+                                ((geo.flags & GBPT_MESH_FLIP_FACING) ? (1u << 9) : 0u) |
+                                ((geo.flags & GBPT_MESH_ALPHA_TEST) ? (1u << 10) : 0u);
             for (uint32_t k = 0; k < geo.triangle_count; ++k) {
                 const uint64_t tri = (uint64_t)geo.first_triangle + k;
                 for (int c = 0; c < 3; ++c) {
@@ -583,6 +584,8 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
         if ((rc = upload(&s.srgb_lut, lut, sizeof(lut), bytes))) return fail(rc);
         s.n_tex = d->texture_count;
     }
+    for (uint32_t g = 0; g < d->geometry_count; ++g)
+        s.alpha |= (d->geometries[g].flags & GBPT_MESH_ALPHA_TEST) != 0u;
     s.bytes = bytes;
     const uint32_t id = ctx->next_scene++;
     ctx->scenes[id] = s;

@@ -1,4 +1,5 @@
-// Host BVH builder: binned-SAH binary BVH, greedily collapsed to an 8-wide tree and written in
+// Host BVH builder: binned-SAH binary BVH, greedily collapsed to an 8-wide tree (inner children
+// expanded by surface area, then free slots filled by splitting multi-triangle leaves) and written in
 // the compressed-wide layout of Ylitie, Karras and Laine, "Efficient Incoherent Ray Traversal on
 // GPUs Through Compressed Wide BVHs" (HPG 2017): 80-byte nodes with 8-bit child boxes relative to
 // a per-node origin and power-of-two scale, octant-ordered child slots, and up to three
@@ -47,8 +48,14 @@ struct B2Node {
     bool leaf = true;
 };
 
-constexpr int kBins = 32;
-constexpr float kCostTraverse = 0.5f; // relative to one triangle test
+#ifndef GBPT_BVH_BINS
+#define GBPT_BVH_BINS 32
+#endif
+#ifndef GBPT_BVH_TRAVERSE_COST
+#define GBPT_BVH_TRAVERSE_COST 0.5f
+#endif
+constexpr int kBins = GBPT_BVH_BINS;
+constexpr float kCostTraverse = GBPT_BVH_TRAVERSE_COST; // relative to one triangle test
 constexpr uint32_t kMaxLeaf = 3;      // CWBVH leaf children hold up to three triangles
 
 struct Builder {
@@ -306,6 +313,22 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
                 float best_area = -1.0f;
                 for (size_t i = 0; i < ch.size(); ++i) {
                     if (is_inner(ch[i]) && b2[ch[i]].box.area() > best_area) {
+                        best_area = b2[ch[i]].box.area();
+                        best = (int)i;
+                    }
+                }
+                if (best < 0) break;
+                const uint32_t k = ch[best];
+                ch[best] = b2[k].left;
+                ch.push_back(b2[k].right);
+            }
+            // Slots left empty cost the traversal as much as full ones: split the largest
+            // multi-triangle leaf children into their binary children while slots remain.
+            while (ch.size() < 8) {
+                int best = -1;
+                float best_area = -1.0f;
+                for (size_t i = 0; i < ch.size(); ++i) {
+                    if (!b2[ch[i]].leaf && b2[ch[i]].box.area() > best_area) {
                         best_area = b2[ch[i]].box.area();
                         best = (int)i;
                     }

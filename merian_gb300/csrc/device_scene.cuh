@@ -20,6 +20,7 @@ struct GeomGPU {
 // per-triangle flag word (third float4 of a triangle record)
 constexpr uint32_t kTriTwoSided = 1u << 8;
 constexpr uint32_t kTriFlip = 1u << 9;
+constexpr uint32_t kTriAlpha = 1u << 10; // non-opaque geometry: candidate hits run the alpha test
 
 struct DevScene {
     const uint4* __restrict__ nodes;  // 5 per CWBVH node
@@ -60,6 +61,56 @@ struct Hit {
     uint32_t prim, geom; // geom = 0xFFFFFFFF on miss (the scene-global geometry index)
     uint32_t inst;       // instance index of two-level scenes, 0xFFFFFFFF otherwise
 };
+
+// ---- alpha test of non-opaque geometry (material-system.slang:28-38, scene.slang:500-519) --------
+// The material's alpha texture, bilinear with repeat addressing at level 0, at the candidate hit's
+// interpolated uv; alpha below 0.5 (merian_alpha_test_threshold) discards the candidate. Rounded
+// operations in a fixed order, shared with the oracle, so the decision is bit-identical.
+constexpr float kAlphaThreshold = 0.5f;
+
+GBPT_DI float texture_alpha(const DevScene& sc, uint32_t t, float u, float v) {
+    const uint4 info = __ldg(&sc.tex_info[t]);
+    const int w = (int)info.y, h = (int)info.z;
+    if (!(fabsf(u) < 65536.0f)) u = 0.0f; // half uvs: only NaN / inf are out of range
+    if (!(fabsf(v) < 65536.0f)) v = 0.0f;
+    const float x = __fsub_rn(__fmul_rn(u, (float)w), 0.5f);
+    const float y = __fsub_rn(__fmul_rn(v, (float)h), 0.5f);
+    const float fx = floorf(x), fy = floorf(y);
+    const float a = __fsub_rn(x, fx), b = __fsub_rn(y, fy);
+    const int ix = (int)fx, iy = (int)fy;
+    const int x0 = ((ix % w) + w) % w, x1 = (((ix + 1) % w) + w) % w;
+    const int y0 = ((iy % h) + h) % h, y1 = (((iy + 1) % h) + h) % h;
+    const uchar4* base = sc.tex + info.x;
+    auto alpha = [&](int xx, int yy) {
+        return __fmul_rn((float)__ldg(&base[(size_t)yy * w + xx]).w, 1.0f / 255.0f);
+    };
+    const float ia = __fsub_rn(1.0f, a), ib = __fsub_rn(1.0f, b);
+    const float top = __fadd_rn(__fmul_rn(alpha(x0, y0), ia), __fmul_rn(alpha(x1, y0), a));
+    const float bot = __fadd_rn(__fmul_rn(alpha(x0, y1), ia), __fmul_rn(alpha(x1, y1), a));
+    return __fadd_rn(__fmul_rn(top, ib), __fmul_rn(bot, b));
+}
+
+// True when the candidate hit (geometry, primitive, barycentrics u, v) is transparent.
+GBPT_DI bool alpha_discard(const DevScene& sc, uint32_t geom, uint32_t prim, float bu, float bv) {
+    const GeomGPU g = sc.geoms[geom];
+    const int tex = __float_as_int(__ldg(&sc.mats[5ull * g.material + 4]).y);
+    if (tex < 0 || (uint32_t)tex >= sc.n_tex) return false;
+    const uint32_t tri = g.first_triangle + prim;
+    float uvx[3], uvy[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t vi = g.first_vertex + __ldg(&sc.idx[3 * tri + k]);
+        const uint32_t uv = __ldg(&sc.verts[6ull * vi + 4]);
+        uvx[k] = __half2float(__ushort_as_half((unsigned short)(uv & 0xFFFFu)));
+        uvy[k] = __half2float(__ushort_as_half((unsigned short)(uv >> 16)));
+    }
+    const float b0 = __fsub_rn(__fsub_rn(1.0f, bu), bv);
+    const float u = __fadd_rn(__fadd_rn(__fmul_rn(b0, uvx[0]), __fmul_rn(bu, uvx[1])),
+                              __fmul_rn(bv, uvx[2]));
+    const float v = __fadd_rn(__fadd_rn(__fmul_rn(b0, uvy[0]), __fmul_rn(bu, uvy[1])),
+                              __fmul_rn(bv, uvy[2]));
+    return texture_alpha(sc, (uint32_t)tex, u, v) < kAlphaThreshold;
+}
 
 // ---- watertight test (Woop, Benthin, Wald 2013) -------------------------------------------------
 // Explicit round-to-nearest intrinsics (no FMA contraction) so the float result equals the
@@ -329,9 +380,10 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
 // = kNoInst on a miss; with ANY the first hit found) or, with WARP, until the warp should refill
 // its idle lanes (returns false; s keeps the state). `st(i)` is stack entry i. A stack overflow
 // raises *err and finishes the ray with what it found.
-template <bool ANY, bool COUNT, bool TWO_LEVEL, bool WARP, class StackRef>
+// `alpha(geom, prim, u, v)` decides the candidate hits of non-opaque triangles (true: skip).
+template <bool ANY, bool COUNT, bool TWO_LEVEL, bool WARP, class StackRef, class Alpha>
 GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32_t* err,
-                        bool pool_empty) {
+                        bool pool_empty, const Alpha& alpha) {
     while (true) {
         if (s.ngroup.y > 0x00FFFFFFu) {
             const uint32_t hits = s.ngroup.y;
@@ -399,6 +451,7 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
             if (t < s.best.t || geom < s.best.geom ||
                 (geom == s.best.geom &&
                  (prim < s.best.prim || (prim == s.best.prim && s.inst < s.best.inst)))) {
+                if ((tfl & kTriAlpha) && alpha(geom, prim, u, v)) continue;
                 s.best.t = t;
                 s.best.u = u;
                 s.best.v = v;
@@ -439,18 +492,21 @@ __device__ __forceinline__ Hit trace_ray(const DevScene& sc, float3 o, float3 d,
     s.mask = ray_mask;
     trace_init(s, o, d, tmin, tmax);
     uint2 stack[kStackSize];
-    trace_loop<ANY, COUNT, true, false>(s, [&](int i) -> uint2& { return stack[i]; }, ctr, err,
-                                        true);
+    trace_loop<ANY, COUNT, true, false>(
+        s, [&](int i) -> uint2& { return stack[i]; }, ctr, err, true,
+        [&](uint32_t g, uint32_t p, float u, float v) { return alpha_discard(sc, g, p, u, v); });
     return s.best;
 }
 
 // Runs the traversal of every ray i < n with persistent warps that pull ray indices from *fetch
 // (zero before the launch; one atomic per warp for all idle lanes). load(i, state) sets ray i's
-// scene (nodes, tris, insts), mask and calls trace_init; store(i, hit) receives its result. Must
-// be called by all 32 lanes of every warp.
-template <bool ANY, bool COUNT, bool TWO_LEVEL, class Load, class Store>
+// scene (nodes, tris, insts), mask and calls trace_init; store(i, hit) receives its result;
+// alpha(i, geom, prim, u, v) is ray i's alpha test (true: skip the candidate). Must be called by
+// all 32 lanes of every warp.
+template <bool ANY, bool COUNT, bool TWO_LEVEL, class Load, class Store, class Alpha>
 __device__ __forceinline__ void trace_persistent(uint32_t n, uint32_t* fetch, Load load,
-                                                 Store store, TraceCounters* ctr, uint32_t* err) {
+                                                 Store store, Alpha alpha, TraceCounters* ctr,
+                                                 uint32_t* err) {
     const uint32_t lane = threadIdx.x & 31u;
 #if GBPT_SMEM_STACK > 0
     // the first GBPT_SMEM_STACK entries of every thread's stack in shared memory (thread-strided:
@@ -491,7 +547,10 @@ __device__ __forceinline__ void trace_persistent(uint32_t n, uint32_t* fetch, Lo
         // once a lane found the pool empty, leaving the loop to refill gains nothing
         const bool pool_empty = __ballot_sync(0xFFFFFFFFu, exhausted) != 0u;
         if (!active) continue;
-        if (trace_loop<ANY, COUNT, TWO_LEVEL, true>(s, st_ref, ctr, err, pool_empty)) {
+        const auto ray_alpha = [&](uint32_t g, uint32_t p, float u, float v) {
+            return alpha(ray, g, p, u, v);
+        };
+        if (trace_loop<ANY, COUNT, TWO_LEVEL, true>(s, st_ref, ctr, err, pool_empty, ray_alpha)) {
             store(ray, s.best);
             active = false;
         }

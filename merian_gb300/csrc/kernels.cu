@@ -49,7 +49,10 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
                    f3(r.direction[0], r.direction[1], r.direction[2]), r.tmin, r.tmax);
     };
     auto store = [&](uint32_t i, const Hit& h) { hits[i] = to_hit(sc, h); };
-    trace_persistent<ANY, true, true>(n, fetch, load, store, &ctr, err);
+    auto alpha = [&](uint32_t, uint32_t g, uint32_t p, float u, float v) {
+        return alpha_discard(sc, g, p, u, v);
+    };
+    trace_persistent<ANY, true, true>(n, fetch, load, store, alpha, &ctr, err);
     if (work_ctr) {
         atomicAdd(work_ctr + 0, (unsigned long long)ctr.nodes);
         atomicAdd(work_ctr + 1, (unsigned long long)ctr.tris);

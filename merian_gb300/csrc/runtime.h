@@ -44,6 +44,7 @@ struct SceneGPU {
     void* tex_info = nullptr; // uint4 per texture: first texel, width, height, sRGB
     void* srgb_lut = nullptr; // 256 floats
     uint32_t n_tex = 0;
+    bool alpha = false; // some geometry is alpha-tested (GBPT_MESH_ALPHA_TEST)
     uint32_t depth = 0;
     uint64_t bytes = 0;
 };

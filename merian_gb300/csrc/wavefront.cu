@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM) k_shade_primary(TickAr
 }
 
 // Closest hit for every entry of ray queue `qi` (persistent warps, counter w.counters[4]).
-template <bool COUNT, bool TWO_LEVEL>
+template <bool COUNT, bool TWO_LEVEL, bool ALPHA>
 __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
     k_trace(TickArgs t, int qi, unsigned long long* work_ctr) {
     const uint32_t n = t.w.counters[qi];
@@ -291,7 +291,11 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
         t.w.hit_geom[i] = h.geom;
         t.w.hit_inst[i] = h.inst;
     };
-    trace_persistent<false, COUNT, TWO_LEVEL>(n, t.w.counters + 4, load, store, &ctr,
+    auto alpha = [&](uint32_t i, uint32_t g, uint32_t p, float u, float v) {
+        return ALPHA &&
+               alpha_discard(t.scenes[t.chunks[__ldg(&qp[i]) >> kPathBits].scene], g, p, u, v);
+    };
+    trace_persistent<false, COUNT, TWO_LEVEL>(n, t.w.counters + 4, load, store, alpha, &ctr,
                                               t.w.counters + 3);
     if (COUNT) {
         atomicAdd(work_ctr + 0, (unsigned long long)ctr.nodes);
@@ -434,7 +438,7 @@ __global__ void __launch_bounds__(256) k_sort_scatter(TickArgs t, int qi, uint32
 
 // Occlusion of the NEE queue; unoccluded contributions are added to their path (one shadow ray
 // per path per bounce, so no two lanes write the same path).
-template <bool TWO_LEVEL>
+template <bool TWO_LEVEL, bool ALPHA>
 __global__ void __launch_bounds__(128, kTraceBlocksPerSM) k_shadow(TickArgs t) {
     const uint32_t n = t.w.counters[2];
     auto load = [&](uint32_t i, TraceState& s) {
@@ -458,7 +462,11 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM) k_shadow(TickArgs t) {
             t.w.rad[p] = r;
         }
     };
-    trace_persistent<true, false, TWO_LEVEL>(n, t.w.counters + 5, load, store, nullptr,
+    auto alpha = [&](uint32_t i, uint32_t g, uint32_t p, float u, float v) {
+        return ALPHA && alpha_discard(t.scenes[t.chunks[__ldg(&t.w.s_path[i]) >> kPathBits].scene],
+                                      g, p, u, v);
+    };
+    trace_persistent<true, false, TWO_LEVEL>(n, t.w.counters + 5, load, store, alpha, nullptr,
                                              t.w.counters + 3);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         atomicAdd(t.w.stats + 0, (unsigned long long)n);
@@ -663,6 +671,7 @@ struct TickPlan {
     bool nee;
     bool sort; // material-sorted shading (some request asked for it and the Work has the buffers)
     bool two_level; // some chunk's scene is instanced: the two-level traversal variants
+    bool alpha;     // some chunk's scene has alpha-tested geometry: the alpha-test variants
 };
 
 struct Grids {
@@ -675,10 +684,36 @@ Grids launch_grids() {
     Grids g;
     g.grid = num_sms() * 8;
     // the two-level variants have the same launch bounds, hence the same residency
-    g.trace = persistent_grid(k_trace<false, false>);
-    g.trace_c = persistent_grid(k_trace<true, false>);
-    g.shadow = persistent_grid(k_shadow<false>);
+    g.trace = persistent_grid(k_trace<false, false, false>);
+    g.trace_c = persistent_grid(k_trace<true, false, false>);
+    g.shadow = persistent_grid(k_shadow<false, false>);
     return g;
+}
+
+// The traversal variants of a tick: work counters, two-level scenes, alpha-tested geometry (the
+// variants without a feature leave its code out; they find the same hits on scenes without it).
+void launch_trace(const TickArgs& ta, const TickPlan& tp, const Grids& g, int qi,
+                  unsigned long long* work_ctr, cudaStream_t st) {
+    const int gr = work_ctr ? g.trace_c : g.trace;
+    switch ((work_ctr ? 4 : 0) | (tp.two_level ? 2 : 0) | (tp.alpha ? 1 : 0)) {
+    case 0: k_trace<false, false, false><<<gr, 128, 0, st>>>(ta, qi, nullptr); break;
+    case 1: k_trace<false, false, true><<<gr, 128, 0, st>>>(ta, qi, nullptr); break;
+    case 2: k_trace<false, true, false><<<gr, 128, 0, st>>>(ta, qi, nullptr); break;
+    case 3: k_trace<false, true, true><<<gr, 128, 0, st>>>(ta, qi, nullptr); break;
+    case 4: k_trace<true, false, false><<<gr, 128, 0, st>>>(ta, qi, work_ctr); break;
+    case 5: k_trace<true, false, true><<<gr, 128, 0, st>>>(ta, qi, work_ctr); break;
+    case 6: k_trace<true, true, false><<<gr, 128, 0, st>>>(ta, qi, work_ctr); break;
+    default: k_trace<true, true, true><<<gr, 128, 0, st>>>(ta, qi, work_ctr); break;
+    }
+}
+
+void launch_shadow(const TickArgs& ta, const TickPlan& tp, const Grids& g, cudaStream_t st) {
+    switch ((tp.two_level ? 2 : 0) | (tp.alpha ? 1 : 0)) {
+    case 0: k_shadow<false, false><<<g.shadow, 128, 0, st>>>(ta); break;
+    case 1: k_shadow<false, true><<<g.shadow, 128, 0, st>>>(ta); break;
+    case 2: k_shadow<true, false><<<g.shadow, 128, 0, st>>>(ta); break;
+    default: k_shadow<true, true><<<g.shadow, 128, 0, st>>>(ta); break;
+    }
 }
 
 // The kernel sequence of one tick; returns the number of kernel launches. Counter words
@@ -707,8 +742,7 @@ uint64_t enqueue_tick(const TickArgs& ta, const TickPlan& tp, const Grids& g, cu
     if (nee) {
         cudaMemsetAsync(ctr + 5, 0, sizeof(uint32_t), st);
         ev = prof->begin(st, 2);
-        if (tp.two_level) k_shadow<true><<<g.shadow, 128, 0, st>>>(ta);
-        else k_shadow<false><<<g.shadow, 128, 0, st>>>(ta);
+        launch_shadow(ta, tp, g, st);
         prof->end(st, ev);
         cudaMemsetAsync(ctr + 2, 0, sizeof(uint32_t), st);
         nl += 1;
@@ -718,10 +752,7 @@ uint64_t enqueue_tick(const TickArgs& ta, const TickPlan& tp, const Grids& g, cu
         const int qo = qi ^ 1;
         cudaMemsetAsync(ctr + 4, 0, sizeof(uint32_t), st);
         ev = prof->begin(st, 0);
-        if (work_ctr && tp.two_level) k_trace<true, true><<<g.trace_c, 128, 0, st>>>(ta, qi, work_ctr);
-        else if (work_ctr) k_trace<true, false><<<g.trace_c, 128, 0, st>>>(ta, qi, work_ctr);
-        else if (tp.two_level) k_trace<false, true><<<g.trace, 128, 0, st>>>(ta, qi, nullptr);
-        else k_trace<false, false><<<g.trace, 128, 0, st>>>(ta, qi, nullptr);
+        launch_trace(ta, tp, g, qi, work_ctr, st);
         prof->end(st, ev);
         const uint32_t* perm = nullptr;
         if (tp.sort) {
@@ -741,8 +772,7 @@ uint64_t enqueue_tick(const TickArgs& ta, const TickPlan& tp, const Grids& g, cu
         if (nee && k < L) {
             cudaMemsetAsync(ctr + 5, 0, sizeof(uint32_t), st);
             ev = prof->begin(st, 2);
-            if (tp.two_level) k_shadow<true><<<g.shadow, 128, 0, st>>>(ta);
-        else k_shadow<false><<<g.shadow, 128, 0, st>>>(ta);
+            launch_shadow(ta, tp, g, st);
             prof->end(st, ev);
             cudaMemsetAsync(ctr + 2, 0, sizeof(uint32_t), st);
             nl += 1;
@@ -816,7 +846,7 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
     DevScene* scenes = (DevScene*)(sb + lay.scenes);
     ChunkGPU* chunks = (ChunkGPU*)(sb + lay.chunks);
     e.scene_ptrs.clear();
-    TickPlan tp{0, 0, 0, 0, 1, false, false, false};
+    TickPlan tp{0, 0, 0, 0, 1, false, false, false, false};
     uint64_t paths = 0, pix = 0;
     for (uint32_t i = 0; i < n_items && tp.n_chunks < cap; ++i) {
         TickItem& it = *items[i];
@@ -846,6 +876,7 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
         c.tris = scenes[si].tris;
         c.insts = scenes[si].n_inst ? scenes[si].inst : nullptr;
         tp.two_level |= scenes[si].n_inst != 0u;
+        tp.alpha |= it.scene->alpha;
         ++tp.n_chunks;
         paths += fit * S;
         pix += fit;
@@ -890,7 +921,8 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
             e.graph_tables = w.tables;
         }
         const uint32_t shape =
-            tp.max_len * 8u + (tp.nee ? 1u : 0u) + (tp.sort ? 2u : 0u) + (tp.two_level ? 4u : 0u);
+            tp.max_len * 16u + (tp.nee ? 1u : 0u) + (tp.sort ? 2u : 0u) + (tp.two_level ? 4u : 0u) +
+            (tp.alpha ? 8u : 0u);
         const TickEngine::Graph* found = nullptr;
         for (const auto& g : e.graphs)
             if (g.shape == shape) found = &g;

@@ -190,6 +190,47 @@ WORKLOADS = {
 }
 
 
+def load_pbrt(path: str):
+    """A pbrt-v4 scene file through gbpt_load_pbrt: (SceneData with its own copies of the arrays,
+    the file's camera, (width, height), warnings)."""
+    lib = N.load()
+    h = C.c_void_p()
+    N.check(lib.gbpt_load_pbrt(str(path).encode(), C.byref(h)))
+    try:
+        info = N.LoadedInfo()
+        N.check(lib.gbpt_loaded_scene_info(h, C.byref(info)))
+        d = info.desc
+
+        def arr(ptr, n, dtype):
+            if not n:
+                return np.zeros(0, dtype)
+            buf = (C.c_uint8 * (n * dtype.itemsize)).from_address(ptr)
+            return np.frombuffer(buf, dtype).copy()
+
+        verts = arr(d.vertices, d.vertex_count, N.VERTEX_DTYPE)
+        idx = arr(d.indices, 3 * d.triangle_count, np.dtype(np.uint32)).reshape(-1, 3)
+        geoms = arr(d.geometries, d.geometry_count, N.GEOMETRY_DTYPE)
+        mats = arr(d.materials, d.material_count, N.MATERIAL_DTYPE)
+        env = None
+        intensity = 1.0
+        if d.env:
+            e = d.env.contents
+            env = np.ctypeslib.as_array(e.texels, (e.height, e.width, 4)).copy()
+            intensity = float(e.intensity)
+        blas = inst = None
+        if d.instance_count:
+            blas = arr(d.blas_ranges, d.blas_count, N.BLAS_DTYPE)
+            inst = arr(d.instances, d.instance_count, N.INSTANCE_DTYPE)
+        warnings = [lib.gbpt_loaded_scene_warning(h, i).decode()
+                    for i in range(info.warning_count)]
+        cam = N.Camera.from_buffer_copy(info.camera)
+        sc = SceneData(verts, idx, geoms, mats, env, env_intensity=intensity, blas_ranges=blas,
+                       instances=inst)
+        return sc, cam, (int(info.width), int(info.height)), warnings
+    finally:
+        lib.gbpt_loaded_scene_free(h)
+
+
 def workload_scene(name: str, seed: int = BASE_SEED, **overrides) -> SceneData:
     w = dict(WORKLOADS[name], **overrides)
     if w["scene"] == "cornell":

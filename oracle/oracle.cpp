@@ -260,6 +260,47 @@ inline bool intersect(const RayPre<R>& p, const float* tv, uint32_t flags, R tmi
     return true;
 }
 
+// ---- alpha test of non-opaque geometry (material-system.slang:28-38, scene.slang:500-519) -------
+// The material's alpha texture, bilinear with repeat addressing at level 0, at the candidate's
+// interpolated uv; alpha below 0.5 (merian_alpha_test_threshold) discards the candidate. In the
+// FP32 build every operation rounds once in the kernels' order, so decisions match bit for bit.
+template <class R> inline R texture_alpha(const Scene& s, uint32_t t, R u, R v) {
+    const uint32_t* info = &s.tex_info[4 * t];
+    const int w = (int)info[1], h = (int)info[2];
+    if (!(std::fabs(u) < R(65536))) u = R(0); // half uvs: only NaN / inf are out of range
+    if (!(std::fabs(v) < R(65536))) v = R(0);
+    const R x = u * (R)w - R(0.5), y = v * (R)h - R(0.5);
+    const R fx = std::floor(x), fy = std::floor(y);
+    const R a = x - fx, b = y - fy;
+    const int ix = (int)fx, iy = (int)fy;
+    auto wrap = [](int i, int n) { return ((i % n) + n) % n; };
+    const int x0 = wrap(ix, w), x1 = wrap(ix + 1, w), y0 = wrap(iy, h), y1 = wrap(iy + 1, h);
+    auto alpha = [&](int xx, int yy) {
+        return (R)s.tex[4 * ((size_t)info[0] + (size_t)yy * w + xx) + 3] * R(1.0f / 255.0f);
+    };
+    const R ia = R(1) - a, ib = R(1) - b;
+    const R top = alpha(x0, y0) * ia + alpha(x1, y0) * a;
+    const R bot = alpha(x0, y1) * ia + alpha(x1, y1) * a;
+    return top * ib + bot * b;
+}
+
+template <class R> inline bool alpha_discard(const Scene& s, uint32_t g, uint32_t prim, R bu, R bv) {
+    const gbpt_geometry& geo = s.geoms[g];
+    const gbpt_material& m = s.mats[geo.material_id];
+    if (m.alpha_texture < 0 || (size_t)m.alpha_texture >= s.tex_info.size() / 4) return false;
+    const uint32_t tri = geo.first_triangle + prim;
+    R ux[3], uy[3];
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t uv = s.verts[geo.first_vertex + s.idx[3 * tri + k]].uv;
+        ux[k] = (R)half_to_float(uv & 0xffffu);
+        uy[k] = (R)half_to_float(uv >> 16);
+    }
+    const R b0 = (R(1) - bu) - bv;
+    const R u = (b0 * ux[0] + bu * ux[1]) + bv * ux[2];
+    const R v = (b0 * uy[0] + bu * uy[1]) + bv * uy[2];
+    return texture_alpha<R>(s, (uint32_t)m.alpha_texture, u, v) < R(0.5);
+}
+
 // Closest (or any) hit of r against one triangle set, updating best / tbest; returns true when an
 // any-hit query found its hit. Ties at equal t go to the smallest (geometry, primitive, instance).
 template <class R>
@@ -308,6 +349,8 @@ static bool trace_set(const Scene& s, const TriSet& ts, const Ray<R>& r, uint32_
                 const uint32_t prim = ts.tprim[tri];
                 if (!best.valid || t < tbest || g < best.geom ||
                     (g == best.geom && (prim < best.prim || (prim == best.prim && inst < best.inst)))) {
+                    if ((geo.flags & GBPT_MESH_ALPHA_TEST) && alpha_discard<R>(s, g, prim, u, v))
+                        continue;
                     tbest = t;
                     best.t = (double)t;
                     best.u = (float)u;
