@@ -408,6 +408,13 @@ def run_batch_mix(args):
     for i, (sid, cam, p) in enumerate(jobs):
         creqs[i] = ctx.request(sid, cam, p, out_device=out_batch[i].data_ptr())
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    tuning = None
+    if not args.no_autotune:
+        # one schedule for both arms, tuned on the batch's largest whole-frame request
+        k = max(range(n), key=lambda i: reqs[i].width * reqs[i].height * reqs[i].spp)
+        t, cand = ctx.autotune(*jobs[k])
+        tuning = {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials,
+                  "tuned_on_request": k, "candidates_ms": [round(m, 2) for m in cand]}
 
     def plain():
         for (sid, cam, p), o in zip(jobs, out_plain):
@@ -460,7 +467,8 @@ def run_batch_mix(args):
                    "resolutions": "256^2 / 512^2 / 1024^2", "spp": "uniform 1..64",
                    "estimator": "NEE + RR from 3; path length 5 (Cornell) / 8 (soup)",
                    "scene_setup_s": round(setup_s, 1),
-                   "l2": "flushed between timed steps (256 MiB write)"},
+                   "l2": "flushed between timed steps (256 MiB write)",
+                   "tuning": tuning},
     }
     print(json.dumps(line), flush=True)
     ctx.close()
@@ -491,6 +499,13 @@ def run_instanced(args):
     acc = torch.zeros((n, 4), device="cuda")
     hist = torch.zeros(n, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    tuning = None
+    if not args.no_autotune:
+        p0, _ = S.render_params(W_, H_, spp, L, nee=True, rr_depth=3, frame=999_999)
+        t, cand = ctx.autotune(sid, cam, p0)
+        tuning = {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials,
+                  "candidates_ms": [round(m, 2) for m in cand]}
 
     def step(base):
         for f in range(frames):
@@ -532,7 +547,7 @@ def run_instanced(args):
                    "spp": spp * frames, "frames": frames, "max_path_length": L,
                    "nee": True, "rr_depth": 3, "bvh_nodes": st["nodes"], "bvh_depth": st["depth"],
                    "scene_setup_s": round(setup_s, 1),
-                   "l2": "flushed between timed steps (256 MiB write)"},
+                   "l2": "flushed between timed steps (256 MiB write)", "tuning": tuning},
     }
     print(json.dumps(line), flush=True)
     ctx.close()
@@ -569,6 +584,15 @@ def run_served(args):
     def job(r, sid):
         kind = "soup" if r.upload else specs[r.scene].kind
         return sid, WL.camera(kind, r.width, r.height), WL.params(kind, r)
+
+    tuning = None
+    if not args.no_autotune:
+        # one schedule for the server and the serial queue, tuned on the largest request
+        _, reqs0 = WL.served_stream(S.BASE_SEED, n_scenes, args.requests, rates[0])
+        big = max((r for r in reqs0 if not r.upload), key=lambda r: r.width * r.height * r.spp)
+        t, cand = ctx.autotune(*job(big, sids[big.scene]))
+        tuning = {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials,
+                  "candidates_ms": [round(m, 2) for m in cand]}
 
     with ClockSampler(0) as clk:
         for rate in rates:
@@ -636,7 +660,7 @@ def run_served(args):
                    "uploads": "5 % of requests bring a new 100k-triangle soup (BVH build + "
                               "upload inside the request's latency)",
                    "estimator": "NEE + RR from 3; path length 5 (Cornell) / 8 (soup)",
-                   "scene_setup_s": round(setup_s, 1)},
+                   "scene_setup_s": round(setup_s, 1), "tuning": tuning},
     }
     print(json.dumps(line), flush=True)
     ctx.close()

@@ -341,7 +341,8 @@ GBPT_API int gbpt_autotune(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam
  * others run joins the next tick). Scenes stay resident; a scene used by a queued or running
  * request cannot be destroyed (GBPT_ERR_BUSY). */
 typedef struct gbpt_server_config {
-    uint64_t wave_paths;  /* paths per tick; 0 = 8 Mi (at most 2^24) */
+    uint64_t wave_paths;  /* paths per tick (at most 2^24); 0 = the context's tuning, else 8 Mi.
+                             The tuning's material-sort override, as at start, also applies */
     uint64_t arena_bytes; /* device arena for host-output staging and pixel lists;
                              0 = a quarter of the free HBM, at most 16 GiB */
     int32_t use_graphs;   /* replay ticks from captured CUDA graphs */
@@ -410,6 +411,11 @@ GBPT_API int gbpt_image_write_pfm(const char* path, const float* texels, uint32_
                                   uint32_t height, uint32_t channels);
 GBPT_API int gbpt_image_read_pfm(const char* path, float* texels, uint32_t channels,
                                  uint32_t* width, uint32_t* height);
+/* PNG to RGBA8 (the loaders' image textures): grey, RGB, palette, grey+alpha and RGBA, 8 and 16
+ * bits (16-bit samples keep their high byte), not interlaced; top row first. rgba = NULL returns
+ * the size only. Host only. */
+GBPT_API int gbpt_image_read_png(const char* path, uint8_t* rgba, uint32_t* width,
+                                 uint32_t* height);
 
 /* ---- traversal queries (the GBuffer node's primary hit, and raw ray queries) ---------------
  * gbpt_trace_primary: the hit merian's GBuffer (Raytraced) node stores for each pixel
@@ -508,6 +514,13 @@ typedef struct gbpt_loaded_info {
 } gbpt_loaded_info;
 
 GBPT_API int gbpt_load_pbrt(const char* path, gbpt_loaded_scene** out);
+/* glTF 2.0 (.gltf with external or data-URI buffers, .glb) the way merian's GLTFScene reads it:
+ * each mesh a BLAS, each node holding one a TLAS instance; triangle primitives with POSITION,
+ * NORMAL, TEXCOORD_0, TANGENT; metallic-roughness materials mapped onto the OpenPBR record (base
+ * colour factor x sRGB PNG texture, metallic, alpha = roughness^2, emissive x strength, ior,
+ * transmission); non-OPAQUE alphaMode alpha-tested against the base colour texture; doubleSided
+ * or transmissive -> two-sided; the first perspective camera. */
+GBPT_API int gbpt_load_gltf(const char* path, gbpt_loaded_scene** out);
 GBPT_API int gbpt_loaded_scene_info(const gbpt_loaded_scene* scene, gbpt_loaded_info* info);
 /* Warning i (0 <= i < warning_count) of the load, or NULL. */
 GBPT_API const char* gbpt_loaded_scene_warning(const gbpt_loaded_scene* scene, uint32_t i);

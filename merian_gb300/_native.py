@@ -218,6 +218,9 @@ EXPORTS = [
     ("gbpt_gen_blob", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("gbpt_gen_noise_texture", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p]),
     ("gbpt_load_pbrt", C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    ("gbpt_load_gltf", C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    ("gbpt_image_read_png", C.c_int, [C.c_char_p, C.c_void_p, C.POINTER(C.c_uint32),
+                                      C.POINTER(C.c_uint32)]),
     ("gbpt_loaded_scene_info", C.c_int, [C.c_void_p, C.POINTER(LoadedInfo)]),
     ("gbpt_loaded_scene_warning", C.c_char_p, [C.c_void_p, C.c_uint32]),
     ("gbpt_loaded_scene_free", None, [C.c_void_p]),

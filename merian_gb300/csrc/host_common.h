@@ -160,6 +160,12 @@ inline void sincos(double x, double& s, double& c) {
 
 void set_error(const std::string& msg);
 
+// PNG to RGBA8, top row first (png.cpp).
+bool decode_png(const uint8_t* data, size_t size, std::vector<uint8_t>& rgba, uint32_t& width,
+                uint32_t& height, std::string& err);
+bool read_png_file(const std::string& path, std::vector<uint8_t>& rgba, uint32_t& width,
+                   uint32_t& height, std::string& err);
+
 // ---- CWBVH (compressed 8-wide BVH, Ylitie/Karras/Laine HPG 2017 layout) -------------------
 // Node = 5 x 16 bytes:
 //   w0: p.x p.y p.z (float), e.x | e.y<<8 | e.z<<16 | imask<<24

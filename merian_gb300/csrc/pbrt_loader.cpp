@@ -21,6 +21,7 @@
 // skipped with a warning, as the reference does.
 #include "gbpt.h"
 #include "host_common.h"
+#include "loaded_scene.h"
 
 #include <algorithm>
 #include <cctype>
@@ -231,22 +232,6 @@ struct State {
 
 } // namespace
 } // namespace gbpt
-
-// The loaded scene: host arrays a gbpt_scene_desc points into.
-struct gbpt_loaded_scene {
-    std::vector<gbpt_packed_vertex> vertices;
-    std::vector<uint32_t> indices;
-    std::vector<gbpt_geometry> geometries;
-    std::vector<gbpt_material> materials;
-    std::vector<gbpt_blas_range> blas;
-    std::vector<gbpt_instance> instances;
-    std::vector<float> env_texels;
-    gbpt_env_map env{};
-    bool has_env = false;
-    gbpt_camera camera{};
-    uint32_t width = 1280, height = 720;
-    std::vector<std::string> warnings;
-};
 
 namespace gbpt {
 namespace {
@@ -1349,6 +1334,8 @@ GBPT_API int gbpt_loaded_scene_info(const gbpt_loaded_scene* s, gbpt_loaded_info
     d.blas_count = (uint32_t)s->blas.size();
     d.instances = s->instances.empty() ? nullptr : s->instances.data();
     d.instance_count = (uint32_t)s->instances.size();
+    d.textures = s->textures.empty() ? nullptr : s->textures.data();
+    d.texture_count = (uint32_t)s->textures.size();
     info->camera = s->camera;
     info->width = s->width;
     info->height = s->height;

@@ -153,7 +153,7 @@ struct TickEngine {
     const void* graph_tables = nullptr;
     std::vector<unsigned char> stage;
     std::vector<const SceneGPU*> scene_ptrs;
-    int grids[4] = {0, 0, 0, 0};
+    int grids[7] = {0, 0, 0, 0, 0, 0, 0}; // launch grids, computed at the first tick
     void release(); // destroys the graphs
 };
 

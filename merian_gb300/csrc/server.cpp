@@ -103,6 +103,7 @@ struct Server {
     cudaStream_t stream = nullptr, copy_stream = nullptr;
     Work work;
     TickEngine engine;
+    int sort_override = -1; // the context tuning's material-sort override at start
     unsigned char* arena = nullptr;
     uint64_t arena_bytes = 0;
     ArenaAlloc alloc;
@@ -225,6 +226,7 @@ void Server::run() {
             r->item.scene = r->scene;
             r->item.camera = r->req.camera;
             r->item.params = r->req.params;
+            if (sort_override >= 0) r->item.params.sort_materials = sort_override;
             r->item.pixel_count = r->n_pix;
             if (r->req.out_host) {
                 r->d_out = (float4*)base;
@@ -415,7 +417,11 @@ GBPT_API int gbpt_server_start(gbpt_ctx* ctx, const gbpt_server_config* cfg) {
     }
     s->engine.work = &s->work;
     s->engine.stream = s->stream;
-    s->engine.wave = s->cfg.wave_paths ? s->cfg.wave_paths : kWavePaths;
+    // unset: the context's tuning (gbpt_set_tuning / gbpt_autotune), else the default
+    s->engine.wave = s->cfg.wave_paths
+                         ? s->cfg.wave_paths
+                         : (ctx->tuning.wave_paths ? ctx->tuning.wave_paths : kWavePaths);
+    s->sort_override = ctx->tuning.sort_materials;
     s->engine.use_graphs = s->cfg.use_graphs != 0;
     if ((rc = work_reserve(s->work, s->engine.wave, s->engine.wave)) != GBPT_OK) {
         set_error("gbpt_server_start: work buffer allocation failed");

@@ -34,7 +34,10 @@ static_assert(kWavePaths <= kMaxWavePaths, "path ids must fit the packed queue e
 
 // resident 128-thread blocks per SM the shading kernels are register-budgeted for
 // (65536 / (5 * 128) = 102 registers per thread)
-constexpr int kShadeBlocksPerSM = 5;
+#ifndef GBPT_SHADE_BLOCKS_PER_SM
+#define GBPT_SHADE_BLOCKS_PER_SM 5
+#endif
+constexpr int kShadeBlocksPerSM = GBPT_SHADE_BLOCKS_PER_SM;
 
 constexpr uint32_t kReqEmission = 1u, kReqNee = 2u, kReqDemodulate = 4u;
 
@@ -674,19 +677,27 @@ struct TickPlan {
     bool alpha;     // some chunk's scene has alpha-tested geometry: the alpha-test variants
 };
 
+// Grid-stride kernels get exactly the blocks that are resident at once: every block strides over
+// the same share of the work, so a second partial wave of blocks would only add a tail.
 struct Grids {
-    int grid;    // grid-stride shading kernels
+    int grid;    // grid-stride kernels without a register budget (finalize, material sort)
     int trace;   // persistent traversal: the blocks resident at once
     int trace_c;
     int shadow;
+    int primary; // k_primary, k_shade_primary, k_shade: their resident blocks
+    int shade_p;
+    int shade;
 };
 Grids launch_grids() {
     Grids g;
     g.grid = num_sms() * 8;
-    // the two-level variants have the same launch bounds, hence the same residency
+    // the two-level and alpha variants have the same launch bounds, hence the same residency
     g.trace = persistent_grid(k_trace<false, false, false>);
     g.trace_c = persistent_grid(k_trace<true, false, false>);
     g.shadow = persistent_grid(k_shadow<false, false>);
+    g.primary = persistent_grid(k_primary);
+    g.shade_p = persistent_grid(k_shade_primary);
+    g.shade = persistent_grid(k_shade);
     return g;
 }
 
@@ -730,11 +741,11 @@ uint64_t enqueue_tick(const TickArgs& ta, const TickPlan& tp, const Grids& g, cu
     const uint64_t paths = fixed_grid ? ~0ull >> 8 : tp.n_paths;
     uint64_t nl = 0;
     cudaMemsetAsync(ctr, 0, 3 * sizeof(uint32_t), st);
-    const int pgrid = (int)std::min<uint64_t>((pix + 127) / 128, (uint64_t)g.grid);
+    const int pgrid = (int)std::min<uint64_t>((pix + 127) / 128, (uint64_t)g.primary);
     int ev = prof->begin(st, 3);
     k_primary<<<pgrid, 128, 0, st>>>(ta);
     prof->end(st, ev);
-    const int sgrid = (int)std::min<uint64_t>((paths + 127) / 128, (uint64_t)g.grid);
+    const int sgrid = (int)std::min<uint64_t>((paths + 127) / 128, (uint64_t)g.shade_p);
     ev = prof->begin(st, 1);
     k_shade_primary<<<sgrid, 128, 0, st>>>(ta);
     prof->end(st, ev);
@@ -766,7 +777,7 @@ uint64_t enqueue_tick(const TickArgs& ta, const TickPlan& tp, const Grids& g, cu
         }
         cudaMemsetAsync(ctr + qo, 0, sizeof(uint32_t), st);
         ev = prof->begin(st, 1);
-        k_shade<<<g.grid, 128, 0, st>>>(ta, (int)k, qi, qo, perm);
+        k_shade<<<g.shade, 128, 0, st>>>(ta, (int)k, qi, qo, perm);
         prof->end(st, ev);
         nl += 2;
         if (nee && k < L) {
@@ -907,12 +918,11 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
     ta.w = w;
     if (e.grids[0] == 0) {
         const Grids g = launch_grids();
-        e.grids[0] = g.grid;
-        e.grids[1] = g.trace;
-        e.grids[2] = g.trace_c;
-        e.grids[3] = g.shadow;
+        static_assert(sizeof(Grids) == sizeof(e.grids), "grid cache");
+        std::memcpy(e.grids, &g, sizeof(g));
     }
-    const Grids grids{e.grids[0], e.grids[1], e.grids[2], e.grids[3]};
+    Grids grids;
+    std::memcpy(&grids, e.grids, sizeof(grids));
     uint64_t nl = 0;
     if (graph) {
         if (e.graph_work != (const void*)w.thr || e.graph_tables != w.tables) {

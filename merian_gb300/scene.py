@@ -193,9 +193,18 @@ WORKLOADS = {
 def load_pbrt(path: str):
     """A pbrt-v4 scene file through gbpt_load_pbrt: (SceneData with its own copies of the arrays,
     the file's camera, (width, height), warnings)."""
+    return _load_file("gbpt_load_pbrt", path)
+
+
+def load_gltf(path: str):
+    """A glTF 2.0 file (.gltf / .glb) through gbpt_load_gltf; returns like load_pbrt."""
+    return _load_file("gbpt_load_gltf", path)
+
+
+def _load_file(entry: str, path: str):
     lib = N.load()
     h = C.c_void_p()
-    N.check(lib.gbpt_load_pbrt(str(path).encode(), C.byref(h)))
+    N.check(getattr(lib, entry)(str(path).encode(), C.byref(h)))
     try:
         info = N.LoadedInfo()
         N.check(lib.gbpt_loaded_scene_info(h, C.byref(info)))
@@ -223,9 +232,14 @@ def load_pbrt(path: str):
             inst = arr(d.instances, d.instance_count, N.INSTANCE_DTYPE)
         warnings = [lib.gbpt_loaded_scene_warning(h, i).decode()
                     for i in range(info.warning_count)]
+        textures = []
+        for t in range(d.texture_count):
+            tx = d.textures[t]
+            px = np.ctypeslib.as_array(tx.texels, (tx.height, tx.width, 4)).copy()
+            textures.append((px, bool(tx.srgb)))
         cam = N.Camera.from_buffer_copy(info.camera)
         sc = SceneData(verts, idx, geoms, mats, env, env_intensity=intensity, blas_ranges=blas,
-                       instances=inst)
+                       instances=inst, textures=textures)
         return sc, cam, (int(info.width), int(info.height)), warnings
     finally:
         lib.gbpt_loaded_scene_free(h)
