@@ -236,9 +236,16 @@ struct State {
 namespace gbpt {
 namespace {
 
+struct TextureDesc {
+    std::string cls;
+    Params params;
+    std::string dir;
+};
+
 class Parser {
   public:
     std::vector<MaterialDesc> materials;
+    std::map<std::string, TextureDesc> textures;
     std::map<std::string, int> named_materials;
     std::vector<ShapeDesc> shapes;
     std::vector<ObjectDesc> objects;
@@ -512,7 +519,7 @@ class Parser {
             if (!need_string(t, i, s) || !need_string(t, i, type) || !need_string(t, i, cls) ||
                 !params(t, i, p))
                 return false;
-            warn("texture_" + cls, "texture class '" + cls + "' is not supported (factor used)");
+            textures[s] = {cls, p, dir};
         } else if (d == "AreaLightSource") {
             if (!need_string(t, i, s) || !params(t, i, p)) return false;
             if (s != "diffuse") warn("area_" + s, "area light '" + s + "' unsupported");
@@ -939,7 +946,50 @@ bool named_metal(const std::string& s, float out[3]) {
 class Converter {
   public:
     Parser& ps;
-    explicit Converter(Parser& p) : ps(p) {}
+    gbpt_loaded_scene& L;
+    std::map<std::string, std::pair<int, bool>> tex_cache; // texture name -> (index, has alpha)
+    Converter(Parser& p, gbpt_loaded_scene& l) : ps(p), L(l) {}
+
+    // An "imagemap" texture (PNG) as an RGBA8 texture of the scene: (index or -1, whether any
+    // texel is not opaque); "scale" multiplies the factor.
+    std::pair<int, bool> image_texture(const std::string& name, float& scale) {
+        auto it = ps.textures.find(name);
+        if (it == ps.textures.end()) {
+            ps.warn("tex_" + name, "unknown texture '" + name + "'");
+            return {-1, false};
+        }
+        const TextureDesc& td = it->second;
+        scale = (float)td.params.num("scale", 1.0);
+        if (td.cls != "imagemap") {
+            ps.warn("texcls_" + td.cls, "texture class '" + td.cls + "' is not supported");
+            return {-1, false};
+        }
+        auto c = tex_cache.find(name);
+        if (c != tex_cache.end()) return c->second;
+        const std::string fn = td.params.str("filename", "");
+        const std::string full = (!fn.empty() && fn[0] == '/') ? fn : td.dir + "/" + fn;
+        std::vector<uint8_t> rgba;
+        uint32_t w = 0, h = 0;
+        std::string err;
+        std::pair<int, bool> r{-1, false};
+        if (fn.size() < 4 || fn.compare(fn.size() - 4, 4, ".png") != 0) {
+            ps.warn("img_" + fn, "image '" + fn + "' is not a PNG: not loaded");
+        } else if (!read_png_file(full, rgba, w, h, err)) {
+            ps.warn("img_" + fn, "image '" + fn + "' not loaded: " + err);
+        } else {
+            bool alpha = false;
+            for (size_t k = 3; k < rgba.size(); k += 4) alpha |= rgba[k] != 255;
+            gbpt_texture tx{};
+            tx.width = w;
+            tx.height = h;
+            tx.srgb = td.params.str("encoding", "sRGB") == "linear" ? 0u : 1u;
+            L.texels.push_back(std::move(rgba));
+            L.textures.push_back(tx);
+            r = {(int)L.textures.size() - 1, alpha};
+        }
+        tex_cache[name] = r;
+        return r;
+    }
 
     void roughness(const Params& p, const std::string& prefix, float alpha[2]) {
         const bool remap = p.flag("remaproughness", true);
@@ -957,16 +1007,43 @@ class Converter {
         }
     }
 
-    void color(const Params& p, const std::string& name, const float def[3], float out[3]) {
+    // A colour parameter: its value, or a texture (tex >= 0) times its scale.
+    void color(const Params& p, const std::string& name, const float def[3], float out[3],
+               int* tex = nullptr, bool* has_alpha = nullptr) {
         std::memcpy(out, def, 12);
+        if (tex) *tex = -1;
+        if (has_alpha) *has_alpha = false;
         const Param* c = p.find(name);
         if (!c) return;
         if (c->type == "texture") {
-            ps.warn("color_tex", "'" + name + "' textures are not supported (default used)");
+            if (c->strs.empty()) return;
+            float scale = 1.0f;
+            const std::pair<int, bool> t = image_texture(c->strs[0], scale);
+            if (t.first >= 0 && tex) {
+                out[0] = out[1] = out[2] = scale;
+                *tex = t.first;
+                if (has_alpha) *has_alpha = t.second;
+            } else if (auto it = ps.textures.find(c->strs[0]);
+                       it != ps.textures.end() && it->second.cls == "constant") {
+                if (const Param* v = it->second.params.find("value")) ps_rgb(*v, out);
+            }
             return;
         }
         float v[3];
         if (ps_rgb(*c, v)) std::memcpy(out, v, 12);
+    }
+
+    // reflectance with its texture: the base colour texture, and (textures with alpha) the alpha
+    // test and two-sidedness merian gives such materials (pbrt_scene.cpp:380-412)
+    void reflectance(const Params& p, const float def[3], gbpt_material& m, uint32_t& flags) {
+        int tex = -1;
+        bool alpha = false;
+        color(p, "reflectance", def, m.base_color, &tex, &alpha);
+        m.base_color_texture = tex;
+        if (tex >= 0 && alpha) {
+            m.alpha_texture = tex;
+            flags |= GBPT_MESH_ALPHA_TEST | GBPT_MESH_TWO_SIDED;
+        }
     }
 
     bool ps_rgb(const Param& c, float v[3]) {
@@ -982,10 +1059,10 @@ class Converter {
         return false;
     }
 
-    // Returns the material and whether it needs two-sided geometry.
-    gbpt_material convert(int index, int depth, bool& two_sided) {
+    // Returns the material and the mesh flags it needs (two-sided, alpha-tested).
+    gbpt_material convert(int index, int depth, uint32_t& flags) {
         gbpt_material m = openpbr_default();
-        two_sided = false;
+        flags = 0;
         const float half[3] = {0.5f, 0.5f, 0.5f};
         if (index < 0 || depth > 4) {
             std::memcpy(m.base_color, half, 12); // pbrt's default: coated diffuse, reflectance 0.5
@@ -997,12 +1074,12 @@ class Converter {
         const std::string& type = md.type;
         if (type == "diffuse" || type == "diffusetransmission" || type == "subsurface" ||
             type == "hair" || type == "measured") {
-            color(p, "reflectance", half, m.base_color);
+            reflectance(p, half, m, flags);
             m.specular_weight = 0.0f;
             if (type != "diffuse")
                 ps.warn("mat_" + type, "material '" + type + "' approximated as diffuse");
         } else if (type == "coateddiffuse") {
-            color(p, "reflectance", half, m.base_color);
+            reflectance(p, half, m, flags);
             m.specular_ior = (float)p.num("eta", 1.5);
             roughness(p, "", m.specular_alpha);
         } else if (type == "conductor" || type == "coatedconductor") {
@@ -1010,7 +1087,7 @@ class Converter {
             m.metalness = 1.0f;
             const float copper[3] = {0.955f, 0.637f, 0.538f}, r09[3] = {0.9f, 0.9f, 0.9f};
             if (p.find("reflectance")) {
-                color(p, "reflectance", r09, m.base_color);
+                reflectance(p, r09, m, flags);
             } else {
                 std::memcpy(m.base_color, copper, 12);
                 const Param* eta = p.find(pre + "eta");
@@ -1043,7 +1120,7 @@ class Converter {
             m.specular_ior = eta;
             m.transmission_weight = 1.0f;
             roughness(p, "", m.specular_alpha);
-            two_sided = true;
+            flags |= GBPT_MESH_TWO_SIDED;
             if (type == "thindielectric")
                 ps.warn("mat_thin", "thindielectric approximated as solid dielectric");
         } else if (type == "mix") {
@@ -1052,7 +1129,7 @@ class Converter {
                 const double amount = p.num("amount", 0.5);
                 const std::string& chosen = mats->strs[amount >= 0.5 ? 1 : 0];
                 auto it = ps.named_materials.find(chosen);
-                if (it != ps.named_materials.end()) return convert(it->second, depth + 1, two_sided);
+                if (it != ps.named_materials.end()) return convert(it->second, depth + 1, flags);
                 ps.warn("mix_" + chosen, "mix references unknown material '" + chosen + "'");
             }
             std::memcpy(m.base_color, half, 12);
@@ -1126,22 +1203,22 @@ GBPT_API int gbpt_load_pbrt(const char* path, gbpt_loaded_scene** out) {
         return GBPT_ERR_INVALID;
     }
     auto L = std::make_unique<gbpt_loaded_scene>();
-    Converter conv(ps);
+    Converter conv(ps, *L);
     // material records per (material, emission), as merian caches them
-    std::map<std::tuple<int, float, float, float>, std::pair<uint32_t, bool>> cache;
-    auto material_for = [&](const ShapeDesc& sh, bool& two_sided) -> uint32_t {
+    std::map<std::tuple<int, float, float, float>, std::pair<uint32_t, uint32_t>> cache;
+    auto material_for = [&](const ShapeDesc& sh, uint32_t& mflags) -> uint32_t {
         const float* e = sh.has_light ? sh.light.radiance : nullptr;
         const auto key = std::make_tuple(sh.material, e ? e[0] : 0.f, e ? e[1] : 0.f, e ? e[2] : 0.f);
         auto it = cache.find(key);
         if (it != cache.end()) {
-            two_sided = it->second.second;
+            mflags = it->second.second;
             return it->second.first;
         }
-        gbpt_material m = conv.convert(sh.material, 0, two_sided);
+        gbpt_material m = conv.convert(sh.material, 0, mflags);
         if (e) std::memcpy(m.emission, e, 12);
         L->materials.push_back(m);
         const uint32_t id = (uint32_t)L->materials.size() - 1;
-        cache[key] = {id, two_sided};
+        cache[key] = {id, mflags};
         return id;
     };
     std::vector<int> object_use(ps.objects.size(), 0);
@@ -1177,9 +1254,10 @@ GBPT_API int gbpt_load_pbrt(const char* path, gbpt_loaded_scene** out) {
             ps.warn("shape_" + sh.type, "shape '" + sh.type + "' is unsupported, skipping");
             return true;
         }
-        bool two_sided_mat = false;
-        const uint32_t mid = material_for(sh, two_sided_mat);
-        uint32_t flags = 0;
+        uint32_t mflags = 0;
+        const uint32_t mid = material_for(sh, mflags);
+        const bool two_sided_mat = (mflags & GBPT_MESH_TWO_SIDED) != 0;
+        uint32_t flags = mflags & GBPT_MESH_ALPHA_TEST;
         const bool two_sided_emitter = sh.has_light && sh.light.twosided;
         if (two_sided_emitter && !two_sided_mat) {
             // a coincident reversed sheet; both stay back-face culled
@@ -1309,6 +1387,7 @@ GBPT_API int gbpt_load_pbrt(const char* path, gbpt_loaded_scene** out) {
         ps.warn("no_camera", "no camera in the file: a default camera looks at the scene box");
     }
     gbpt_camera_look_at(pos, tgt, up, fov_y, aspect, 0.01f, 1000.0f, &L->camera);
+    for (size_t i = 0; i < L->textures.size(); ++i) L->textures[i].texels = L->texels[i].data();
     L->warnings = ps.warnings;
     *out = L.release();
     return GBPT_OK;

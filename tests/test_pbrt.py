@@ -67,6 +67,17 @@ AttributeBegin
   Shape "disk" "float radius" 0.4
 AttributeEnd
 Include "extra.pbrt"
+Texture "leaves" "spectrum" "imagemap" "string filename" "leaf.png" "float scale" 0.8
+AttributeBegin
+  Material "diffuse" "texture reflectance" "leaves"
+  Translate 0 2 2
+  Shape "trianglemesh" "point3 P" [ -1 0 0  1 0 0  1 1 0  -1 1 0 ]
+      "point2 uv" [ 0 0  1 0  1 1  0 1 ] "integer indices" [ 0 1 2  0 2 3 ]
+AttributeEnd
+AttributeBegin
+  Material "coateddiffuse" "texture reflectance" "checks"
+  Shape "trianglemesh" "point3 P" [ 3 0 2  4 0 2  3 1 2 ]
+AttributeEnd
 ObjectBegin "tree"
   Material "conductor" "rgb reflectance" [ 0.9 0.8 0.7 ] "float uroughness" 0.09
       "float vroughness" 0.16 "bool remaproughness" false
@@ -136,6 +147,11 @@ def pbrt_dir(tmp_path_factory):
     (d / "extra.pbrt").write_text(EXTRA)
     (d / "mesh_ascii.ply").write_text(PLY_ASCII)
     binary_ply(d / "mesh_binary.ply")
+    from test_png import write_png
+    leaf = np.zeros((4, 4, 4), np.uint8)
+    leaf[..., 1] = 180
+    leaf[..., 3] = np.where(np.arange(16).reshape(4, 4) % 3 == 0, 0, 255)
+    write_png(d / "leaf.png", leaf.reshape(4, 16), 6, 8)
     return d
 
 
@@ -149,12 +165,13 @@ def test_pbrt_geometry_and_instances(native, pbrt_dir):
     sc, cam, (w, h), warnings = _load(pbrt_dir)
     assert (w, h) == (160, 90)
     g = sc.geometries
-    # world BLAS: light quad, floor, sphere, ascii ply, disk, measured triangle; then the object
+    # world BLAS: light quad, floor, sphere, ascii ply, disk, measured triangle, textured leaf,
+    # checkerboard triangle; then the object
     counts = list(g["triangle_count"])
-    assert counts == [2, 2, 64 * 32 * 2, 3, 128, 1, 4]
+    assert counts == [2, 2, 64 * 32 * 2, 3, 128, 1, 2, 1, 4]
     assert len(sc.blas_ranges) == 2 and len(sc.instances) == 3
-    assert list(sc.blas_ranges["first_geometry"]) == [0, 6]
-    assert list(sc.blas_ranges["geometry_count"]) == [6, 1]
+    assert list(sc.blas_ranges["first_geometry"]) == [0, 8]
+    assert list(sc.blas_ranges["geometry_count"]) == [8, 1]
     assert list(sc.instances["blas"]) == [0, 1, 1]
     m0 = sc.instances["object_to_world"][0].reshape(3, 4)
     assert np.array_equal(m0, np.eye(3, 4, dtype=np.float32))
@@ -177,7 +194,7 @@ def test_pbrt_geometry_and_instances(native, pbrt_dir):
     assert not g["flags"][1] & N.MESH_FLIP_FACING
     assert np.all(g["flags"] & N.MESH_TWO_SIDED)
     # object geometry stays in object space (relative to the CTM at ObjectBegin = identity)
-    tet = pos[g["first_vertex"][6]:g["first_vertex"][6] + 4]
+    tet = pos[g["first_vertex"][8]:g["first_vertex"][8] + 4]
     assert np.allclose(tet, [[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]])
     idx = sc.indices
     assert idx.max() < len(sc.vertices)
@@ -189,7 +206,7 @@ def test_pbrt_materials_camera_env(native, pbrt_dir):
     from merian_gb300 import _native as N
     sc, cam, (w, h), _ = _load(pbrt_dir)
     m = sc.materials[sc.geometries["material_id"]]
-    light, floor, sphere, ply, disk, meas, tree = m
+    light, floor, sphere, ply, disk, meas, leaf, checks, tree = m
     assert np.allclose(light["emission"], [12, 10.5, 9])
     assert light["model"] == N.MATERIAL_OPENPBR and np.allclose(light["base_color"], 0.5)
     assert np.allclose(light["specular_alpha"], 0.0)   # pbrt's default coated diffuse
@@ -202,7 +219,15 @@ def test_pbrt_materials_camera_env(native, pbrt_dir):
     assert meas["specular_weight"] == 0                 # approximated as diffuse
     assert np.allclose(tree["base_color"], [0.9, 0.8, 0.7])
     assert np.allclose(tree["specular_alpha"], [0.09, 0.16])
-    assert np.all(m["base_color_texture"] == -1) and np.all(m["alpha_texture"] == -1)
+    # the imagemap texture: base colour x scale, alpha-tested and two-sided (it has alpha)
+    assert leaf["base_color_texture"] == 0 and leaf["alpha_texture"] == 0
+    assert np.allclose(leaf["base_color"], 0.8)
+    assert sc.geometries["flags"][6] & N.MESH_ALPHA_TEST
+    assert len(sc.textures) == 1 and sc.textures[0][1] is True
+    assert sc.textures[0][0].shape == (4, 4, 4) and sc.textures[0][0][0, 0, 3] == 0
+    assert checks["base_color_texture"] == -1      # checkerboard: unsupported, factor kept
+    others = np.delete(m, 6)
+    assert np.all(others["base_color_texture"] == -1) and np.all(others["alpha_texture"] == -1)
     # environment: constant L x scale
     assert sc.env is not None and np.allclose(sc.env[..., :3], [0.2, 0.3, 0.4])
     assert sc.env_intensity == 2.0
