@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tuning", default=None,
+                    help="WAVE_PATHS,SORT: a fixed schedule instead of the autotuner's")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default schedule instead of gbpt_autotune's choice of tick "
                          "size and material sorting (made before the warm-up, untimed)")
@@ -56,6 +58,24 @@ def parse():
 def dist_info():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
             int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def rank_max(values, world):
+    """Each value's maximum over the ranks (host all_reduce over the process group): the timing
+    rule for N > 1. Identity for one rank."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def whole_job(world, units_per_rank, ms):
+    """Millions of units per second of the whole job: every rank's units over the slowest
+    rank's time (replicas with fixed work per rank: weak scaling)."""
+    return world * units_per_rank / (ms / 1e3) / 1e6
 
 
 def measured_peaks():
@@ -256,7 +276,11 @@ def run_gbpt(args):
 
     frame_base = 1_000_000 * rank
     tuning = None
-    if not args.no_autotune:
+    if args.tuning:
+        wave, sort = (int(x) for x in args.tuning.split(","))
+        ctx.set_tuning(wave, sort)
+        tuning = {"wave_paths": wave, "sort_materials": sort, "fixed": True}
+    elif not args.no_autotune:
         t, cand_ms = ctx.autotune(sid, cam, params(frame_base + 998))
         tuning = {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials,
                   "candidates_ms": [round(m, 2) for m in cand_ms]}
@@ -313,16 +337,14 @@ def run_gbpt(args):
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e = float(np.mean(e2e_ms))
 
+    ms, e2e = rank_max([ms, e2e], world)
     if world > 1:
         import torch.distributed as dist
-        t = torch.tensor([ms, e2e], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, e2e = float(t[0]), float(t[1])
         dist.barrier()
 
     samples_per_step = n_pix * w["spp"]
-    value = world * samples_per_step / (ms / 1e3) / 1e6
-    e2e_value = world * samples_per_step / (e2e / 1e3) / 1e6
+    value = whole_job(world, samples_per_step, ms)
+    e2e_value = whole_job(world, samples_per_step, e2e)
     peak, peak_kind = measured_peaks()
     achieved = (trace_rays * bytes_per_ray) / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else None
     tpr, tsrc = ncu_traffic_per_ray()

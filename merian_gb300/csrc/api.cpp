@@ -259,6 +259,7 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
     }
     // validate geometry ranges and gather world-space triangles
     BuildInput bi;
+    bi.split = true;
     uint64_t total_tris = 0;
     for (uint32_t g = 0; g < d->geometry_count; ++g) {
         const gbpt_geometry& geo = d->geometries[g];
@@ -331,6 +332,7 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
         std::vector<CwBvh> blas(d->blas_count);
         for (uint32_t b = 0; b < d->blas_count; ++b) {
             BuildInput in;
+            in.split = true;
             if ((rc = gather(d->blas_ranges[b].first_geometry, d->blas_ranges[b].geometry_count, in)))
                 return rc;
             if (in.prim.empty()) {

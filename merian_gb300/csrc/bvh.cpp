@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstring>
 #include <thread>
 
 namespace gbpt {
@@ -54,6 +55,14 @@ struct B2Node {
 #ifndef GBPT_BVH_TRAVERSE_COST
 #define GBPT_BVH_TRAVERSE_COST 0.5f
 #endif
+#ifndef GBPT_BVH_SPLIT_RATIO
+#define GBPT_BVH_SPLIT_RATIO 8.0
+#endif
+#ifndef GBPT_BVH_SPLIT_DEPTH
+#define GBPT_BVH_SPLIT_DEPTH 2
+#endif
+constexpr double kSplitRatio = GBPT_BVH_SPLIT_RATIO;
+constexpr int kSplitDepth = GBPT_BVH_SPLIT_DEPTH;
 constexpr int kBins = GBPT_BVH_BINS;
 constexpr float kCostTraverse = GBPT_BVH_TRAVERSE_COST; // relative to one triangle test
 constexpr uint32_t kMaxLeaf = 3;      // CWBVH leaf children hold up to three triangles
@@ -185,19 +194,104 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
         out.nodes.push_back(root);
         return true;
     }
-    std::vector<Box> pbox(n);
-    std::vector<float> cent(3 * n);
-    std::vector<uint32_t> idx(n);
+    // References: one per triangle, or several clipped pieces of a triangle whose bounding box is
+    // much larger than the triangle (early split clipping, Ernst and Greiner 2007): a piece is
+    // halved along its longest axis while its box area exceeds kSplitRatio x twice the triangle's
+    // area (scaled by 1/2 per halving), at most kSplitDepth times. Pieces keep the triangle's
+    // record, so a ray may test one triangle twice; the tie rule makes that harmless.
+    std::vector<Box> pbox;
+    std::vector<uint32_t> rprim;
+    pbox.reserve(n);
+    rprim.reserve(n);
     Box scene;
-    for (size_t i = 0; i < n; ++i) {
+    struct P3 {
+        float x[3];
+    };
+    struct Piece {
+        P3 poly[9];
+        int m;
         Box b;
-        b.grow(&in.v[9 * i + 0]);
-        b.grow(&in.v[9 * i + 3]);
-        b.grow(&in.v[9 * i + 6]);
-        pbox[i] = b;
-        for (int a = 0; a < 3; ++a) cent[3 * i + a] = 0.5f * (b.lo[a] + b.hi[a]);
-        idx[i] = (uint32_t)i;
+        int depth;
+    };
+    std::vector<Piece> pieces;
+    for (size_t i = 0; i < n; ++i) {
+        const float* t = &in.v[9 * i];
+        Box b;
+        b.grow(t);
+        b.grow(t + 3);
+        b.grow(t + 6);
         scene.grow(b);
+        double area = 0.0;
+        if (in.split) {
+            double e1[3], e2[3];
+            for (int a = 0; a < 3; ++a) {
+                e1[a] = (double)t[3 + a] - t[a];
+                e2[a] = (double)t[6 + a] - t[a];
+            }
+            const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                         cz = e1[0] * e2[1] - e1[1] * e2[0];
+            area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+        }
+        if (!(area > 0.0) || b.area() <= kSplitRatio * 2.0 * area) {
+            pbox.push_back(b);
+            rprim.push_back((uint32_t)i);
+            continue;
+        }
+        pieces.clear();
+        Piece p0;
+        for (int k = 0; k < 3; ++k) std::memcpy(p0.poly[k].x, t + 3 * k, 12);
+        p0.m = 3;
+        p0.b = b;
+        p0.depth = 0;
+        pieces.push_back(p0);
+        while (!pieces.empty()) {
+            const Piece it = pieces.back();
+            pieces.pop_back();
+            if (it.depth >= kSplitDepth ||
+                it.b.area() <= kSplitRatio * 2.0 * area * std::ldexp(1.0, -it.depth)) {
+                pbox.push_back(it.b);
+                rprim.push_back((uint32_t)i);
+                continue;
+            }
+            int ax = 0;
+            for (int a = 1; a < 3; ++a)
+                if (it.b.hi[a] - it.b.lo[a] > it.b.hi[ax] - it.b.lo[ax]) ax = a;
+            const float mid = 0.5f * (it.b.lo[ax] + it.b.hi[ax]);
+            for (int side = 0; side < 2; ++side) {
+                Piece c;
+                c.m = 0;
+                c.depth = it.depth + 1;
+                for (int k = 0; k < it.m; ++k) {
+                    const P3& A = it.poly[k];
+                    const P3& B = it.poly[(k + 1) % it.m];
+                    const bool ina = side == 0 ? A.x[ax] <= mid : A.x[ax] >= mid;
+                    const bool inb = side == 0 ? B.x[ax] <= mid : B.x[ax] >= mid;
+                    if (ina) c.poly[c.m++] = A;
+                    if (ina != inb) {
+                        const float tt = (mid - A.x[ax]) / (B.x[ax] - A.x[ax]);
+                        P3 q;
+                        for (int a = 0; a < 3; ++a) q.x[a] = A.x[a] + tt * (B.x[a] - A.x[a]);
+                        q.x[ax] = mid;
+                        c.poly[c.m++] = q;
+                    }
+                }
+                if (c.m < 3) continue;
+                for (int k = 0; k < c.m; ++k) c.b.grow(c.poly[k].x);
+                // within the parent box (rounding of the clip points)
+                for (int a = 0; a < 3; ++a) {
+                    c.b.lo[a] = std::max(c.b.lo[a], it.b.lo[a]);
+                    c.b.hi[a] = std::min(c.b.hi[a], it.b.hi[a]);
+                }
+                pieces.push_back(c);
+            }
+        }
+    }
+    const size_t nref = pbox.size();
+    std::vector<float> cent(3 * nref);
+    std::vector<uint32_t> idx(nref);
+    for (size_t i = 0; i < nref; ++i) {
+        for (int a = 0; a < 3; ++a) cent[3 * i + a] = 0.5f * (pbox[i].lo[a] + pbox[i].hi[a]);
+        idx[i] = (uint32_t)i;
     }
     for (int a = 0; a < 3; ++a) {
         out.lo[a] = scene.lo[a];
@@ -206,20 +300,20 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
 
     Builder bld(pbox, cent, idx);
     std::vector<B2Node>& b2 = bld.nodes;
-    b2.reserve(2 * n);
+    b2.reserve(2 * nref);
     b2.emplace_back();
     // Top levels serially until there are enough independent subtrees, then the subtrees in
     // parallel into private node arrays that are appended afterwards.
     {
         const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-        if (n < 200000 || hw == 1) {
-            bld.build_range(b2, 0, 0, (uint32_t)n);
+        if (nref < 200000 || hw == 1) {
+            bld.build_range(b2, 0, 0, (uint32_t)nref);
         } else {
             // split the root range into up to 2*hw pieces by a coarse serial build (depth-limited)
             struct Part {
                 uint32_t node, begin, end;
             };
-            std::vector<Part> parts{{0, 0, (uint32_t)n}};
+            std::vector<Part> parts{{0, 0, (uint32_t)nref}};
             // expand the largest part with one SAH split at a time
             while (parts.size() < 2 * hw) {
                 size_t bi = 0;
@@ -293,7 +387,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
         uint32_t b2node, cw, depth;
     };
     out.nodes.reserve(b2.size() / 4 + 1);
-    out.tris.reserve(n);
+    out.tris.reserve(nref);
     out.nodes.emplace_back();
     std::vector<Task> stack{{0, 0, 1}};
     auto is_inner = [&](uint32_t k) { return !b2[k].leaf && b2[k].count > kMaxLeaf; };
@@ -423,7 +517,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
                 const uint32_t off = (uint32_t)out.tris.size() - tri_base;
                 const uint32_t cnt = c.count;
                 for (uint32_t k = 0; k < cnt; ++k) {
-                    const uint32_t p = idx[c.first + k];
+                    const uint32_t p = rprim[idx[c.first + k]];
                     TriRecord tr{};
                     std::memcpy(tr.v0, &in.v[9 * p + 0], 12);
                     std::memcpy(tr.v1, &in.v[9 * p + 3], 12);

@@ -237,12 +237,7 @@ GBPT_DI float3 xform_vector(float4 r0, float4 r1, float4 r2, float3 v) {
 #endif
 constexpr int kRefillLanes = GBPT_REFILL_LANES;
 constexpr int kPostponeLanes = GBPT_POSTPONE_LANES;
-// Triangles a lane tests in one round before it postpones the rest of its group to take its next
-// node (lanes with long triangle groups would otherwise hold the warp's node step back).
-#ifndef GBPT_TRIS_PER_ITER
-#define GBPT_TRIS_PER_ITER 64
-#endif
-constexpr int kTrisPerIter = GBPT_TRIS_PER_ITER;
+
 
 struct TraceState {
     const uint4* nodes;  // the ray's scene (rays of one launch may belong to different scenes)
@@ -421,15 +416,12 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
         bool done_any = false;
         // only groups followed by node work are postponed (a group popped back is tested)
         const bool may_postpone = WARP && s.ngroup.y > 0x00FFFFFFu;
-        int tested = 0;
         while (s.tgroup.y != 0u) {
-            if (may_postpone && s.sp < kStackSize &&
-                (tested >= kTrisPerIter || __popc(__activemask()) < kPostponeLanes)) {
+            if (may_postpone && s.sp < kStackSize && __popc(__activemask()) < kPostponeLanes) {
                 st(s.sp++) = s.tgroup;
                 s.tgroup.y = 0u;
                 break;
             }
-            ++tested;
             const uint32_t b = __ffs(s.tgroup.y) - 1u;
             s.tgroup.y &= s.tgroup.y - 1u;
             const uint32_t ti = s.tgroup.x + b;

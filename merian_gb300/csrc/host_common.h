@@ -198,6 +198,9 @@ struct BuildInput {
     std::vector<uint32_t> prim;
     std::vector<uint32_t> geom;
     std::vector<uint32_t> flags; // instance mask (bits 0-7), two-sided (bit 8), flip (bit 9)
+    // split triangles whose bounding box is loose into clipped references (never for TLAS
+    // builds, whose "triangles" are instance boxes)
+    bool split = false;
 };
 
 struct CwBvh {
