@@ -81,7 +81,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False,
             # no FMA contraction on the host: scene generation and BVH quantisation give the
             # same bits on x86-64 and aarch64
             jobs.append([cxx, "-O3", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall",
-                         "-ffp-contract=off",
+                         "-ffp-contract=off", *[f"-D{d}" for d in defines],
                          "-I", str(INCLUDE), "-I", str(CSRC), "-I", str(cuda / "include"),
                          "-c", str(CSRC / src), "-o", str(obj)])
     if jobs:
