@@ -324,7 +324,14 @@ typedef struct gbpt_tuning {
     uint64_t wave_paths;    /* paths per tick: 0 = default (2^23), else in [1024, 2^24] */
     int32_t sort_materials; /* -1: as each request's params ask; 0 / 1: force off / on */
     int32_t use_graphs;     /* gbpt_render_batch replays ticks from CUDA graphs */
+    int32_t bvh_build;      /* scenes created after it: GBPT_BVH_* */
+    int32_t reserved;
 } gbpt_tuning;
+
+/* BVH build of gbpt_scene_create (the traversal finds the same hits in every case). */
+#define GBPT_BVH_SPLIT 0  /* default: loose triangles split into up to 16 clipped references */
+#define GBPT_BVH_FAST 1   /* one reference per triangle: fastest build, smallest tree */
+#define GBPT_BVH_MEDIUM 2 /* up to 8 references for very loose triangles only */
 
 GBPT_API int gbpt_set_tuning(gbpt_ctx* ctx, const gbpt_tuning* tuning);
 GBPT_API int gbpt_get_tuning(gbpt_ctx* ctx, gbpt_tuning* tuning);

@@ -98,6 +98,13 @@ void free_scene(SceneGPU& s) {
     s = SceneGPU{};
 }
 
+// The build input's reference splitting for a GBPT_BVH_* setting.
+void set_split(BuildInput& in, int32_t bvh_build) {
+    in.split = bvh_build != GBPT_BVH_FAST;
+    in.split_ratio = bvh_build == GBPT_BVH_MEDIUM ? 8.0 : 2.0;
+    in.split_depth = bvh_build == GBPT_BVH_MEDIUM ? 3 : 4;
+}
+
 // Reads and clears the kernels' error word; returns GBPT_ERR_DEVICE when it was set.
 int check_device_error(gbpt_ctx* ctx) {
     uint32_t flags[2] = {0, 0};
@@ -259,7 +266,7 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
     }
     // validate geometry ranges and gather world-space triangles
     BuildInput bi;
-    bi.split = true;
+    set_split(bi, ctx->tuning.bvh_build);
     uint64_t total_tris = 0;
     for (uint32_t g = 0; g < d->geometry_count; ++g) {
         const gbpt_geometry& geo = d->geometries[g];
@@ -332,7 +339,7 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
         std::vector<CwBvh> blas(d->blas_count);
         for (uint32_t b = 0; b < d->blas_count; ++b) {
             BuildInput in;
-            in.split = true;
+            set_split(in, ctx->tuning.bvh_build);
             if ((rc = gather(d->blas_ranges[b].first_geometry, d->blas_ranges[b].geometry_count, in)))
                 return rc;
             if (in.prim.empty()) {
@@ -953,12 +960,15 @@ GBPT_API int gbpt_set_graphs(gbpt_ctx* ctx, int enable) {
 
 static int check_tuning(const gbpt_tuning* t) {
     if (!t || t->wave_paths > (1ull << 24) || (t->wave_paths && t->wave_paths < 1024) ||
-        t->sort_materials < -1 || t->sort_materials > 1) {
-        set_error("tuning: wave_paths must be 0 or in [1024, 2^24], sort_materials in {-1, 0, 1}");
+        t->sort_materials < -1 || t->sort_materials > 1 || t->bvh_build < GBPT_BVH_SPLIT ||
+        t->bvh_build > GBPT_BVH_MEDIUM) {
+        set_error("tuning: wave_paths must be 0 or in [1024, 2^24], sort_materials in {-1, 0, 1}, "
+                  "bvh_build a GBPT_BVH_* value");
         return GBPT_ERR_INVALID;
     }
     return GBPT_OK;
 }
+
 
 GBPT_API int gbpt_set_tuning(gbpt_ctx* ctx, const gbpt_tuning* t) {
     int rc = check_ctx(ctx);
@@ -1047,6 +1057,7 @@ GBPT_API int gbpt_autotune(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam
     }
     if ((rc = check_device_error(ctx))) return rc;
     best.use_graphs = ctx->tuning.use_graphs;
+    best.bvh_build = ctx->tuning.bvh_build;
     ctx->tuning = best;
     ctx->batch.wave = best.wave_paths;
     ctx->batch.release();

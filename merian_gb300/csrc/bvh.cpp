@@ -55,14 +55,7 @@ struct B2Node {
 #ifndef GBPT_BVH_TRAVERSE_COST
 #define GBPT_BVH_TRAVERSE_COST 0.5f
 #endif
-#ifndef GBPT_BVH_SPLIT_RATIO
-#define GBPT_BVH_SPLIT_RATIO 8.0
-#endif
-#ifndef GBPT_BVH_SPLIT_DEPTH
-#define GBPT_BVH_SPLIT_DEPTH 2
-#endif
-constexpr double kSplitRatio = GBPT_BVH_SPLIT_RATIO;
-constexpr int kSplitDepth = GBPT_BVH_SPLIT_DEPTH;
+constexpr int kMaxSplitDepth = 6;
 constexpr int kBins = GBPT_BVH_BINS;
 constexpr float kCostTraverse = GBPT_BVH_TRAVERSE_COST; // relative to one triangle test
 constexpr uint32_t kMaxLeaf = 3;      // CWBVH leaf children hold up to three triangles
@@ -170,6 +163,20 @@ struct Builder {
     }
 };
 
+// A fixed-capacity vector for the collapse's per-node lists (no heap traffic per node).
+template <class T, int N> struct SmallVec {
+    T v[N];
+    size_t n = 0;
+    void push_back(const T& x) { v[n++] = x; }
+    size_t size() const { return n; }
+    T& operator[](size_t i) { return v[i]; }
+    const T& operator[](size_t i) const { return v[i]; }
+    T* begin() { return v; }
+    T* end() { return v + n; }
+    const T* begin() const { return v; }
+    const T* end() const { return v + n; }
+};
+
 // Smallest power-of-two scale with 255 * scale >= ext, as a biased exponent in [1, 254].
 int quant_exponent(double ext) {
     if (!(ext > 0.0)) return 1;
@@ -196,94 +203,124 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
     }
     // References: one per triangle, or several clipped pieces of a triangle whose bounding box is
     // much larger than the triangle (early split clipping, Ernst and Greiner 2007): a piece is
-    // halved along its longest axis while its box area exceeds kSplitRatio x twice the triangle's
-    // area (scaled by 1/2 per halving), at most kSplitDepth times. Pieces keep the triangle's
+    // halved along its longest axis while its box area exceeds split_ratio x twice the triangle's
+    // area (scaled by 1/2 per halving), at most split_depth times. Pieces keep the triangle's
     // record, so a ray may test one triangle twice; the tie rule makes that harmless.
-    std::vector<Box> pbox;
-    std::vector<uint32_t> rprim;
-    pbox.reserve(n);
-    rprim.reserve(n);
-    Box scene;
     struct P3 {
         float x[3];
     };
     struct Piece {
-        P3 poly[9];
+        P3 poly[9]; // a triangle clipped by at most kMaxSplitDepth planes: 3 + that many corners
         int m;
         Box b;
         int depth;
     };
-    std::vector<Piece> pieces;
-    for (size_t i = 0; i < n; ++i) {
-        const float* t = &in.v[9 * i];
-        Box b;
-        b.grow(t);
-        b.grow(t + 3);
-        b.grow(t + 6);
-        scene.grow(b);
-        double area = 0.0;
-        if (in.split) {
-            double e1[3], e2[3];
-            for (int a = 0; a < 3; ++a) {
-                e1[a] = (double)t[3 + a] - t[a];
-                e2[a] = (double)t[6 + a] - t[a];
+    static_assert(kMaxSplitDepth <= 6, "clipped pieces hold at most 9 corners");
+    const int split_depth = std::min(std::max(in.split_depth, 0), kMaxSplitDepth);
+    const double split_ratio = std::max(in.split_ratio, 1.0);
+    // references of triangles [begin, end), in triangle order
+    auto make_refs = [&](size_t begin, size_t end, std::vector<Box>& boxes,
+                         std::vector<uint32_t>& prims, Box& bounds) {
+        std::vector<Piece> pieces;
+        for (size_t i = begin; i < end; ++i) {
+            const float* t = &in.v[9 * i];
+            Box b;
+            b.grow(t);
+            b.grow(t + 3);
+            b.grow(t + 6);
+            bounds.grow(b);
+            double area = 0.0;
+            if (in.split) {
+                double e1[3], e2[3];
+                for (int a = 0; a < 3; ++a) {
+                    e1[a] = (double)t[3 + a] - t[a];
+                    e2[a] = (double)t[6 + a] - t[a];
+                }
+                const double cx = e1[1] * e2[2] - e1[2] * e2[1],
+                             cy = e1[2] * e2[0] - e1[0] * e2[2],
+                             cz = e1[0] * e2[1] - e1[1] * e2[0];
+                area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
             }
-            const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
-                         cz = e1[0] * e2[1] - e1[1] * e2[0];
-            area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
-        }
-        if (!(area > 0.0) || b.area() <= kSplitRatio * 2.0 * area) {
-            pbox.push_back(b);
-            rprim.push_back((uint32_t)i);
-            continue;
-        }
-        pieces.clear();
-        Piece p0;
-        for (int k = 0; k < 3; ++k) std::memcpy(p0.poly[k].x, t + 3 * k, 12);
-        p0.m = 3;
-        p0.b = b;
-        p0.depth = 0;
-        pieces.push_back(p0);
-        while (!pieces.empty()) {
-            const Piece it = pieces.back();
-            pieces.pop_back();
-            if (it.depth >= kSplitDepth ||
-                it.b.area() <= kSplitRatio * 2.0 * area * std::ldexp(1.0, -it.depth)) {
-                pbox.push_back(it.b);
-                rprim.push_back((uint32_t)i);
+            if (!(area > 0.0) || split_depth == 0 || b.area() <= split_ratio * 2.0 * area) {
+                boxes.push_back(b);
+                prims.push_back((uint32_t)i);
                 continue;
             }
-            int ax = 0;
-            for (int a = 1; a < 3; ++a)
-                if (it.b.hi[a] - it.b.lo[a] > it.b.hi[ax] - it.b.lo[ax]) ax = a;
-            const float mid = 0.5f * (it.b.lo[ax] + it.b.hi[ax]);
-            for (int side = 0; side < 2; ++side) {
-                Piece c;
-                c.m = 0;
-                c.depth = it.depth + 1;
-                for (int k = 0; k < it.m; ++k) {
-                    const P3& A = it.poly[k];
-                    const P3& B = it.poly[(k + 1) % it.m];
-                    const bool ina = side == 0 ? A.x[ax] <= mid : A.x[ax] >= mid;
-                    const bool inb = side == 0 ? B.x[ax] <= mid : B.x[ax] >= mid;
-                    if (ina) c.poly[c.m++] = A;
-                    if (ina != inb) {
-                        const float tt = (mid - A.x[ax]) / (B.x[ax] - A.x[ax]);
-                        P3 q;
-                        for (int a = 0; a < 3; ++a) q.x[a] = A.x[a] + tt * (B.x[a] - A.x[a]);
-                        q.x[ax] = mid;
-                        c.poly[c.m++] = q;
+            pieces.clear();
+            Piece p0;
+            for (int k = 0; k < 3; ++k) std::memcpy(p0.poly[k].x, t + 3 * k, 12);
+            p0.m = 3;
+            p0.b = b;
+            p0.depth = 0;
+            pieces.push_back(p0);
+            while (!pieces.empty()) {
+                const Piece it = pieces.back();
+                pieces.pop_back();
+                if (it.depth >= split_depth ||
+                    it.b.area() <= split_ratio * 2.0 * area * std::ldexp(1.0, -it.depth)) {
+                    boxes.push_back(it.b);
+                    prims.push_back((uint32_t)i);
+                    continue;
+                }
+                int ax = 0;
+                for (int a = 1; a < 3; ++a)
+                    if (it.b.hi[a] - it.b.lo[a] > it.b.hi[ax] - it.b.lo[ax]) ax = a;
+                const float mid = 0.5f * (it.b.lo[ax] + it.b.hi[ax]);
+                for (int side = 0; side < 2; ++side) {
+                    Piece c;
+                    c.m = 0;
+                    c.depth = it.depth + 1;
+                    for (int k = 0; k < it.m; ++k) {
+                        const P3& A = it.poly[k];
+                        const P3& B = it.poly[(k + 1) % it.m];
+                        const bool ina = side == 0 ? A.x[ax] <= mid : A.x[ax] >= mid;
+                        const bool inb = side == 0 ? B.x[ax] <= mid : B.x[ax] >= mid;
+                        if (ina) c.poly[c.m++] = A;
+                        if (ina != inb) {
+                            const float tt = (mid - A.x[ax]) / (B.x[ax] - A.x[ax]);
+                            P3 q;
+                            for (int a = 0; a < 3; ++a) q.x[a] = A.x[a] + tt * (B.x[a] - A.x[a]);
+                            q.x[ax] = mid;
+                            c.poly[c.m++] = q;
+                        }
                     }
+                    if (c.m < 3) continue;
+                    for (int k = 0; k < c.m; ++k) c.b.grow(c.poly[k].x);
+                    // within the parent box (rounding of the clip points)
+                    for (int a = 0; a < 3; ++a) {
+                        c.b.lo[a] = std::max(c.b.lo[a], it.b.lo[a]);
+                        c.b.hi[a] = std::min(c.b.hi[a], it.b.hi[a]);
+                    }
+                    pieces.push_back(c);
                 }
-                if (c.m < 3) continue;
-                for (int k = 0; k < c.m; ++k) c.b.grow(c.poly[k].x);
-                // within the parent box (rounding of the clip points)
-                for (int a = 0; a < 3; ++a) {
-                    c.b.lo[a] = std::max(c.b.lo[a], it.b.lo[a]);
-                    c.b.hi[a] = std::min(c.b.hi[a], it.b.hi[a]);
-                }
-                pieces.push_back(c);
             }
+        }
+    };
+    std::vector<Box> pbox;
+    std::vector<uint32_t> rprim;
+    Box scene;
+    {
+        // in parallel over contiguous triangle ranges, concatenated in order (deterministic)
+        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        const size_t parts = n < 100000 ? 1 : hw;
+        std::vector<std::vector<Box>> pb(parts);
+        std::vector<std::vector<uint32_t>> pp(parts);
+        std::vector<Box> bounds(parts);
+        std::vector<std::thread> threads;
+        for (size_t k = 0; k < parts; ++k) {
+            const size_t b = n * k / parts, e = n * (k + 1) / parts;
+            if (parts == 1) make_refs(b, e, pb[k], pp[k], bounds[k]);
+            else threads.emplace_back([&, b, e, k]() { make_refs(b, e, pb[k], pp[k], bounds[k]); });
+        }
+        for (auto& t : threads) t.join();
+        size_t total = 0;
+        for (size_t k = 0; k < parts; ++k) total += pb[k].size();
+        pbox.reserve(total);
+        rprim.reserve(total);
+        for (size_t k = 0; k < parts; ++k) {
+            pbox.insert(pbox.end(), pb[k].begin(), pb[k].end());
+            rprim.insert(rprim.end(), pp[k].begin(), pp[k].end());
+            scene.grow(bounds[k]);
         }
     }
     const size_t nref = pbox.size();
@@ -332,9 +369,12 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
                         if (cbox.hi[a] - cbox.lo[a] > cbox.hi[axis] - cbox.lo[axis]) axis = a;
                     // median split on the widest centroid axis keeps the parts balanced
                     const uint32_t mid = p.begin + (p.end - p.begin) / 2;
+                    // ties broken by reference index: a strict order keeps the selection
+                    // linear when many centroids coincide (pieces of one split triangle)
                     std::nth_element(idx.begin() + p.begin, idx.begin() + mid,
                                      idx.begin() + p.end, [&](uint32_t x, uint32_t y) {
-                                         return cent[3 * x + axis] < cent[3 * y + axis];
+                                         const float cx = cent[3 * x + axis], cy = cent[3 * y + axis];
+                                         return cx < cy || (cx == cy && x < y);
                                      });
                     b2[p.node].box = box;
                     b2[p.node].first = p.begin;
@@ -399,9 +439,10 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
             set_error("BVH deeper than the traversal stack (" + std::to_string(max_depth) + ")");
             return false;
         }
-        std::vector<uint32_t> ch;
+        SmallVec<uint32_t, 8> ch;
         if (is_inner(t.b2node)) {
-            ch = {b2[t.b2node].left, b2[t.b2node].right};
+            ch.push_back(b2[t.b2node].left);
+            ch.push_back(b2[t.b2node].right);
             while (ch.size() < 8) {
                 int best = -1;
                 float best_area = -1.0f;
@@ -433,7 +474,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
                 ch.push_back(b2[k].right);
             }
         } else {
-            ch = {t.b2node}; // the whole tree is one leaf
+            ch.push_back(t.b2node); // the whole tree is one leaf
         }
         // node box and centroid
         Box nbox;
@@ -446,11 +487,9 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
         const size_t m = ch.size();
         int slot_of[8];
         {
-            struct Cand {
-                float cost;
-                int child, slot;
-            };
-            std::vector<Cand> cands;
+            // greedy over (child, slot) pairs in ascending (cost, child, slot) order: m rounds
+            // of picking the cheapest pair whose child and slot are both free
+            float cost[8][8];
             for (size_t i = 0; i < m; ++i) {
                 float off[3];
                 for (int a = 0; a < 3; ++a)
@@ -458,20 +497,27 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
                 for (int s = 0; s < 8; ++s) {
                     float c = 0.0f;
                     for (int a = 0; a < 3; ++a) c += ((s >> a) & 1) ? -off[a] : off[a];
-                    cands.push_back({c, (int)i, s});
+                    cost[i][s] = c;
                 }
             }
-            std::sort(cands.begin(), cands.end(), [](const Cand& x, const Cand& y) {
-                if (x.cost != y.cost) return x.cost < y.cost;
-                if (x.child != y.child) return x.child < y.child;
-                return x.slot < y.slot;
-            });
             bool used_slot[8] = {};
             for (size_t i = 0; i < m; ++i) slot_of[i] = -1;
-            for (const Cand& c : cands) {
-                if (slot_of[c.child] >= 0 || used_slot[c.slot]) continue;
-                slot_of[c.child] = c.slot;
-                used_slot[c.slot] = true;
+            for (size_t round = 0; round < m; ++round) {
+                int bi = -1, bs = -1;
+                for (size_t i = 0; i < m; ++i) {
+                    if (slot_of[i] >= 0) continue;
+                    for (int s2 = 0; s2 < 8; ++s2) {
+                        if (used_slot[s2]) continue;
+                        // children and slots are scanned in increasing order, so a strict
+                        // comparison keeps the first (lowest child, then slot) of equal costs
+                        if (bi < 0 || cost[i][s2] < cost[bi][bs]) {
+                            bi = (int)i;
+                            bs = s2;
+                        }
+                    }
+                }
+                slot_of[bi] = bs;
+                used_slot[bs] = true;
             }
         }
         int child_at[8];
@@ -494,7 +540,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
         const uint32_t tri_base = (uint32_t)out.tris.size();
         uint32_t n_inner = 0;
         uint8_t meta[8] = {}, qlo[3][8] = {}, qhi[3][8] = {};
-        std::vector<Task> push;
+        SmallVec<Task, 8> push;
         for (int s = 0; s < 8; ++s) {
             const int i = child_at[s];
             if (i < 0) continue;
@@ -544,7 +590,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
         std::memcpy(&node.w[18], qhi[2], 8);
         out.nodes.resize(out.nodes.size() + n_inner);
         out.nodes[t.cw] = node;
-        for (auto it = push.rbegin(); it != push.rend(); ++it) stack.push_back(*it);
+        for (size_t q = push.size(); q-- > 0;) stack.push_back(push[q]);
     }
     return true;
 }

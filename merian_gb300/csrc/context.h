@@ -36,7 +36,7 @@ struct gbpt_ctx {
     gbpt::TickEngine batch; // gbpt_render_batch, over `work`
     // schedule of gbpt_render* and gbpt_render_batch: paths per tick (0 = default), material sort
     // override (-1 = as each request asks), CUDA graphs
-    gbpt_tuning tuning{0, -1, 0};
+    gbpt_tuning tuning{0, -1, 0, GBPT_BVH_SPLIT, 0};
     unsigned long long* d_misc = nullptr; // [0] nodes, [1] tris, [2] error word
     gbpt_hit* d_hits = nullptr;
     uint64_t hits_cap = 0;

@@ -199,8 +199,11 @@ struct BuildInput {
     std::vector<uint32_t> geom;
     std::vector<uint32_t> flags; // instance mask (bits 0-7), two-sided (bit 8), flip (bit 9)
     // split triangles whose bounding box is loose into clipped references (never for TLAS
-    // builds, whose "triangles" are instance boxes)
+    // builds, whose "triangles" are instance boxes): box area above split_ratio x twice the
+    // triangle area, at most split_depth halvings
     bool split = false;
+    double split_ratio = 2.0;
+    int split_depth = 4;
 };
 
 struct CwBvh {

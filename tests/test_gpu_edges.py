@@ -153,3 +153,45 @@ def test_frame_larger_than_a_tick_matches_pixel_list(gpu_ctx):
         assert np.array_equal(full.view(np.uint32), sub.view(np.uint32))
     finally:
         gpu_ctx.destroy_scene(sid)
+
+
+@pytest.mark.gpu
+def test_bvh_build_modes_find_the_same_hits(gpu_ctx):
+    """GBPT_BVH_SPLIT (default), _MEDIUM and _FAST build different trees (split references or
+    not); closest and any hits of incoherent rays are the same bits in all three, and equal the
+    FP32 oracle's."""
+    import torch
+    from merian_gb300 import _native as N
+    from merian_gb300 import scene as S
+    sc = S.soup(S.BASE_SEED, 100_000, 64, (64, 32))
+    rng = np.random.default_rng(2)
+    rays = np.zeros(100_000, N.RAY_DTYPE)
+    rays["origin"] = rng.uniform(-0.2, 1.2, (len(rays), 3))
+    d = rng.normal(size=(len(rays), 3))
+    rays["direction"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays["tmax"] = 1e7
+    o, _, _ = O.OracleScene(sc).trace_rays(rays, fp64=False, hit_dtype=N.HIT_DTYPE)
+    d_rays = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
+    d_hits = torch.zeros(len(rays) * N.HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    nodes = []
+    try:
+        for mode in (N.BVH_FAST, N.BVH_MEDIUM, N.BVH_SPLIT):
+            gpu_ctx.set_tuning(bvh_build=mode)
+            sid = gpu_ctx.upload(sc)
+            try:
+                nodes.append(gpu_ctx.scene_stats(sid)["nodes"])
+                for any_hit in (False, True):
+                    gpu_ctx.trace(sid, d_rays.data_ptr(), len(rays), d_hits.data_ptr(),
+                                  any_hit=any_hit)
+                    gpu_ctx.synchronize()
+                    g = d_hits.cpu().numpy().view(N.HIT_DTYPE)
+                    if any_hit:
+                        assert np.array_equal(g["t"] > 0, o["t"] > 0)
+                    else:
+                        assert np.array_equal(g["primitive_id"], o["primitive_id"])
+                        assert np.array_equal(g["t"].view(np.uint32), o["t"].view(np.uint32))
+            finally:
+                gpu_ctx.destroy_scene(sid)
+        assert nodes[0] < nodes[1] < nodes[2]
+    finally:
+        gpu_ctx.set_tuning()
