@@ -329,9 +329,10 @@ typedef struct gbpt_tuning {
 } gbpt_tuning;
 
 /* BVH build of gbpt_scene_create (the traversal finds the same hits in every case). */
-#define GBPT_BVH_SPLIT 0  /* default: loose triangles split into up to 16 clipped references */
+#define GBPT_BVH_SPLIT 0  /* default: loose triangles split into up to 16 clipped references
+                           * (single-level scenes), up to 4 for very loose ones (BLASes) */
 #define GBPT_BVH_FAST 1   /* one reference per triangle: fastest build, smallest tree */
-#define GBPT_BVH_MEDIUM 2 /* up to 8 references for very loose triangles only */
+#define GBPT_BVH_MEDIUM 2 /* up to 4 references for very loose triangles only */
 
 GBPT_API int gbpt_set_tuning(gbpt_ctx* ctx, const gbpt_tuning* tuning);
 GBPT_API int gbpt_get_tuning(gbpt_ctx* ctx, gbpt_tuning* tuning);

@@ -11,6 +11,7 @@
 #include "host_common.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -426,15 +427,12 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
     struct Task {
         uint32_t b2node, cw, depth;
     };
-    out.nodes.reserve(b2.size() / 4 + 1);
-    out.tris.reserve(nref);
-    out.nodes.emplace_back();
-    std::vector<Task> stack{{0, 0, 1}};
     auto is_inner = [&](uint32_t k) { return !b2[k].leaf && b2[k].count > kMaxLeaf; };
-    while (!stack.empty()) {
-        const Task t = stack.back();
-        stack.pop_back();
-        out.depth = std::max(out.depth, t.depth);
+    // One CWBVH node from task t into (nodes, tris); its inner children become tasks. Returns
+    // false when the tree is deeper than max_depth.
+    auto emit = [&](const Task t, std::vector<CwNode>& nodes, std::vector<TriRecord>& tris,
+                    std::vector<Task>& stack, uint32_t& depth) -> bool {
+        depth = std::max(depth, t.depth);
         if (t.depth > max_depth) {
             set_error("BVH deeper than the traversal stack (" + std::to_string(max_depth) + ")");
             return false;
@@ -536,8 +534,8 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
         std::memcpy(&node.w[1], &nbox.lo[1], 4);
         std::memcpy(&node.w[2], &nbox.lo[2], 4);
         uint32_t imask = 0;
-        const uint32_t child_base = (uint32_t)out.nodes.size();
-        const uint32_t tri_base = (uint32_t)out.tris.size();
+        const uint32_t child_base = (uint32_t)nodes.size();
+        const uint32_t tri_base = (uint32_t)tris.size();
         uint32_t n_inner = 0;
         uint8_t meta[8] = {}, qlo[3][8] = {}, qhi[3][8] = {};
         SmallVec<Task, 8> push;
@@ -560,7 +558,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
                 push.push_back({ch[i], child_base + n_inner, t.depth + 1});
                 n_inner++;
             } else {
-                const uint32_t off = (uint32_t)out.tris.size() - tri_base;
+                const uint32_t off = (uint32_t)tris.size() - tri_base;
                 const uint32_t cnt = c.count;
                 for (uint32_t k = 0; k < cnt; ++k) {
                     const uint32_t p = rprim[idx[c.first + k]];
@@ -571,7 +569,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
                     tr.prim = in.prim[p];
                     tr.geom = in.geom[p];
                     tr.pad = in.flags.empty() ? 0xFFu : in.flags[p];
-                    out.tris.push_back(tr);
+                    tris.push_back(tr);
                 }
                 static const uint8_t unary[4] = {0, 1, 3, 7};
                 meta[s] = (uint8_t)((unary[cnt] << 5) | off);
@@ -588,9 +586,79 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
         std::memcpy(&node.w[14], qhi[0], 8);
         std::memcpy(&node.w[16], qhi[1], 8);
         std::memcpy(&node.w[18], qhi[2], 8);
-        out.nodes.resize(out.nodes.size() + n_inner);
-        out.nodes[t.cw] = node;
+        nodes.resize(nodes.size() + n_inner);
+        nodes[t.cw] = node;
         for (size_t q = push.size(); q-- > 0;) stack.push_back(push[q]);
+        return true;
+    };
+    // The top of the tree serially until there are enough independent subtrees, then every
+    // subtree into its own arrays in parallel, appended in order with rebased node and triangle
+    // indices (the layout is deterministic).
+    out.nodes.reserve(b2.size() / 4 + 1);
+    out.tris.reserve(nref);
+    out.nodes.emplace_back();
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<Task> stack{{0, 0, 1}};
+    if (nref >= 200000 && hw > 1) {
+        // breadth first until the frontier holds enough subtrees
+        std::vector<Task> frontier{{0, 0, 1}};
+        size_t head = 0;
+        while (head < frontier.size() && frontier.size() - head < 8 * (size_t)hw) {
+            const Task t = frontier[head++];
+            if (!emit(t, out.nodes, out.tris, frontier, out.depth)) return false;
+        }
+        stack.assign(frontier.begin() + (std::ptrdiff_t)head, frontier.end());
+    } else {
+        while (!stack.empty()) {
+            const Task t = stack.back();
+            stack.pop_back();
+            if (!emit(t, out.nodes, out.tris, stack, out.depth)) return false;
+        }
+    }
+    if (!stack.empty()) {
+        struct Sub {
+            std::vector<CwNode> nodes;
+            std::vector<TriRecord> tris;
+            uint32_t depth = 0;
+            bool ok = true;
+        };
+        std::vector<Sub> subs(stack.size());
+        std::vector<std::thread> threads;
+        std::atomic<size_t> next{0};
+        for (unsigned w = 0; w < hw; ++w) {
+            threads.emplace_back([&]() {
+                for (size_t i; (i = next.fetch_add(1)) < subs.size();) {
+                    Sub& sb = subs[i];
+                    sb.nodes.emplace_back(); // the subtree root, at local index 0
+                    std::vector<Task> st{{stack[i].b2node, 0, stack[i].depth}};
+                    while (!st.empty() && sb.ok) {
+                        const Task t = st.back();
+                        st.pop_back();
+                        sb.ok = emit(t, sb.nodes, sb.tris, st, sb.depth);
+                    }
+                }
+            });
+        }
+        for (auto& th : threads) th.join();
+        for (size_t i = 0; i < subs.size(); ++i) {
+            Sub& sb = subs[i];
+            if (!sb.ok) { // the worker's message is on its own thread
+                set_error("BVH deeper than the traversal stack (" + std::to_string(max_depth) + ")");
+                return false;
+            }
+            out.depth = std::max(out.depth, sb.depth);
+            // local node k >= 1 goes to base + k; the root goes to the task's reserved slot
+            const uint32_t base = (uint32_t)out.nodes.size() - 1;
+            const uint32_t tbase = (uint32_t)out.tris.size();
+            for (size_t k = 0; k < sb.nodes.size(); ++k) {
+                CwNode nd = sb.nodes[k];
+                nd.w[4] += base;
+                nd.w[5] += tbase;
+                if (k == 0) out.nodes[stack[i].cw] = nd;
+                else out.nodes.push_back(nd);
+            }
+            out.tris.insert(out.tris.end(), sb.tris.begin(), sb.tris.end());
+        }
     }
     return true;
 }
