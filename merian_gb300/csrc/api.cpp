@@ -92,10 +92,23 @@ bool invert_affine(const float* m, double* inv) {
 void free_scene(SceneGPU& s) {
     void* ptrs[] = {s.nodes,    s.tris,     s.verts,      s.idx,       s.geoms,    s.mats,
                     s.env,      s.env_marg, s.env_cond,   s.env_func,  s.light_tris, s.light_cdf,
+                    s.light_guide, s.env_marg_guide, s.env_cond_guide, s.geom_key,
                     s.inst,     s.tex,      s.tex_info,   s.srgb_lut};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     s = SceneGPU{};
+}
+
+// Guide table of an increasing float CDF a[0..n) ending at 1: entry k (k = 0..G) is
+// upper_bound(a, a + n, k / G) with the device's float comparison; G is the power of two at or
+// above n, at most 4096 (k / G and u * G are exact in float).
+std::vector<uint32_t> cdf_guide(const float* a, uint32_t n, uint32_t& G) {
+    G = 1;
+    while (G < n && G < 4096u) G <<= 1;
+    std::vector<uint32_t> g(G + 1);
+    for (uint32_t k = 0; k <= G; ++k)
+        g[k] = (uint32_t)(std::upper_bound(a, a + n, (float)k / (float)G) - a);
+    return g;
 }
 
 // The build input's reference splitting for a GBPT_BVH_* setting. GBPT_BVH_SPLIT splits hard in
@@ -445,6 +458,16 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
                  d->geometries[g].material_id, d->geometries[g].flags};
     if ((rc = upload(&s.geoms, gh.data(), gh.size() * sizeof(GeomHost), bytes))) return fail(rc);
     if ((rc = upload(&s.mats, d->materials, d->material_count * sizeof(gbpt_material), bytes))) return fail(rc);
+    // material-sort key per geometry: 0 environment (UseEnvMap), 1 + min(model, 2) otherwise
+    {
+        std::vector<uint8_t> keys(std::max<uint32_t>(d->geometry_count, 1u), 0u);
+        for (uint32_t g = 0; g < d->geometry_count; ++g) {
+            const gbpt_geometry& geo = d->geometries[g];
+            if (!(geo.flags & GBPT_MESH_USE_ENV_MAP))
+                keys[g] = (uint8_t)(1u + std::min(d->materials[geo.material_id].model, 2u));
+        }
+        if ((rc = upload(&s.geom_key, keys.data(), keys.size(), bytes))) return fail(rc);
+    }
     if (two_level) {
         if ((rc = upload(&s.inst, inst_rec.data(), inst_rec.size() * sizeof(float), bytes))) return fail(rc);
         s.n_inst = d->instance_count;
@@ -528,6 +551,8 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
             cdf.back() = 1.0f;
             if ((rc = upload(&s.light_tris, lt.data(), lt.size() * sizeof(float), bytes))) return fail(rc);
             if ((rc = upload(&s.light_cdf, cdf.data(), cdf.size() * sizeof(float), bytes))) return fail(rc);
+            const std::vector<uint32_t> lg = cdf_guide(cdf.data(), (uint32_t)cdf.size(), s.light_g);
+            if ((rc = upload(&s.light_guide, lg.data(), lg.size() * 4, bytes))) return fail(rc);
             s.n_lights = (uint32_t)pw.size();
             s.light_total = (float)acc;
         }
@@ -582,6 +607,15 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
         if ((rc = upload(&s.env_func, ffunc.data(), ffunc.size() * sizeof(float), bytes))) return fail(rc);
         if ((rc = upload(&s.env_cond, cond.data(), cond.size() * sizeof(float), bytes))) return fail(rc);
         if ((rc = upload(&s.env_marg, marg.data(), marg.size() * sizeof(float), bytes))) return fail(rc);
+        const std::vector<uint32_t> mg = cdf_guide(marg.data() + 1, h, s.env_marg_g);
+        std::vector<uint32_t> cg;
+        for (uint32_t y = 0; y < h; ++y) {
+            const std::vector<uint32_t> row =
+                cdf_guide(cond.data() + (size_t)y * (w + 1) + 1, w, s.env_cond_g);
+            cg.insert(cg.end(), row.begin(), row.end());
+        }
+        if ((rc = upload(&s.env_marg_guide, mg.data(), mg.size() * 4, bytes))) return fail(rc);
+        if ((rc = upload(&s.env_cond_guide, cg.data(), cg.size() * 4, bytes))) return fail(rc);
     }
     // RGBA8 textures, concatenated, with (first texel, width, height, sRGB) per texture and the
     // sRGB decoding table (IEC 61966-2-1), evaluated in double and rounded once

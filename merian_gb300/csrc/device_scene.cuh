@@ -45,6 +45,12 @@ struct DevScene {
     uint32_t n_lights;
     float light_total; // sum of area x luminance
     float p_env;       // probability of choosing the environment in NEE
+    // guide tables of the light, marginal and conditional CDFs: entry k is the upper bound of
+    // k / G (G a power of two), so the search for u covers [guide[k], guide[k + 1]] only
+    const uint32_t* __restrict__ light_guide;
+    const uint32_t* __restrict__ env_marg_guide;
+    const uint32_t* __restrict__ env_cond_guide; // G + 1 per row
+    uint32_t light_g, env_marg_g, env_cond_g;
     // two-level scenes: instance records (7 float4 each), n_inst = 0 for single-level scenes
     const float4* __restrict__ inst;
     uint32_t n_inst;

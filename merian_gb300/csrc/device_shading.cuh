@@ -29,6 +29,12 @@ inline DevScene make_dev_scene(const SceneGPU& s) {
     d.light_cdf = (const float*)s.light_cdf;
     d.n_lights = s.n_lights;
     d.light_total = s.light_total;
+    d.light_guide = (const uint32_t*)s.light_guide;
+    d.env_marg_guide = (const uint32_t*)s.env_marg_guide;
+    d.env_cond_guide = (const uint32_t*)s.env_cond_guide;
+    d.light_g = s.light_g;
+    d.env_marg_g = s.env_marg_g;
+    d.env_cond_g = s.env_cond_g;
     d.p_env = d.ew ? (s.n_lights ? 0.5f : 1.0f) : 0.0f;
     d.inst = (const float4*)s.inst;
     d.n_inst = s.n_inst;
@@ -242,8 +248,15 @@ GBPT_DI Material load_material(const DevScene& sc, uint32_t mid, bool front, flo
 }
 
 // ---- lights (next-event estimation; not in the reference, same expectation) ---------------------------
-GBPT_DI uint32_t upper_bound_f(const float* a, uint32_t n, float x) {
+// upper_bound(a, a + n, x) for x in [0, 1), the search narrowed by the CDF's guide table g (G
+// entries + 1): x * G is exact for a power-of-two G, so the bound lies in [g[k], g[k + 1]].
+GBPT_DI uint32_t upper_bound_f(const float* a, uint32_t n, float x, const uint32_t* g, uint32_t G) {
     uint32_t lo = 0, hi = n;
+    if (G) {
+        const uint32_t k = min((uint32_t)(x * (float)G), G - 1u);
+        lo = __ldg(&g[k]);
+        hi = __ldg(&g[k + 1]);
+    }
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
         if (__ldg(&a[mid]) <= x) lo = mid + 1;
@@ -286,11 +299,13 @@ GBPT_DI LightSample sample_light(const DevScene& sc, float3 pos, Pcg& rng) {
     const float u0 = rng.next_float(), u1 = rng.next_float(), u2 = rng.next_float();
     if (sc.p_env <= 0.f && sc.n_lights == 0u) return ls;
     if (u0 < sc.p_env) {
-        uint32_t y = upper_bound_f(sc.env_marg + 1, sc.eh, u1);
+        uint32_t y = upper_bound_f(sc.env_marg + 1, sc.eh, u1, sc.env_marg_guide, sc.env_marg_g);
         y = min(y, sc.eh - 1u);
         const float m0 = __ldg(&sc.env_marg[y]), m1 = __ldg(&sc.env_marg[y + 1]);
         const float* c = sc.env_cond + (size_t)y * (sc.ew + 1);
-        uint32_t x = upper_bound_f(c + 1, sc.ew, u2);
+        uint32_t x = upper_bound_f(c + 1, sc.ew, u2,
+                                   sc.env_cond_guide + (size_t)y * (sc.env_cond_g + 1u),
+                                   sc.env_cond_g);
         x = min(x, sc.ew - 1u);
         const float c0 = __ldg(&c[x]), c1 = __ldg(&c[x + 1]);
         const float fy = fminf(fmaxf((u1 - m0) / (m1 - m0), 0.f), 1.f);
@@ -313,7 +328,7 @@ GBPT_DI LightSample sample_light(const DevScene& sc, float3 pos, Pcg& rng) {
         return ls;
     }
     const float ut = sc.p_env > 0.f ? (u0 - sc.p_env) / (1.0f - sc.p_env) : u0;
-    uint32_t k = upper_bound_f(sc.light_cdf, sc.n_lights, ut);
+    uint32_t k = upper_bound_f(sc.light_cdf, sc.n_lights, ut, sc.light_guide, sc.light_g);
     k = min(k, sc.n_lights - 1u);
     const float4 a4 = __ldg(&sc.light_tris[3 * k + 0]);
     const float4 b4 = __ldg(&sc.light_tris[3 * k + 1]);

@@ -19,6 +19,7 @@ struct SceneGPU {
     void* verts = nullptr;      // gbpt_packed_vertex
     void* idx = nullptr;        // uint32 x 3 per triangle
     void* geoms = nullptr;      // GeomGPU
+    void* geom_key = nullptr;   // uint8 material-sort key per geometry
     void* mats = nullptr;       // gbpt_material
     void* env = nullptr;        // float4 texels
     void* env_marg = nullptr;
@@ -26,6 +27,11 @@ struct SceneGPU {
     void* env_func = nullptr;
     void* light_tris = nullptr; // 3 float4 per emissive triangle
     void* light_cdf = nullptr;
+    // guide tables of the CDFs (upper bound of k / G for k = 0..G, G a power of two)
+    void* light_guide = nullptr;
+    void* env_marg_guide = nullptr;
+    void* env_cond_guide = nullptr; // G + 1 entries per row
+    uint32_t light_g = 0, env_marg_g = 0, env_cond_g = 0;
     uint64_t n_nodes = 0, n_tris = 0, n_verts = 0;
     uint32_t geom_count = 0, mat_count = 0;
     uint32_t ew = 0, eh = 0;

@@ -41,6 +41,12 @@ constexpr int kShadeBlocksPerSM = GBPT_SHADE_BLOCKS_PER_SM;
 
 constexpr uint32_t kReqEmission = 1u, kReqNee = 2u, kReqDemodulate = 4u;
 
+// "shader execution reordering" (render_pt.cpp:160-161): the closest-hit queue is ordered by
+// material model before shading, so the warps of k_shade run one BSDF model at a time. Keys:
+// 0 environment (miss or UseEnvMap geometry), 1 diffuse, 2 OpenPBR, 3 OpenPBR with transmission.
+// Shading results do not depend on the order (each entry updates only its own path).
+constexpr int kSortKeys = 4;
+
 struct ReqGPU {
     CamGPU cam;
     uint32_t width, height, spp, max_len;
@@ -64,7 +70,7 @@ struct ChunkGPU {
     const uint4* nodes; // the scene's traversal data, for the trace kernels
     const float4* tris;
     const float4* insts; // instance records of a two-level scene, else nullptr
-    uint64_t pad;
+    const uint8_t* geom_key; // material-sort key of each geometry of the scene
 };
 static_assert(sizeof(ChunkGPU) == 64, "chunk layout");
 
@@ -274,9 +280,13 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM) k_shade_primary(TickAr
 // Closest hit for every entry of ray queue `qi` (persistent warps, counter w.counters[4]).
 template <bool COUNT, bool TWO_LEVEL, bool ALPHA>
 __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
-    k_trace(TickArgs t, int qi, unsigned long long* work_ctr) {
+    k_trace(TickArgs t, int qi, unsigned long long* work_ctr, int sort) {
     const uint32_t n = t.w.counters[qi];
     TraceCounters ctr{0, 0};
+    // with material-sorted shading: each hit's sort key, counted per block in shared memory
+    __shared__ uint32_t key_count[kSortKeys];
+    if (threadIdx.x < kSortKeys) key_count[threadIdx.x] = 0u;
+    __syncthreads();
     const float4* q = t.w.q_od[qi];
     const uint32_t* qp = t.w.q_path[qi];
     auto load = [&](uint32_t i, TraceState& s) {
@@ -293,6 +303,13 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
         t.w.hit_tuv[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
         t.w.hit_geom[i] = h.geom;
         t.w.hit_inst[i] = h.inst;
+        if (sort) {
+            uint32_t key = 0u; // misses shade the environment
+            if (h.geom != kNoInst)
+                key = __ldg(&t.chunks[__ldg(&qp[i]) >> kPathBits].geom_key[h.geom]);
+            t.w.keys[i] = (uint8_t)key;
+            atomicAdd(&key_count[key], 1u);
+        }
     };
     auto alpha = [&](uint32_t i, uint32_t g, uint32_t p, float u, float v) {
         return ALPHA &&
@@ -300,6 +317,11 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
     };
     trace_persistent<false, COUNT, TWO_LEVEL>(n, t.w.counters + 4, load, store, alpha, &ctr,
                                               t.w.counters + 3);
+    if (sort) {
+        __syncthreads();
+        if (threadIdx.x < kSortKeys && key_count[threadIdx.x])
+            atomicAdd(t.w.counters + 8 + threadIdx.x, key_count[threadIdx.x]);
+    }
     if (COUNT) {
         atomicAdd(work_ctr + 0, (unsigned long long)ctr.nodes);
         atomicAdd(work_ctr + 1, (unsigned long long)ctr.tris);
@@ -379,63 +401,70 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM)
     }
 }
 
-// "shader execution reordering" (render_pt.cpp:160-161): the closest-hit queue is ordered by
-// material model before shading, so the warps of k_shade run one BSDF model at a time. Keys:
-// 0 environment (miss or UseEnvMap geometry), 1 diffuse, 2 OpenPBR, 3 OpenPBR with transmission.
-// Shading results do not depend on the order (each entry updates only its own path).
-constexpr int kSortKeys = 4;
-
-__global__ void __launch_bounds__(256) k_sort_keys(TickArgs t, int qi) {
-    const uint32_t n = t.w.counters[qi];
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t n_round = (n + 31u) & ~31u;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
-        uint32_t key = 0xFFu;
-        if (i < n) {
-            key = 0u;
-            const uint32_t geom = t.w.hit_geom[i];
-            const ChunkGPU& c = t.chunks[__ldg(&t.w.q_path[qi][i]) >> kPathBits];
-            const DevScene& sc = t.scenes[c.scene];
-            if (geom < sc.geom_count) {
-                const GeomGPU g = sc.geoms[geom];
-                if (!(g.flags & GBPT_MESH_USE_ENV_MAP))
-                    key = 1u + min(__float_as_uint(__ldg(&sc.mats[5 * g.material]).x), 2u);
-            }
-            t.w.keys[i] = (uint8_t)key;
-        }
-#pragma unroll
-        for (uint32_t k = 0; k < kSortKeys; ++k) {
-            const uint32_t m = __ballot_sync(0xFFFFFFFFu, key == k);
-            if (lane == 0 && m) atomicAdd(t.w.counters + 8 + k, (uint32_t)__popc(m));
-        }
-    }
-}
-
+// The entries in key order (a stable-within-tile counting sort): the traversal wrote each
+// entry's key and the per-key totals; each block takes tiles of kSortTile consecutive entries,
+// ranks them per key with warp ballots, reserves its ranges with one atomic per key and tile, and
+// writes the permutation. The order of the tiles within a key is not deterministic (shading does
+// not depend on it).
+constexpr uint32_t kSortTile = 2048; // 256 threads x 8 entries
 __global__ void __launch_bounds__(256) k_sort_scatter(TickArgs t, int qi, uint32_t* perm) {
     const uint32_t n = t.w.counters[qi];
-    const uint32_t lane = threadIdx.x & 31u;
-    uint32_t base[kSortKeys];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    __shared__ uint32_t warp_count[8][kSortKeys]; // then each warp's offset within the tile
+    __shared__ uint32_t tile_base[kSortKeys];
+    uint32_t key_base[kSortKeys];
     uint32_t acc = 0;
 #pragma unroll
     for (int k = 0; k < kSortKeys; ++k) {
-        base[k] = acc;
+        key_base[k] = acc;
         acc += t.w.counters[8 + k];
     }
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t n_round = (n + 31u) & ~31u;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
-        const uint32_t key = i < n ? t.w.keys[i] : 0xFFu;
+    for (uint32_t tile = blockIdx.x; tile * kSortTile < n; tile += gridDim.x) {
+        // this warp's 256 consecutive entries: 8 rounds of 32
+        const uint32_t first = tile * kSortTile + warp * 256u;
+        uint8_t key[8];
+        uint32_t count[kSortKeys] = {0u, 0u, 0u, 0u};
 #pragma unroll
-        for (uint32_t k = 0; k < kSortKeys; ++k) {
-            const uint32_t m = __ballot_sync(0xFFFFFFFFu, key == k);
-            if (!m) continue;
-            const uint32_t leader = __ffs(m) - 1u;
-            uint32_t b = 0;
-            if (lane == leader) b = atomicAdd(t.w.counters + 12 + k, (uint32_t)__popc(m));
-            b = __shfl_sync(0xFFFFFFFFu, b, leader);
-            if (key == k) perm[base[k] + b + __popc(m & ((1u << lane) - 1u))] = i;
+        for (int r = 0; r < 8; ++r) {
+            const uint32_t i = first + 32u * r + lane;
+            key[r] = i < n ? t.w.keys[i] : (uint8_t)0xFF;
+#pragma unroll
+            for (int k = 0; k < kSortKeys; ++k)
+                count[k] += __popc(__ballot_sync(0xFFFFFFFFu, key[r] == k));
         }
+        if (lane < kSortKeys) {
+            uint32_t c = 0;
+#pragma unroll
+            for (int k = 0; k < kSortKeys; ++k)
+                if (k == (int)lane) c = count[k];
+            warp_count[warp][lane] = c;
+        }
+        __syncthreads();
+        if (threadIdx.x < kSortKeys) {
+            const uint32_t k = threadIdx.x;
+            uint32_t run = 0;
+            for (int w = 0; w < 8; ++w) {
+                const uint32_t c = warp_count[w][k];
+                warp_count[w][k] = run;
+                run += c;
+            }
+            tile_base[k] = run ? key_base[k] + atomicAdd(t.w.counters + 12 + k, run) : 0u;
+        }
+        __syncthreads();
+        uint32_t at[kSortKeys];
+#pragma unroll
+        for (int k = 0; k < kSortKeys; ++k) at[k] = tile_base[k] + warp_count[warp][k];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const uint32_t i = first + 32u * r + lane;
+#pragma unroll
+            for (int k = 0; k < kSortKeys; ++k) {
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, key[r] == k);
+                if (key[r] == k) perm[at[k] + __popc(m & ((1u << lane) - 1u))] = i;
+                at[k] += __popc(m);
+            }
+        }
+        __syncthreads(); // warp_count and tile_base are reused by the next tile
     }
 }
 
@@ -706,15 +735,16 @@ Grids launch_grids() {
 void launch_trace(const TickArgs& ta, const TickPlan& tp, const Grids& g, int qi,
                   unsigned long long* work_ctr, cudaStream_t st) {
     const int gr = work_ctr ? g.trace_c : g.trace;
+    const int so = tp.sort ? 1 : 0;
     switch ((work_ctr ? 4 : 0) | (tp.two_level ? 2 : 0) | (tp.alpha ? 1 : 0)) {
-    case 0: k_trace<false, false, false><<<gr, 128, 0, st>>>(ta, qi, nullptr); break;
-    case 1: k_trace<false, false, true><<<gr, 128, 0, st>>>(ta, qi, nullptr); break;
-    case 2: k_trace<false, true, false><<<gr, 128, 0, st>>>(ta, qi, nullptr); break;
-    case 3: k_trace<false, true, true><<<gr, 128, 0, st>>>(ta, qi, nullptr); break;
-    case 4: k_trace<true, false, false><<<gr, 128, 0, st>>>(ta, qi, work_ctr); break;
-    case 5: k_trace<true, false, true><<<gr, 128, 0, st>>>(ta, qi, work_ctr); break;
-    case 6: k_trace<true, true, false><<<gr, 128, 0, st>>>(ta, qi, work_ctr); break;
-    default: k_trace<true, true, true><<<gr, 128, 0, st>>>(ta, qi, work_ctr); break;
+    case 0: k_trace<false, false, false><<<gr, 128, 0, st>>>(ta, qi, nullptr, so); break;
+    case 1: k_trace<false, false, true><<<gr, 128, 0, st>>>(ta, qi, nullptr, so); break;
+    case 2: k_trace<false, true, false><<<gr, 128, 0, st>>>(ta, qi, nullptr, so); break;
+    case 3: k_trace<false, true, true><<<gr, 128, 0, st>>>(ta, qi, nullptr, so); break;
+    case 4: k_trace<true, false, false><<<gr, 128, 0, st>>>(ta, qi, work_ctr, so); break;
+    case 5: k_trace<true, false, true><<<gr, 128, 0, st>>>(ta, qi, work_ctr, so); break;
+    case 6: k_trace<true, true, false><<<gr, 128, 0, st>>>(ta, qi, work_ctr, so); break;
+    default: k_trace<true, true, true><<<gr, 128, 0, st>>>(ta, qi, work_ctr, so); break;
     }
 }
 
@@ -762,18 +792,17 @@ uint64_t enqueue_tick(const TickArgs& ta, const TickPlan& tp, const Grids& g, cu
     for (uint32_t k = 2; k <= L; ++k) {
         const int qo = qi ^ 1;
         cudaMemsetAsync(ctr + 4, 0, sizeof(uint32_t), st);
+        if (tp.sort) cudaMemsetAsync(ctr + 8, 0, 8 * sizeof(uint32_t), st); // key counts, cursors
         ev = prof->begin(st, 0);
         launch_trace(ta, tp, g, qi, work_ctr, st);
         prof->end(st, ev);
         const uint32_t* perm = nullptr;
         if (tp.sort) {
-            cudaMemsetAsync(ctr + 8, 0, 8 * sizeof(uint32_t), st);
             ev = prof->begin(st, 1);
-            k_sort_keys<<<g.grid / 2, 256, 0, st>>>(ta, qi);
             k_sort_scatter<<<g.grid / 2, 256, 0, st>>>(ta, qi, ta.w.perm);
             prof->end(st, ev);
             perm = ta.w.perm;
-            nl += 2;
+            nl += 1;
         }
         cudaMemsetAsync(ctr + qo, 0, sizeof(uint32_t), st);
         ev = prof->begin(st, 1);
@@ -886,6 +915,7 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
         c.nodes = scenes[si].nodes;
         c.tris = scenes[si].tris;
         c.insts = scenes[si].n_inst ? scenes[si].inst : nullptr;
+        c.geom_key = (const uint8_t*)it.scene->geom_key;
         tp.two_level |= scenes[si].n_inst != 0u;
         tp.alpha |= it.scene->alpha;
         ++tp.n_chunks;
