@@ -109,9 +109,13 @@ GBPT_DI uint32_t chunk_by_path(const ChunkGPU* c, uint32_t n, uint32_t p) {
 GBPT_DI uint32_t pixel_id(const ReqGPU& r, uint32_t li) { return r.pixels ? __ldg(&r.pixels[li]) : li; }
 
 // Primary hit + shading point per pixel slot (gbuffer_rt.slang:18-58, render_pt.slang:98-103)
-__global__ void __launch_bounds__(128) k_primary(TickArgs t) {
+__global__ void __launch_bounds__(128) k_primary(TickArgs t, int sort) {
     const uint32_t n = t.hdr->n_pix, nc = t.hdr->n_chunks;
     const uint32_t stride = gridDim.x * blockDim.x;
+    // with material-sorted shading: the key of each pixel's primary hit for all its paths
+    __shared__ uint32_t key_count[kSortKeys];
+    if (threadIdx.x < kSortKeys) key_count[threadIdx.x] = 0u;
+    __syncthreads();
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
         const ChunkGPU c = t.chunks[chunk_by_slot(t.chunks, nc, q)];
         const ReqGPU& r = t.reqs[c.req];
@@ -123,6 +127,12 @@ __global__ void __launch_bounds__(128) k_primary(TickArgs t) {
         camera_ray(r.cam, px, py, r.width, r.height, o, d, tmin, tmax);
         const Hit h = trace_ray<false, false>(sc, o, d, tmin, tmax, c.mask, nullptr,
                                               t.w.counters + 3);
+        if (sort) {
+            const uint32_t key = h.geom < sc.geom_count ? __ldg(&c.geom_key[h.geom]) : 0u;
+            uint8_t* kp = t.w.keys + c.path_base + (q - c.slot_base) * c.spp;
+            for (uint32_t s2 = 0; s2 < c.spp; ++s2) kp[s2] = (uint8_t)key;
+            atomicAdd(&key_count[key], c.spp);
+        }
         SPd sp;
         if (h.geom == 0xFFFFFFFFu || h.geom >= sc.geom_count) {
             sp = env_sp(sc, o, d);
@@ -154,6 +164,11 @@ __global__ void __launch_bounds__(128) k_primary(TickArgs t) {
         pc[6] = make_float4(sp.tex_color.x, sp.tex_color.y, sp.tex_color.z, 0.f);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(t.w.stats + 0, (unsigned long long)n);
+    if (sort) {
+        __syncthreads();
+        if (threadIdx.x < kSortKeys && key_count[threadIdx.x])
+            atomicAdd(t.w.counters + 8 + threadIdx.x, key_count[threadIdx.x]);
+    }
 }
 
 // One iteration of the trace_path loop (render_pt.slang:35-79) from shading point sp, reached
@@ -213,16 +228,18 @@ GBPT_DI bool scatter(const DevScene& sc, const ReqGPU& r, int k, const SPd& sp, 
 }
 
 // Path start at the primary shading point (render_pt.slang:113-117) and the first scatter.
-__global__ void __launch_bounds__(128, kShadeBlocksPerSM) k_shade_primary(TickArgs t) {
+__global__ void __launch_bounds__(128, kShadeBlocksPerSM)
+    k_shade_primary(TickArgs t, const uint32_t* __restrict__ perm) {
     const uint32_t n = t.hdr->n_paths, nc = t.hdr->n_chunks;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_round = (n + 31u) & ~31u;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_round; p += stride) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_round; j += stride) {
         bool want = false, want_shadow = false;
         float3 no, nd;
         float4 s_o, s_d, s_c;
         uint32_t ci = 0;
-        if (p < n) {
+        const uint32_t p = (perm && j < n) ? __ldg(&perm[j]) : j;
+        if (j < n) {
             ci = chunk_by_path(t.chunks, nc, p);
             const ChunkGPU c = t.chunks[ci];
             const ReqGPU& r = t.reqs[c.req];
@@ -408,7 +425,7 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM)
 // not depend on it).
 constexpr uint32_t kSortTile = 2048; // 256 threads x 8 entries
 __global__ void __launch_bounds__(256) k_sort_scatter(TickArgs t, int qi, uint32_t* perm) {
-    const uint32_t n = t.w.counters[qi];
+    const uint32_t n = qi < 0 ? t.hdr->n_paths : t.w.counters[qi]; // qi < 0: the tick's paths
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __shared__ uint32_t warp_count[8][kSortKeys]; // then each warp's offset within the tile
     __shared__ uint32_t tile_base[kSortKeys];
@@ -772,12 +789,21 @@ uint64_t enqueue_tick(const TickArgs& ta, const TickPlan& tp, const Grids& g, cu
     uint64_t nl = 0;
     cudaMemsetAsync(ctr, 0, 3 * sizeof(uint32_t), st);
     const int pgrid = (int)std::min<uint64_t>((pix + 127) / 128, (uint64_t)g.primary);
+    if (tp.sort) cudaMemsetAsync(ctr + 8, 0, 8 * sizeof(uint32_t), st); // key counts, cursors
     int ev = prof->begin(st, 3);
-    k_primary<<<pgrid, 128, 0, st>>>(ta);
+    k_primary<<<pgrid, 128, 0, st>>>(ta, tp.sort ? 1 : 0);
     prof->end(st, ev);
+    const uint32_t* pperm = nullptr;
+    if (tp.sort) {
+        ev = prof->begin(st, 1);
+        k_sort_scatter<<<g.grid / 2, 256, 0, st>>>(ta, -1, ta.w.perm);
+        prof->end(st, ev);
+        pperm = ta.w.perm;
+        nl += 1;
+    }
     const int sgrid = (int)std::min<uint64_t>((paths + 127) / 128, (uint64_t)g.shade_p);
     ev = prof->begin(st, 1);
-    k_shade_primary<<<sgrid, 128, 0, st>>>(ta);
+    k_shade_primary<<<sgrid, 128, 0, st>>>(ta, pperm);
     prof->end(st, ev);
     nl += 2;
     if (nee) {
@@ -1069,7 +1095,7 @@ int primary_points(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaS
     ta.chunks = d_chunks;
     ta.hdr = d_hdr;
     ta.w = w;
-    k_primary<<<(P + 127) / 128, 128, 0, st>>>(ta);
+    k_primary<<<(P + 127) / 128, 128, 0, st>>>(ta, 0);
     // the first 6 float4 of every cached point: the gbpt_debug_primary_points layout
     if (cudaMemcpy2DAsync(out_device, 6 * sizeof(float4), w.pix, kPixFloat4 * sizeof(float4),
                           6 * sizeof(float4), P, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
