@@ -57,6 +57,9 @@ struct B2Node {
 #define GBPT_BVH_TRAVERSE_COST 0.5f
 #endif
 constexpr int kMaxSplitDepth = 6;
+// Split clipping falls back to one reference per triangle above this many references (node and
+// triangle indices are 32-bit; 2^30 references are 48 GB of triangle records).
+constexpr size_t kMaxReferences = size_t(1) << 30;
 constexpr int kBins = GBPT_BVH_BINS;
 constexpr float kCostTraverse = GBPT_BVH_TRAVERSE_COST; // relative to one triangle test
 constexpr uint32_t kMaxLeaf = 3;      // CWBVH leaf children hold up to three triangles
@@ -217,7 +220,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
         int depth;
     };
     static_assert(kMaxSplitDepth <= 6, "clipped pieces hold at most 9 corners");
-    const int split_depth = std::min(std::max(in.split_depth, 0), kMaxSplitDepth);
+    int split_depth = std::min(std::max(in.split_depth, 0), kMaxSplitDepth);
     const double split_ratio = std::max(in.split_ratio, 1.0);
     // references of triangles [begin, end), in triangle order
     auto make_refs = [&](size_t begin, size_t end, std::vector<Box>& boxes,
@@ -300,7 +303,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
     std::vector<Box> pbox;
     std::vector<uint32_t> rprim;
     Box scene;
-    {
+    for (int attempt = 0; attempt < 2; ++attempt) {
         // in parallel over contiguous triangle ranges, concatenated in order (deterministic)
         const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
         const size_t parts = n < 100000 ? 1 : hw;
@@ -316,6 +319,10 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
         for (auto& t : threads) t.join();
         size_t total = 0;
         for (size_t k = 0; k < parts; ++k) total += pb[k].size();
+        if (total > kMaxReferences && split_depth > 0) {
+            split_depth = 0; // too many pieces: one reference per triangle
+            continue;
+        }
         pbox.reserve(total);
         rprim.reserve(total);
         for (size_t k = 0; k < parts; ++k) {
@@ -323,6 +330,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
             rprim.insert(rprim.end(), pp[k].begin(), pp[k].end());
             scene.grow(bounds[k]);
         }
+        break;
     }
     const size_t nref = pbox.size();
     std::vector<float> cent(3 * nref);
