@@ -57,9 +57,9 @@ struct B2Node {
 #define GBPT_BVH_TRAVERSE_COST 0.5f
 #endif
 constexpr int kMaxSplitDepth = 6;
-// Split clipping falls back to one reference per triangle above this many references (node and
-// triangle indices are 32-bit; 2^30 references are 48 GB of triangle records).
-constexpr size_t kMaxReferences = size_t(1) << 30;
+// Split clipping halves its depth while it would make more references than this (2^28 references
+// are 13 GB of triangle records and about 27 GB of host memory during the build).
+constexpr size_t kMaxReferences = size_t(1) << 28;
 constexpr int kBins = GBPT_BVH_BINS;
 constexpr float kCostTraverse = GBPT_BVH_TRAVERSE_COST; // relative to one triangle test
 constexpr uint32_t kMaxLeaf = 3;      // CWBVH leaf children hold up to three triangles
@@ -303,7 +303,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
     std::vector<Box> pbox;
     std::vector<uint32_t> rprim;
     Box scene;
-    for (int attempt = 0; attempt < 2; ++attempt) {
+    while (true) {
         // in parallel over contiguous triangle ranges, concatenated in order (deterministic)
         const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
         const size_t parts = n < 100000 ? 1 : hw;
@@ -320,7 +320,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
         size_t total = 0;
         for (size_t k = 0; k < parts; ++k) total += pb[k].size();
         if (total > kMaxReferences && split_depth > 0) {
-            split_depth = 0; // too many pieces: one reference per triangle
+            split_depth /= 2; // too many pieces: split less, at last one reference per triangle
             continue;
         }
         pbox.reserve(total);
