@@ -425,6 +425,43 @@ GBPT_API int gbpt_image_read_pfm(const char* path, float* texels, uint32_t chann
 GBPT_API int gbpt_image_read_png(const char* path, uint8_t* rgba, uint32_t* width,
                                  uint32_t* height);
 
+/* ---- the node graph: merian graph JSONs of this path's nodes (graph.cpp) --------------------
+ * merian's nodes are C++ classes behind a registry (node_registry.cpp:60-110) that Graph::run
+ * calls once per iteration (graph.cpp:323-360). These calls host the same node types in C++:
+ * "Render (Path-traced)", "GBuffer (Raytraced)", "Accumulate", "Image Write" (PFM), "Error
+ * Plot", "GLTF Scene" and "PBRT Scene" (the loaders below; the scene is made resident when the
+ * graph first runs), with merian's connector names, property keys and defaults, from a graph JSON in
+ * merian's layout (examples/renderers/pt.json). A graph created with ctx = NULL is checked
+ * (types, properties, edges) but cannot run. Not thread-safe: one caller per graph.
+ * Properties: gbpt_graph_set_property takes one JSON value ("group/key" for a property in a
+ * group such as Image Write's "advanced") and returns merian's NodeStatusFlags (1 =
+ * NEEDS_RECONNECT); unknown keys are errors there and warnings in the graph JSON. Outputs are
+ * named "node.output" and read to the host (synchronising the context stream). */
+typedef struct gbpt_graph gbpt_graph;
+GBPT_API int gbpt_graph_create(gbpt_ctx* ctx, const char* graph_json, gbpt_graph** out_graph);
+GBPT_API int gbpt_graph_destroy(gbpt_graph* graph);
+/* nodes in run order (dependencies first, ties by name) */
+GBPT_API int gbpt_graph_node_count(const gbpt_graph* graph, uint32_t* count);
+GBPT_API int gbpt_graph_node(const gbpt_graph* graph, uint32_t index, const char** name,
+                             const char** type);
+GBPT_API uint32_t gbpt_graph_warning_count(const gbpt_graph* graph);
+GBPT_API const char* gbpt_graph_warning(const gbpt_graph* graph, uint32_t index);
+GBPT_API int gbpt_graph_set_property(gbpt_graph* graph, const char* node, const char* key,
+                                     const char* json_value, uint32_t* out_flags);
+/* key = NULL: every property of the node as one JSON object. length = the text's size. */
+GBPT_API int gbpt_graph_get_property(const gbpt_graph* graph, const char* node, const char* key,
+                                     char* json_out, uint64_t capacity, uint64_t* length);
+/* Runs `iterations` graph iterations on the context stream. A node with a connected "scene"
+ * input renders that scene with its file's camera; the others render `scene` with `camera`
+ * (NULL when every renderer has a scene input). width x height is the extent of a renderer
+ * without a GBuffer input. */
+GBPT_API int gbpt_graph_run(gbpt_graph* graph, uint32_t scene, const gbpt_camera* camera,
+                            uint32_t width, uint32_t height, uint32_t iterations);
+/* out_host = NULL returns the size only (floats_per_texel: 4 RGBA32F, 1 history, 16 GBuffer). */
+GBPT_API int gbpt_graph_output(gbpt_graph* graph, const char* connector, float* out_host,
+                               uint64_t capacity_floats, uint32_t* width, uint32_t* height,
+                               uint32_t* floats_per_texel);
+
 /* ---- traversal queries (the GBuffer node's primary hit, and raw ray queries) ---------------
  * gbpt_trace_primary: the hit merian's GBuffer (Raytraced) node stores for each pixel
  * (gbuffer_rt.slang:18-58) with full-precision barycentrics and t, written to a host array of

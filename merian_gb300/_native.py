@@ -228,6 +228,22 @@ EXPORTS = [
     ("gbpt_loaded_scene_warning", C.c_char_p, [C.c_void_p, C.c_uint32]),
     ("gbpt_loaded_scene_free", None, [C.c_void_p]),
     ("gbpt_gen_env", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p]),
+    ("gbpt_graph_create", C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_void_p)]),
+    ("gbpt_graph_destroy", C.c_int, [C.c_void_p]),
+    ("gbpt_graph_node_count", C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
+    ("gbpt_graph_node", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_char_p),
+                                  C.POINTER(C.c_char_p)]),
+    ("gbpt_graph_warning_count", C.c_uint32, [C.c_void_p]),
+    ("gbpt_graph_warning", C.c_char_p, [C.c_void_p, C.c_uint32]),
+    ("gbpt_graph_set_property", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p,
+                                          C.POINTER(C.c_uint32)]),
+    ("gbpt_graph_get_property", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p,
+                                          C.c_uint64, C.POINTER(C.c_uint64)]),
+    ("gbpt_graph_run", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.c_uint32,
+                                 C.c_uint32, C.c_uint32]),
+    ("gbpt_graph_output", C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_uint64,
+                                    C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                    C.POINTER(C.c_uint32)]),
 ]
 
 _lib = None

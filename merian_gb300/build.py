@@ -21,7 +21,7 @@ BUILD = HERE / "_build"
 LIB = HERE / "libgbpt.so"
 
 CUDA_SOURCES = ["wavefront.cu", "kernels.cu", "nodes.cu", "debug_kernels.cu"]
-HOST_SOURCES = ["api.cpp", "server.cpp", "bvh.cpp", "scenegen.cpp", "image_io.cpp", "pbrt_loader.cpp", "gltf_loader.cpp", "png.cpp"]
+HOST_SOURCES = ["api.cpp", "server.cpp", "bvh.cpp", "scenegen.cpp", "image_io.cpp", "pbrt_loader.cpp", "gltf_loader.cpp", "png.cpp", "graph.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

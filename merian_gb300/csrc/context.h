@@ -62,5 +62,9 @@ int check_ctx(gbpt_ctx* ctx);
 int validate_params(const gbpt_camera* cam, const gbpt_render_params* p);
 // Seconds on the host's steady clock (request timestamps).
 double host_clock();
+// The GBuffer node's emission image: n RGBA32F texels (alpha 1) from n GBuffer texels, device
+// memory, enqueued on the context stream (nodes.cu).
+int gbuffer_emission(gbpt_ctx* ctx, const gbpt_gbuffer_texel* texels, float* out_device,
+                     uint64_t n);
 
 } // namespace gbpt

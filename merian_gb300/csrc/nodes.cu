@@ -75,7 +75,28 @@ __global__ void __launch_bounds__(256) k_error_partial(const float4* __restrict_
     }
 }
 
+// The GBuffer node's "emission" image: RGBA32F texels (alpha 1) from the GBuffer texels.
+__global__ void k_gbuffer_emission(const gbpt_gbuffer_texel* __restrict__ g, float4* out,
+                                   uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = make_float4(g[i].emission[0], g[i].emission[1], g[i].emission[2], 1.0f);
+}
+
 } // namespace
+
+int gbuffer_emission(gbpt_ctx* ctx, const gbpt_gbuffer_texel* texels, float* out_device,
+                     uint64_t n) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (n == 0) return GBPT_OK;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    const int grid = (int)std::min<uint64_t>((n + 255) / 256, (uint64_t)num_sms() * 16);
+    k_gbuffer_emission<<<grid, 256, 0, ctx->stream>>>(texels, (float4*)out_device, n);
+    GBPT_CUDA_CHECK(cudaGetLastError());
+    return GBPT_OK;
+}
+
 } // namespace gbpt
 
 using namespace gbpt;
