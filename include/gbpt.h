@@ -457,6 +457,13 @@ GBPT_API int gbpt_graph_get_property(const gbpt_graph* graph, const char* node, 
  * without a GBuffer input. */
 GBPT_API int gbpt_graph_run(gbpt_graph* graph, uint32_t scene, const gbpt_camera* camera,
                             uint32_t width, uint32_t height, uint32_t iterations);
+/* Checkpoint / resume of a progressive render: gbpt_graph_save writes directory/
+ * graph_state.json (the iteration count, every node's properties and counters) and each
+ * Accumulate node's image as PFM files (node.rgb.pfm = rgb, node.aux.pfm = (alpha, history, 0),
+ * exact float32); gbpt_graph_load restores them into a graph made from the same JSON, and its
+ * next run continues as if it had not stopped. JSON has no infinity: null stands for it. */
+GBPT_API int gbpt_graph_save(gbpt_graph* graph, const char* directory);
+GBPT_API int gbpt_graph_load(gbpt_graph* graph, const char* directory);
 /* out_host = NULL returns the size only (floats_per_texel: 4 RGBA32F, 1 history, 16 GBuffer). */
 GBPT_API int gbpt_graph_output(gbpt_graph* graph, const char* connector, float* out_host,
                                uint64_t capacity_floats, uint32_t* width, uint32_t* height,
@@ -493,6 +500,11 @@ GBPT_API int gbpt_trace_counted(gbpt_ctx* ctx, uint32_t scene, const gbpt_ray* r
  * the device BSDFs, one thread: kind 0 Lambert(albedo), 1 GGX(alpha, alpha_y), 2 conductor(alpha,
  * f0), 3 rough dielectric(alpha, eta, tint = albedo), 4 Fresnel mix GGX/Lambert(alpha, albedo,
  * ior_f0); 16 floats in the reference's slot layout. */
+/* Host-side fault injection for failure tests: the next `after` device allocations of the
+ * library succeed, the `count` after them fail as if HBM were full (the call that needed them
+ * returns GBPT_ERR_NO_MEMORY and leaves the context usable), then allocation is normal again;
+ * count = 0 disarms. The allocation is refused before cudaMalloc is called: no GPU is involved. */
+GBPT_API int gbpt_debug_fail_allocations(int64_t after, int64_t count);
 GBPT_API int gbpt_debug_material_samples(const gbpt_material* material, int front_facing,
                                          float ior, const float wi[3], uint32_t seed, uint32_t n,
                                          float* out_host);

@@ -48,6 +48,29 @@ double host_clock() {
 
 } // namespace gbpt
 
+namespace gbpt {
+std::mutex g_inject_mu;
+int64_t g_inject_after = 0, g_inject_count = 0; // see gbpt_debug_fail_allocations
+
+cudaError_t device_malloc(void** p, size_t bytes) {
+    {
+        std::lock_guard<std::mutex> lk(g_inject_mu);
+        if (g_inject_count > 0) {
+            if (g_inject_after > 0) {
+                --g_inject_after;
+            } else {
+                --g_inject_count;
+                *p = nullptr;
+                return cudaErrorMemoryAllocation;
+            }
+        }
+    }
+    const cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) *p = nullptr;
+    return e;
+}
+} // namespace gbpt
+
 using namespace gbpt;
 
 namespace {
@@ -57,7 +80,7 @@ int upload(void** dst, const void* src, size_t bytes, uint64_t& total) {
         *dst = nullptr;
         return GBPT_OK;
     }
-    GBPT_CUDA_CHECK(cudaMalloc(dst, bytes));
+    GBPT_CUDA_CHECK(device_malloc(dst, bytes));
     total += bytes;
     const cudaError_t e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
@@ -188,7 +211,7 @@ GBPT_API int gbpt_create(int device, uint64_t stream, gbpt_ctx** out_ctx) {
         GBPT_CUDA_CHECK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
         ctx->own_stream = true;
     }
-    GBPT_CUDA_CHECK(cudaMalloc((void**)&ctx->d_misc, 4 * sizeof(unsigned long long)));
+    GBPT_CUDA_CHECK(device_malloc((void**)&ctx->d_misc, 4 * sizeof(unsigned long long)));
     GBPT_CUDA_CHECK(cudaMemset(ctx->d_misc, 0, 4 * sizeof(unsigned long long)));
     GBPT_CUDA_CHECK(cudaEventCreate(&ctx->ev0));
     GBPT_CUDA_CHECK(cudaEventCreate(&ctx->ev1));
@@ -240,6 +263,17 @@ GBPT_API int gbpt_memory_info(gbpt_ctx* ctx, uint64_t* free_bytes, uint64_t* tot
         for (auto& kv : ctx->scenes) b += kv.second.bytes;
         *ctx_bytes = b;
     }
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_debug_fail_allocations(int64_t after, int64_t count) {
+    if (after < 0 || count < 0) {
+        set_error("gbpt_debug_fail_allocations: negative argument");
+        return GBPT_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(gbpt::g_inject_mu);
+    gbpt::g_inject_after = after;
+    gbpt::g_inject_count = count;
     return GBPT_OK;
 }
 
@@ -751,7 +785,7 @@ static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
             if (w.pix_id) cudaFree(w.pix_id);
             w.pix_id = nullptr;
             w.pix_id_cap = 0;
-            GBPT_CUDA_CHECK(cudaMalloc((void**)&w.pix_id, (size_t)p->pixel_count * 4));
+            GBPT_CUDA_CHECK(device_malloc((void**)&w.pix_id, (size_t)p->pixel_count * 4));
             w.pix_id_cap = p->pixel_count;
         }
         GBPT_CUDA_CHECK(cudaMemcpyAsync(w.pix_id, p->pixels, (size_t)p->pixel_count * 4,
@@ -763,7 +797,7 @@ static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
             if (w.out) cudaFree(w.out);
             w.out = nullptr;
             w.out_cap = 0;
-            GBPT_CUDA_CHECK(cudaMalloc((void**)&w.out, (size_t)n_pix * sizeof(float4)));
+            GBPT_CUDA_CHECK(device_malloc((void**)&w.out, (size_t)n_pix * sizeof(float4)));
             w.out_cap = n_pix;
         }
         a.out_device = w.out;
@@ -937,14 +971,14 @@ GBPT_API int gbpt_render_batch(gbpt_ctx* ctx, const gbpt_request* reqs, uint32_t
         if (w.pix_id) cudaFree(w.pix_id);
         w.pix_id = nullptr;
         w.pix_id_cap = 0;
-        GBPT_CUDA_CHECK(cudaMalloc((void**)&w.pix_id, (size_t)list_words * 4));
+        GBPT_CUDA_CHECK(device_malloc((void**)&w.pix_id, (size_t)list_words * 4));
         w.pix_id_cap = list_words;
     }
     if (host_texels > w.out_cap) {
         if (w.out) cudaFree(w.out);
         w.out = nullptr;
         w.out_cap = 0;
-        GBPT_CUDA_CHECK(cudaMalloc((void**)&w.out, (size_t)host_texels * sizeof(float4)));
+        GBPT_CUDA_CHECK(device_malloc((void**)&w.out, (size_t)host_texels * sizeof(float4)));
         w.out_cap = host_texels;
     }
     uint64_t list_at = 0, out_at = 0;
@@ -1072,7 +1106,7 @@ GBPT_API int gbpt_autotune(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam
         if (w.out) cudaFree(w.out);
         w.out = nullptr;
         w.out_cap = 0;
-        GBPT_CUDA_CHECK(cudaMalloc((void**)&w.out, (size_t)n_pix * sizeof(float4)));
+        GBPT_CUDA_CHECK(device_malloc((void**)&w.out, (size_t)n_pix * sizeof(float4)));
         w.out_cap = n_pix;
     }
     const uint64_t waves[4] = {1ull << 21, 1ull << 22, 1ull << 23, 1ull << 24};
@@ -1147,7 +1181,7 @@ GBPT_API int gbpt_debug_primary_points(gbpt_ctx* ctx, uint32_t scene, const gbpt
             if (w.pix_id) cudaFree(w.pix_id);
             w.pix_id = nullptr;
             w.pix_id_cap = 0;
-            GBPT_CUDA_CHECK(cudaMalloc((void**)&w.pix_id, (size_t)p->pixel_count * 4));
+            GBPT_CUDA_CHECK(device_malloc((void**)&w.pix_id, (size_t)p->pixel_count * 4));
             w.pix_id_cap = p->pixel_count;
         }
         GBPT_CUDA_CHECK(cudaMemcpyAsync(w.pix_id, p->pixels, (size_t)p->pixel_count * 4,
@@ -1156,7 +1190,7 @@ GBPT_API int gbpt_debug_primary_points(gbpt_ctx* ctx, uint32_t scene, const gbpt
     }
     float* d = nullptr;
     const size_t bytes = (size_t)n_pix * 24 * sizeof(float);
-    GBPT_CUDA_CHECK(cudaMalloc((void**)&d, bytes));
+    GBPT_CUDA_CHECK(device_malloc((void**)&d, bytes));
     rc = primary_points(it->second, w, a, ctx->stream, d);
     if (rc == GBPT_OK) {
         const cudaError_t e = cudaMemcpyAsync(out_host, d, bytes, cudaMemcpyDeviceToHost, ctx->stream);
@@ -1191,7 +1225,7 @@ GBPT_API int gbpt_trace_primary(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera
         if (ctx->d_hits) cudaFree(ctx->d_hits);
         ctx->d_hits = nullptr;
         ctx->hits_cap = 0;
-        GBPT_CUDA_CHECK(cudaMalloc((void**)&ctx->d_hits, n * sizeof(gbpt_hit)));
+        GBPT_CUDA_CHECK(device_malloc((void**)&ctx->d_hits, n * sizeof(gbpt_hit)));
         ctx->hits_cap = n;
     }
     rc = trace_primary(it->second, *camera, width, height, instance_mask, ctx->d_hits,

@@ -77,7 +77,7 @@ struct Buffer {
         height = h;
         floats = fl;
         const size_t bytes = (size_t)w * h * fl * sizeof(float);
-        if (bytes && cudaMalloc(&dev, bytes) != cudaSuccess) {
+        if (bytes && device_malloc(&dev, bytes) != cudaSuccess) {
             dev = nullptr;
             throw std::bad_alloc();
         }
@@ -133,6 +133,9 @@ class Node {
         if (obj.type != Json::Obj) throw NodeError(type_ + ": properties must be a JSON object");
         std::vector<std::pair<Prop*, const Json*>> todo;
         collect(obj, prefix, warnings, todo);
+        static const Json kInf = jnum(INFINITY);
+        for (auto& t : todo) // JSON has no infinity: null reads as +inf for a number property
+            if (t.first->kind == Prop::Float && t.second->type == Json::Null) t.second = &kInf;
         for (auto& t : todo) {
             check_type(*t.first, *t.second);
             validate(t.first->key, *t.second);
@@ -186,6 +189,11 @@ class Node {
         auto it = outs_.find(name);
         return it == outs_.end() ? nullptr : it->second.get();
     }
+    // Checkpoint of what the node carries from one iteration to the next: counters in the
+    // returned JSON, images as files `base` + suffix. load_state takes them back before the next
+    // connect.
+    virtual Json save_state(gbpt_ctx*, const std::string&) { return Json(); }
+    virtual void load_state(const Json&, const std::string&) {}
 
   protected:
     void add(Prop::Kind k, const std::string& key, Json def, std::vector<std::string> opts = {},
@@ -463,6 +471,70 @@ class AccumulateNode : public Node {
         if (o.width != src->width || o.height != src->height) clear_ = true;
         o.allocate(src->width, src->height, 4);
         out("history").allocate(src->width, src->height, 1);
+        if (!pending_out_.empty()) {
+            if (pending_w_ != src->width || pending_h_ != src->height)
+                throw NodeError(type() + ": the checkpoint's extent differs from the input's");
+            if (cudaMemcpy(o.dev, pending_out_.data(), pending_out_.size() * sizeof(float),
+                           cudaMemcpyHostToDevice) != cudaSuccess ||
+                cudaMemcpy(out("history").dev, pending_hist_.data(),
+                           pending_hist_.size() * sizeof(float),
+                           cudaMemcpyHostToDevice) != cudaSuccess)
+                throw NodeError(type() + ": restoring the checkpoint failed");
+            pending_out_.clear();
+            pending_hist_.clear();
+            clear_ = pending_clear_;
+        }
+    }
+    // The accumulated image as two 3-channel PFM files (exact float32): base.rgb.pfm = out.rgb,
+    // base.aux.pfm = (out.a, history, 0).
+    Json save_state(gbpt_ctx* ctx, const std::string& base) override {
+        Json st;
+        st.type = Json::Obj;
+        st.o.emplace_back("clear", jbool(clear_));
+        Buffer* o = output("out");
+        if (!o || !o->dev || !ctx) return st;
+        std::vector<float> img(o->texels() * 4), hist(o->texels());
+        check_rc(gbpt_synchronize(ctx));
+        if (cudaMemcpy(img.data(), o->dev, img.size() * sizeof(float), cudaMemcpyDeviceToHost) !=
+                cudaSuccess ||
+            cudaMemcpy(hist.data(), output("history")->dev, hist.size() * sizeof(float),
+                       cudaMemcpyDeviceToHost) != cudaSuccess)
+            throw NodeError(type() + ": reading the accumulator failed");
+        std::vector<float> aux(o->texels() * 3, 0.0f);
+        for (uint64_t t = 0; t < o->texels(); ++t) {
+            aux[3 * t] = img[4 * t + 3];
+            aux[3 * t + 1] = hist[t];
+        }
+        check_rc(gbpt_image_write_pfm((base + ".rgb.pfm").c_str(), img.data(), o->width,
+                                      o->height, 4));
+        check_rc(gbpt_image_write_pfm((base + ".aux.pfm").c_str(), aux.data(), o->width,
+                                      o->height, 3));
+        st.o.emplace_back("width", jnum(o->width));
+        st.o.emplace_back("height", jnum(o->height));
+        return st;
+    }
+    void load_state(const Json& st, const std::string& base) override {
+        if (st.type != Json::Obj) return;
+        const Json* w = st.get("width");
+        pending_clear_ = st.get("clear") && st.get("clear")->b;
+        clear_ = pending_clear_;
+        if (!w) return;
+        uint32_t pw = 0, ph = 0;
+        check_rc(gbpt_image_read_pfm((base + ".rgb.pfm").c_str(), nullptr, 4, &pw, &ph));
+        std::vector<float> rgb((size_t)pw * ph * 4), aux((size_t)pw * ph * 3);
+        check_rc(gbpt_image_read_pfm((base + ".rgb.pfm").c_str(), rgb.data(), 4, &pw, &ph));
+        uint32_t aw = 0, ah = 0;
+        check_rc(gbpt_image_read_pfm((base + ".aux.pfm").c_str(), nullptr, 3, &aw, &ah));
+        if (aw != pw || ah != ph) throw NodeError(type() + ": checkpoint images differ in size");
+        check_rc(gbpt_image_read_pfm((base + ".aux.pfm").c_str(), aux.data(), 3, &aw, &ah));
+        pending_hist_.assign((size_t)pw * ph, 0.0f);
+        for (size_t t = 0; t < pending_hist_.size(); ++t) {
+            rgb[4 * t + 3] = aux[3 * t];
+            pending_hist_[t] = aux[3 * t + 1];
+        }
+        pending_out_ = std::move(rgb);
+        pending_w_ = pw;
+        pending_h_ = ph;
     }
     void process(gbpt_ctx* ctx, uint32_t, const gbpt_camera*, uint64_t iteration,
                  const std::map<std::string, const Buffer*>& in,
@@ -478,6 +550,9 @@ class AccumulateNode : public Node {
 
   private:
     bool clear_ = true;
+    bool pending_clear_ = false;
+    std::vector<float> pending_out_, pending_hist_;
+    uint32_t pending_w_ = 0, pending_h_ = 0;
 };
 
 // ---- Image Write -------------------------------------------------------------------------------
@@ -593,6 +668,33 @@ class ImageWriteNode : public Node {
         const int64_t it = i("iteration");
         const int64_t next = recording ? it * i("iteration power") + i("iteration offset") : it;
         set("iteration", jnum((double)next));
+    }
+
+    Json save_state(gbpt_ctx*, const std::string&) override {
+        Json st;
+        st.type = Json::Obj;
+        st.o.emplace_back("recording", jbool(b("enable")));
+        st.o.emplace_back("record_next", jbool(record_next_));
+        st.o.emplace_back("start_stop", jbool(start_stop_));
+        st.o.emplace_back("iteration", jnum((double)iteration_));
+        st.o.emplace_back("captures_since_record", jnum((double)captures_since_record_));
+        st.o.emplace_back("captures_total", jnum((double)captures_total_));
+        st.o.emplace_back("iteration_at_start", jnum((double)iteration_at_start_));
+        return st;
+    }
+    void load_state(const Json& st, const std::string&) override {
+        if (st.type != Json::Obj) return;
+        auto num = [&](const char* k, int64_t def) { return (int64_t)st.num(k, (double)def); };
+        const Json* rec = st.get("recording");
+        set("enable", jbool(rec && rec->b));
+        const Json* rn = st.get("record_next");
+        const Json* ss = st.get("start_stop");
+        record_next_ = rn && rn->b;
+        start_stop_ = ss && ss->b;
+        iteration_ = num("iteration", 0);
+        captures_since_record_ = num("captures_since_record", 0);
+        captures_total_ = num("captures_total", 0);
+        iteration_at_start_ = num("iteration_at_start", 1);
     }
 
   private:
@@ -775,6 +877,22 @@ class ErrorPlotNode : public Node {
         history_.push_back(e);
         while (history_.size() > (size_t)i("History")) history_.erase(history_.begin());
         publish();
+    }
+
+    Json save_state(gbpt_ctx*, const std::string&) override {
+        Json st;
+        st.type = Json::Arr;
+        for (const auto& h : history_)
+            for (int c = 0; c < 4; ++c) st.a.push_back(jnum(h.v[c]));
+        return st;
+    }
+    void load_state(const Json& st, const std::string&) override {
+        history_.clear();
+        for (size_t k = 0; k + 3 < st.size(); k += 4) {
+            Rgba r;
+            for (int c = 0; c < 4; ++c) r.v[c] = (float)st.a[k + c].n;
+            history_.push_back(r);
+        }
     }
 
   private:
@@ -1109,6 +1227,77 @@ GBPT_API int gbpt_graph_run(gbpt_graph* graph, uint32_t scene, const gbpt_camera
             for (const auto& name : graph->order)
                 graph->nodes[name]->process(graph->ctx, scene, camera, graph->iteration,
                                             graph->inputs_of(name), graph->warnings);
+        return GBPT_OK;
+    });
+}
+
+GBPT_API int gbpt_graph_save(gbpt_graph* graph, const char* directory) {
+    if (!graph || !directory) return fail("gbpt_graph_save: null argument");
+    if (graph->ctx) {
+        int rc = check_ctx(graph->ctx);
+        if (rc) return rc;
+    }
+    return guarded("gbpt_graph_save", [&]() -> int {
+        const std::string dir = directory;
+        mkdir(dir.c_str(), 0777);
+        Json root;
+        root.type = Json::Obj;
+        root.o.emplace_back("iteration", jnum((double)graph->iteration));
+        Json nodes;
+        nodes.type = Json::Obj;
+        for (const auto& name : graph->order) {
+            Node& n = *graph->nodes[name];
+            Json e;
+            e.type = Json::Obj;
+            e.o.emplace_back("type", jstr(n.type()));
+            e.o.emplace_back("properties", n.all_properties());
+            e.o.emplace_back("state", n.save_state(graph->ctx, dir + "/" + name));
+            nodes.o.emplace_back(name, std::move(e));
+        }
+        root.o.emplace_back("nodes", std::move(nodes));
+        std::string text;
+        dump_json(root, text);
+        const std::string path = dir + "/graph_state.json";
+        FILE* f = std::fopen(path.c_str(), "wb");
+        if (!f) throw NodeError("cannot write " + path);
+        const bool ok = std::fwrite(text.data(), 1, text.size(), f) == text.size();
+        if (std::fclose(f) != 0 || !ok) throw NodeError("cannot write " + path);
+        return GBPT_OK;
+    });
+}
+
+GBPT_API int gbpt_graph_load(gbpt_graph* graph, const char* directory) {
+    if (!graph || !directory) return fail("gbpt_graph_load: null argument");
+    return guarded("gbpt_graph_load", [&]() -> int {
+        const std::string dir = directory;
+        const std::string path = dir + "/graph_state.json";
+        FILE* f = std::fopen(path.c_str(), "rb");
+        if (!f) throw NodeError("cannot read " + path);
+        std::string text;
+        char buf[65536];
+        size_t n;
+        while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, n);
+        std::fclose(f);
+        Json root;
+        std::string err;
+        if (!parse_json(text, root, err)) throw NodeError(path + ": " + err);
+        const Json* nodes = root.get("nodes");
+        if (!nodes || nodes->type != Json::Obj) throw NodeError(path + ": no \"nodes\"");
+        for (const auto& kv : nodes->o) {
+            Node* node = find_node(graph, kv.first.c_str());
+            if (!node || node->type() != kv.second.str("type", ""))
+                throw NodeError(path + ": node \"" + kv.first + "\" is not in this graph");
+        }
+        for (const auto& kv : nodes->o) {
+            Node* node = find_node(graph, kv.first.c_str());
+            std::vector<std::string> unknown;
+            if (const Json* props = kv.second.get("properties"))
+                node->set_properties(*props, unknown);
+            const Json* st = kv.second.get("state");
+            node->load_state(st ? *st : Json(), dir + "/" + kv.first);
+        }
+        graph->iteration = (uint64_t)root.num("iteration", 0.0);
+        graph->connected = false;
         return GBPT_OK;
     });
 }

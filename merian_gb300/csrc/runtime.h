@@ -56,6 +56,10 @@ struct SceneGPU {
 };
 
 // Work buffers of the wavefront, grown on demand and kept for the context's lifetime.
+// cudaMalloc behind the host-side fault injection of gbpt_debug_fail_allocations (api.cpp). On
+// failure *p is null.
+cudaError_t device_malloc(void** p, size_t bytes);
+
 struct Work {
     uint64_t path_cap = 0;  // paths per wave
     uint64_t pixel_cap = 0; // pixels per wave
@@ -93,6 +97,9 @@ struct Work {
     void* tables = nullptr;
     uint64_t tables_bytes = 0;
     uint64_t bytes = 0;
+    // changes (to a value never used before, process-wide) whenever a buffer is (re)allocated:
+    // CUDA graphs captured over older buffers are then recaptured
+    uint64_t generation = 0;
 };
 
 // One request of a batch: a scene, a camera, the render parameters and a device output of
@@ -155,8 +162,7 @@ struct TickEngine {
         uint64_t launches;
     };
     std::vector<Graph> graphs;
-    const void* graph_work = nullptr; // the buffers the graphs were captured with
-    const void* graph_tables = nullptr;
+    uint64_t graph_generation = 0; // Work::generation the graphs were captured with
     std::vector<unsigned char> stage;
     std::vector<const SceneGPU*> scene_ptrs;
     int grids[7] = {0, 0, 0, 0, 0, 0, 0}; // launch grids, computed at the first tick

@@ -405,7 +405,7 @@ GBPT_API int gbpt_server_start(gbpt_ctx* ctx, const gbpt_server_config* cfg) {
     s->arena_bytes = align_up(s->arena_bytes);
     GBPT_CUDA_CHECK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     GBPT_CUDA_CHECK(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
-    GBPT_CUDA_CHECK(cudaMalloc((void**)&s->arena, s->arena_bytes));
+    GBPT_CUDA_CHECK(device_malloc((void**)&s->arena, s->arena_bytes));
     s->alloc.reset(s->arena_bytes);
     GBPT_CUDA_CHECK(cudaHostAlloc((void**)&s->h_flags, kTicksAhead * sizeof(uint32_t),
                                   cudaHostAllocDefault));

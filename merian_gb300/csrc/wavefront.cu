@@ -17,6 +17,7 @@
 #include "device_shading.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -569,9 +570,20 @@ __global__ void __launch_bounds__(128) k_finalize(TickArgs t) {
     }
 }
 
+std::atomic<uint64_t> g_generation{0};
+void new_generation(Work& w) { w.generation = ++g_generation; }
+
+// On failure p is null (never a stale address).
 template <class T> cudaError_t alloc(T*& p, uint64_t n, uint64_t& bytes) {
     bytes += n * sizeof(T);
-    return cudaMalloc((void**)&p, n * sizeof(T) + 16);
+    void* q = nullptr;
+    const cudaError_t e = device_malloc(&q, n * sizeof(T) + 16);
+    p = e == cudaSuccess ? (T*)q : nullptr;
+    return e;
+}
+template <class T> void release(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
 }
 
 ReqGPU to_req(const BatchItem& it, uint32_t scene_index) {
@@ -631,20 +643,41 @@ void work_free(Work& w) {
 
 int work_reserve(Work& w, uint64_t paths, uint64_t pixels) {
     if (w.fixed) return (paths <= w.path_cap && pixels <= w.pixel_cap) ? GBPT_OK : GBPT_ERR_NO_MEMORY;
-    if (!w.counters) {
+    if (!w.counters || !w.stats) {
         uint64_t b = 0;
-        if (alloc(w.counters, 16, b) != cudaSuccess) return GBPT_ERR_NO_MEMORY;
-        if (alloc(w.stats, 8, b) != cudaSuccess) return GBPT_ERR_NO_MEMORY;
+        release(w.counters);
+        release(w.stats);
+        if (alloc(w.counters, 16, b) != cudaSuccess || alloc(w.stats, 8, b) != cudaSuccess) {
+            release(w.counters);
+            release(w.stats);
+            return GBPT_ERR_NO_MEMORY;
+        }
+        new_generation(w);
         cudaMemset(w.counters, 0, 16 * sizeof(uint32_t));
         cudaMemset(w.stats, 0, 8 * sizeof(unsigned long long));
         w.bytes += b;
     }
     if (paths > w.path_cap) {
-        void* old[] = {w.thr, w.rad, w.rng, w.q_od[0], w.q_od[1], w.q_path[0], w.q_path[1],
-                       w.hit_tuv, w.hit_geom, w.hit_inst, w.s_od, w.s_contrib, w.s_path,
-                       w.keys, w.perm};
-        for (void* p : old)
-            if (p) cudaFree(p);
+        auto release_paths = [&w]() {
+            release(w.thr);
+            release(w.rad);
+            release(w.rng);
+            release(w.q_od[0]);
+            release(w.q_od[1]);
+            release(w.q_path[0]);
+            release(w.q_path[1]);
+            release(w.hit_tuv);
+            release(w.hit_geom);
+            release(w.hit_inst);
+            release(w.s_od);
+            release(w.s_contrib);
+            release(w.s_path);
+            release(w.keys);
+            release(w.perm);
+            w.path_cap = 0;
+        };
+        release_paths();
+        new_generation(w);
         uint64_t b = 0;
         bool ok = alloc(w.thr, paths, b) == cudaSuccess && alloc(w.rad, paths, b) == cudaSuccess &&
                   alloc(w.rng, paths, b) == cudaSuccess &&
@@ -660,14 +693,16 @@ int work_reserve(Work& w, uint64_t paths, uint64_t pixels) {
                   alloc(w.s_path, paths, b) == cudaSuccess &&
                   alloc(w.keys, paths, b) == cudaSuccess && alloc(w.perm, paths, b) == cudaSuccess;
         if (!ok) {
-            w.path_cap = 0;
+            release_paths();
             return GBPT_ERR_NO_MEMORY;
         }
         w.path_cap = paths;
         w.bytes += b;
     }
     if (pixels > w.pixel_cap) {
-        if (w.pix) cudaFree(w.pix);
+        release(w.pix);
+        w.pixel_cap = 0;
+        new_generation(w);
         uint64_t b = 0;
         if (alloc(w.pix, kPixFloat4 * pixels, b) != cudaSuccess) return GBPT_ERR_NO_MEMORY;
         w.pixel_cap = pixels;
@@ -709,7 +744,11 @@ int tables_reserve(Work& w, uint64_t need) {
     w.tables = nullptr;
     w.tables_bytes = 0;
     const uint64_t cap = std::max<uint64_t>(need + need / 2, 64 << 10);
-    if (cudaMalloc(&w.tables, cap) != cudaSuccess) return GBPT_ERR_NO_MEMORY;
+    new_generation(w);
+    if (device_malloc(&w.tables, cap) != cudaSuccess) {
+        w.tables = nullptr;
+        return GBPT_ERR_NO_MEMORY;
+    }
     w.tables_bytes = cap;
     w.bytes += cap;
     return GBPT_OK;
@@ -883,8 +922,7 @@ void Profile::destroy() {
 void TickEngine::release() {
     for (const Graph& g : graphs) cudaGraphExecDestroy(g.exec);
     graphs.clear();
-    graph_work = nullptr;
-    graph_tables = nullptr;
+    graph_generation = 0;
 }
 
 int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64_t* n_paths,
@@ -981,10 +1019,9 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
     std::memcpy(&grids, e.grids, sizeof(grids));
     uint64_t nl = 0;
     if (graph) {
-        if (e.graph_work != (const void*)w.thr || e.graph_tables != w.tables) {
+        if (e.graph_generation != w.generation) {
             e.release();
-            e.graph_work = w.thr;
-            e.graph_tables = w.tables;
+            e.graph_generation = w.generation;
         }
         const uint32_t shape =
             tp.max_len * 16u + (tp.nee ? 1u : 0u) + (tp.sort ? 2u : 0u) + (tp.two_level ? 4u : 0u) +

@@ -109,6 +109,15 @@ class Graph:
         N.check(self.lib.gbpt_graph_run(self.handle, scene_id, cam, int(extent[0]),
                                         int(extent[1]), iterations))
 
+    def save(self, directory: str | Path) -> None:
+        """Checkpoint: iteration count, node properties and counters, accumulated images."""
+        Path(directory).mkdir(parents=True, exist_ok=True)
+        N.check(self.lib.gbpt_graph_save(self.handle, str(directory).encode()))
+
+    def load(self, directory: str | Path) -> None:
+        """Resume from a checkpoint of a graph made from the same JSON."""
+        N.check(self.lib.gbpt_graph_load(self.handle, str(directory).encode()))
+
     def output(self, connector: str) -> np.ndarray:
         """The output "node.output" as a host array (height, width, floats per texel)."""
         w, h, f = C.c_uint32(), C.c_uint32(), C.c_uint32()

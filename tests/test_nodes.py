@@ -297,3 +297,62 @@ def test_graph_scene_file_node(gpu_ctx, tmp_path):
     with node.Graph(gpu_ctx, cfg) as g:
         with pytest.raises(N.GbptError):
             g.run(0, None, (72, 48))
+
+
+def test_graph_checkpoint_properties(native, tmp_path):
+    """A checkpoint of a graph without a context carries the iteration count and every property
+    (infinity as null) into a graph made from the same JSON."""
+    from merian_gb300 import _native as N
+    from merian_gb300 import node
+    g = node.Graph(None, PT_JSON)
+    g.set_property("render", "samples per pixel", 7)
+    g.set_property("accumulate", "max history", 32)
+    g.set_property("write", "advanced/stop at run", 9)
+    g.save(tmp_path / "ck")
+    state = (tmp_path / "ck" / "graph_state.json").read_text()
+    assert '"iteration":0' in state
+    h = node.Graph(None, PT_JSON)
+    h.load(tmp_path / "ck")
+    for name in ("render", "accumulate", "write"):
+        assert h.properties(name) == g.properties(name)
+    other = node.Graph(None, {"nodes": {"render": {"type": "Accumulate"}}})
+    with pytest.raises(N.GbptError):
+        other.load(tmp_path / "ck")
+    with pytest.raises(N.GbptError):
+        h.load(tmp_path / "missing")
+
+
+@pytest.mark.gpu
+def test_graph_checkpoint_resume(gpu_ctx, tmp_path):
+    """Render -> Accumulate for 6 iterations equals 3 iterations, a checkpoint, a new graph
+    loading it, and 3 more iterations, bit for bit (frame seeds continue from the iteration
+    count; the accumulator and its history are restored exactly)."""
+    from merian_gb300 import node
+    from merian_gb300 import scene as S
+    sid = gpu_ctx.upload(S.cornell())
+    cam = S.workload_camera("cornell-256-16spp")
+    cfg = {"nodes": {
+        "render": {"type": "Render (Path-traced)", "outputs": ["irradiance->accumulate.src"],
+                   "properties": {"samples per pixel": 1, "seed": 5}},
+        "accumulate": {"type": "Accumulate", "outputs": ["out->plot.input"],
+                       "properties": {"alpha": 1.0, "inf history": True}},
+        "gt": {"type": "Render (Path-traced)", "outputs": ["irradiance->plot.reference"],
+               "properties": {"samples per pixel": 4}},
+        "plot": {"type": "Error Plot", "properties": {"Metric": "RMSE"}}}}
+    try:
+        with node.Graph(gpu_ctx, cfg) as g:
+            g.run(sid, cam, (40, 24), iterations=6)
+            full = g.output("accumulate.out")
+            full_hist = g.output("plot.history")
+        with node.Graph(gpu_ctx, cfg) as g:
+            g.run(sid, cam, (40, 24), iterations=3)
+            g.save(tmp_path / "ck")
+        with node.Graph(gpu_ctx, cfg) as g:
+            g.load(tmp_path / "ck")
+            g.run(sid, cam, (40, 24), iterations=3)
+            resumed = g.output("accumulate.out")
+            assert np.all(g.output("accumulate.history") == 6)
+            assert np.array_equal(g.output("plot.history"), full_hist)
+        assert np.array_equal(resumed.view(np.uint32), full.view(np.uint32))
+    finally:
+        gpu_ctx.destroy_scene(sid)
