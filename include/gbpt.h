@@ -448,6 +448,13 @@ GBPT_API uint32_t gbpt_graph_warning_count(const gbpt_graph* graph);
 GBPT_API const char* gbpt_graph_warning(const gbpt_graph* graph, uint32_t index);
 GBPT_API int gbpt_graph_set_property(gbpt_graph* graph, const char* node, const char* key,
                                      const char* json_value, uint32_t* out_flags);
+/* The graph JSON's "cli" options (merian-graph-run, main.cpp:31-51): each names a JSON pointer
+ * "/nodes/<node>/properties/<key>"; setting an option sets that property. Options whose pointer
+ * names no property of an enabled node are dropped with a warning. */
+GBPT_API int gbpt_graph_option(const gbpt_graph* graph, uint32_t index, const char** name,
+                               const char** pointer);
+GBPT_API int gbpt_graph_set_option(gbpt_graph* graph, const char* option, const char* json_value,
+                                   uint32_t* out_flags);
 /* key = NULL: every property of the node as one JSON object. length = the text's size. */
 GBPT_API int gbpt_graph_get_property(const gbpt_graph* graph, const char* node, const char* key,
                                      char* json_out, uint64_t capacity, uint64_t* length);

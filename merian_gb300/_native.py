@@ -242,6 +242,10 @@ EXPORTS = [
     ("gbpt_graph_run", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.c_uint32,
                                  C.c_uint32, C.c_uint32]),
     ("gbpt_debug_fail_allocations", C.c_int, [C.c_int64, C.c_int64]),
+    ("gbpt_graph_option", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_char_p),
+                                    C.POINTER(C.c_char_p)]),
+    ("gbpt_graph_set_option", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p,
+                                        C.POINTER(C.c_uint32)]),
     ("gbpt_graph_save", C.c_int, [C.c_void_p, C.c_char_p]),
     ("gbpt_graph_load", C.c_int, [C.c_void_p, C.c_char_p]),
     ("gbpt_graph_output", C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_uint64,

@@ -993,6 +993,12 @@ struct gbpt_graph {
     std::vector<std::string> order; // dependency order, ties by name
     std::vector<Edge> edges;
     std::vector<std::string> warnings;
+    // the graph JSON's "cli" options (main.cpp:31-51): option name -> JSON pointer, and the node
+    // and property key ("group/key") the pointer addresses
+    struct Option {
+        std::string name, pointer, node, key;
+    };
+    std::vector<Option> options;
     bool connected = false;
     uint32_t width = 0, height = 0; // the extent of the last connect
     uint64_t iteration = 0;         // graph iterations run so far
@@ -1115,6 +1121,37 @@ GBPT_API int gbpt_graph_create(gbpt_ctx* ctx, const char* graph_json, gbpt_graph
                     throw NodeError("input \"" + e.dst + "." + e.input + "\" connected twice");
             g->edges.push_back(e);
         }
+        if (const Json* cli = root.get("cli")) {
+            for (const auto& kv : cli->o) {
+                const std::string ptr = kv.second.str("pointer", "");
+                // RFC 6901 tokens: "~1" is "/", "~0" is "~"
+                std::vector<std::string> tok;
+                for (size_t at = 0; at < ptr.size() && ptr[at] == '/';) {
+                    const size_t next = ptr.find('/', at + 1);
+                    std::string t = ptr.substr(at + 1, next == std::string::npos ? std::string::npos
+                                                                                  : next - at - 1);
+                    for (size_t q; (q = t.find("~1")) != std::string::npos;) t.replace(q, 2, "/");
+                    for (size_t q; (q = t.find("~0")) != std::string::npos;) t.replace(q, 2, "~");
+                    tok.push_back(t);
+                    if (next == std::string::npos) break;
+                    at = next;
+                }
+                if (tok.size() < 4 || tok[0] != "nodes" || tok[2] != "properties" ||
+                    !g->nodes.count(tok[1])) {
+                    g->warnings.push_back("cli option \"" + kv.first + "\": pointer \"" + ptr +
+                                          "\" does not name a property of an enabled node");
+                    continue;
+                }
+                std::string key = tok[3];
+                for (size_t k = 4; k < tok.size(); ++k) key += "/" + tok[k];
+                if (!g->nodes[tok[1]]->prop(key)) {
+                    g->warnings.push_back("cli option \"" + kv.first + "\": node \"" + tok[1] +
+                                          "\" has no property \"" + key + "\"");
+                    continue;
+                }
+                g->options.push_back({kv.first, ptr, tok[1], key});
+            }
+        }
         topological(*g);
         *out_graph = g.release();
         return GBPT_OK;
@@ -1182,6 +1219,27 @@ GBPT_API int gbpt_graph_set_property(gbpt_graph* graph, const char* node, const 
         if (out_flags) *out_flags = flags;
         return GBPT_OK;
     });
+}
+
+GBPT_API int gbpt_graph_option(const gbpt_graph* graph, uint32_t index, const char** name,
+                               const char** pointer) {
+    if (!graph) return fail("gbpt_graph_option: null graph");
+    if (index >= graph->options.size()) return fail("gbpt_graph_option: no such option",
+                                                    GBPT_ERR_NOT_FOUND);
+    if (name) *name = graph->options[index].name.c_str();
+    if (pointer) *pointer = graph->options[index].pointer.c_str();
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_graph_set_option(gbpt_graph* graph, const char* option, const char* json_value,
+                                   uint32_t* out_flags) {
+    if (!graph || !option) return fail("gbpt_graph_set_option: null argument");
+    for (const auto& o : graph->options)
+        if (o.name == option)
+            return gbpt_graph_set_property(graph, o.node.c_str(), o.key.c_str(), json_value,
+                                           out_flags);
+    return fail(std::string("gbpt_graph_set_option: no option \"") + option + "\"",
+                GBPT_ERR_NOT_FOUND);
 }
 
 GBPT_API int gbpt_graph_get_property(const gbpt_graph* graph, const char* node, const char* key,

@@ -109,6 +109,23 @@ class Graph:
         N.check(self.lib.gbpt_graph_run(self.handle, scene_id, cam, int(extent[0]),
                                         int(extent[1]), iterations))
 
+    @property
+    def options(self) -> dict[str, str]:
+        """The graph JSON's "cli" options: name -> JSON pointer of the property it sets."""
+        out, i = {}, 0
+        while True:
+            name, ptr = C.c_char_p(), C.c_char_p()
+            if self.lib.gbpt_graph_option(self.handle, i, C.byref(name), C.byref(ptr)) != 0:
+                return out
+            out[name.value.decode()] = ptr.value.decode()
+            i += 1
+
+    def set_option(self, name: str, value) -> int:
+        flags = C.c_uint32()
+        N.check(self.lib.gbpt_graph_set_option(self.handle, name.encode(),
+                                               json.dumps(value).encode(), C.byref(flags)))
+        return flags.value
+
     def save(self, directory: str | Path) -> None:
         """Checkpoint: iteration count, node properties and counters, accumulated images."""
         Path(directory).mkdir(parents=True, exist_ok=True)

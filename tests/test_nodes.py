@@ -356,3 +356,28 @@ def test_graph_checkpoint_resume(gpu_ctx, tmp_path):
         assert np.array_equal(resumed.view(np.uint32), full.view(np.uint32))
     finally:
         gpu_ctx.destroy_scene(sid)
+
+
+def test_graph_cli_options(native):
+    """pt.json's "cli" section: options name JSON pointers to node properties (RFC 6901
+    escapes); setting one sets the property; pointers to nothing are dropped with a warning."""
+    from merian_gb300 import _native as N
+    from merian_gb300 import node
+    cfg = dict(PT_JSON)
+    cfg["cli"] = {"max-path-length": {"pointer": "/nodes/render/properties/max path length"},
+                  "spp": {"pointer": "/nodes/render/properties/samples per pixel"},
+                  "stop": {"pointer": "/nodes/write/properties/advanced/stop at run"},
+                  "bad": {"pointer": "/nodes/nope/properties/x"}}
+    g = node.Graph(None, cfg)
+    assert set(g.options) == {"max-path-length", "spp", "stop"}
+    assert len(g.warnings) == 1 and "bad" in g.warnings[0]
+    g.set_option("spp", 16)
+    g.set_option("max-path-length", 9)
+    g.set_option("stop", 3)
+    assert g.properties("render", "samples per pixel") == 16
+    assert g.properties("render", "max path length") == 9
+    assert g.properties("write")["advanced"]["stop at run"] == 3
+    with pytest.raises(N.GbptError):
+        g.set_option("nope", 1)
+    with pytest.raises(N.GbptError):
+        g.set_option("spp", "many")
