@@ -464,6 +464,10 @@ GBPT_API int gbpt_graph_get_property(const gbpt_graph* graph, const char* node, 
  * without a GBuffer input. */
 GBPT_API int gbpt_graph_run(gbpt_graph* graph, uint32_t scene, const gbpt_camera* camera,
                             uint32_t width, uint32_t height, uint32_t iterations);
+/* The graph as a graph JSON in merian's layout (graph_load_store.cpp): "cli", then every node
+ * with "enabled", "outputs", all "properties" and "type"; it loads back into the same graph. */
+GBPT_API int gbpt_graph_to_json(const gbpt_graph* graph, char* json_out, uint64_t capacity,
+                                uint64_t* length);
 /* Checkpoint / resume of a progressive render: gbpt_graph_save writes directory/
  * graph_state.json (the iteration count, every node's properties and counters) and each
  * Accumulate node's image as PFM files (node.rgb.pfm = rgb, node.aux.pfm = (alpha, history, 0),

@@ -246,6 +246,7 @@ EXPORTS = [
                                     C.POINTER(C.c_char_p)]),
     ("gbpt_graph_set_option", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p,
                                         C.POINTER(C.c_uint32)]),
+    ("gbpt_graph_to_json", C.c_int, [C.c_void_p, C.c_char_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     ("gbpt_graph_save", C.c_int, [C.c_void_p, C.c_char_p]),
     ("gbpt_graph_load", C.c_int, [C.c_void_p, C.c_char_p]),
     ("gbpt_graph_output", C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_uint64,

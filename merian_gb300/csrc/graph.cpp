@@ -1289,6 +1289,53 @@ GBPT_API int gbpt_graph_run(gbpt_graph* graph, uint32_t scene, const gbpt_camera
     });
 }
 
+GBPT_API int gbpt_graph_to_json(const gbpt_graph* graph, char* json_out, uint64_t capacity,
+                                uint64_t* length) {
+    if (!graph) return fail("gbpt_graph_to_json: null graph");
+    // merian's layout (graph_load_store.cpp): "cli", then "nodes" by name with "enabled",
+    // "outputs" ("output->node.input"), "properties" and "type"
+    Json root;
+    root.type = Json::Obj;
+    if (!graph->options.empty()) {
+        Json cli;
+        cli.type = Json::Obj;
+        for (const auto& o : graph->options) {
+            Json e;
+            e.type = Json::Obj;
+            e.o.emplace_back("pointer", jstr(o.pointer));
+            cli.o.emplace_back(o.name, std::move(e));
+        }
+        root.o.emplace_back("cli", std::move(cli));
+    }
+    Json nodes;
+    nodes.type = Json::Obj;
+    for (const auto& kv : graph->nodes) {
+        Json e;
+        e.type = Json::Obj;
+        e.o.emplace_back("enabled", jbool(true));
+        Json outs;
+        outs.type = Json::Arr;
+        for (const auto& ed : graph->edges)
+            if (ed.src == kv.first)
+                outs.a.push_back(jstr(ed.output + "->" + ed.dst + "." + ed.input));
+        e.o.emplace_back("outputs", std::move(outs));
+        e.o.emplace_back("properties", kv.second->all_properties());
+        e.o.emplace_back("type", jstr(kv.second->type()));
+        nodes.o.emplace_back(kv.first, std::move(e));
+    }
+    root.o.emplace_back("nodes", std::move(nodes));
+    std::string text;
+    dump_json(root, text);
+    if (length) *length = text.size();
+    if (json_out && capacity) {
+        const size_t c = std::min<size_t>(text.size(), capacity - 1);
+        std::memcpy(json_out, text.data(), c);
+        json_out[c] = '\0';
+        if (c < text.size()) return fail("gbpt_graph_to_json: buffer too small");
+    }
+    return GBPT_OK;
+}
+
 GBPT_API int gbpt_graph_save(gbpt_graph* graph, const char* directory) {
     if (!graph || !directory) return fail("gbpt_graph_save: null argument");
     if (graph->ctx) {

@@ -126,6 +126,14 @@ class Graph:
                                                json.dumps(value).encode(), C.byref(flags)))
         return flags.value
 
+    def to_json(self) -> dict:
+        """The graph in merian's graph-JSON layout, every property included."""
+        n = C.c_uint64()
+        N.check(self.lib.gbpt_graph_to_json(self.handle, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value + 1)
+        N.check(self.lib.gbpt_graph_to_json(self.handle, buf, n.value + 1, None))
+        return json.loads(buf.value.decode())
+
     def save(self, directory: str | Path) -> None:
         """Checkpoint: iteration count, node properties and counters, accumulated images."""
         Path(directory).mkdir(parents=True, exist_ok=True)

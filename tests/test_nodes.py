@@ -381,3 +381,20 @@ def test_graph_cli_options(native):
         g.set_option("nope", 1)
     with pytest.raises(N.GbptError):
         g.set_option("spp", "many")
+
+
+def test_graph_json_round_trip(native):
+    """Load -> store -> load gives the same graph (as merian's graph_load_store tests check):
+    the stored JSON holds every property with its value, the edges and the cli options."""
+    from merian_gb300 import node
+    cfg = dict(PT_JSON)
+    cfg["cli"] = {"spp": {"pointer": "/nodes/render/properties/samples per pixel"}}
+    g = node.Graph(None, cfg)
+    g.set_property("render", "seed", 11)
+    stored = g.to_json()
+    assert stored["cli"] == cfg["cli"]
+    assert stored["nodes"]["render"]["outputs"] == ["irradiance->accumulate.src"]
+    assert stored["nodes"]["render"]["properties"]["seed"] == 11
+    assert stored["nodes"]["write"]["type"] == "Image Write"
+    h = node.Graph(None, stored)
+    assert h.to_json() == stored and h.order == g.order and h.warnings == []
