@@ -44,7 +44,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tuning", default=None,
-                    help="WAVE_PATHS,SORT: a fixed schedule instead of the autotuner's")
+                    help="WAVE_PATHS,SORT[,STREAMS]: a fixed schedule instead of the "
+                         "autotuner's")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default schedule instead of gbpt_autotune's choice of tick "
                          "size and material sorting (made before the warm-up, untimed)")
@@ -259,7 +260,10 @@ def run_gbpt(args):
     from merian_gb300 import scene as S
 
     w, sc, cam = build_workload(args.workload)
-    stream = torch.cuda.current_stream()
+    # the context renders on this stream (gbpt_create with 0 would make a private one): events
+    # recorded on it order with every launch of a step, including the second tick stream's
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = S.Context(local_rank, stream.cuda_stream)
     sid = ctx.upload(sc)
     bvh = ctx.scene_stats(sid)
@@ -277,16 +281,39 @@ def run_gbpt(args):
     frame_base = 1_000_000 * rank
     tuning = None
     if args.tuning:
-        wave, sort = (int(x) for x in args.tuning.split(","))
-        ctx.set_tuning(wave, sort)
-        tuning = {"wave_paths": wave, "sort_materials": sort, "fixed": True}
+        wave, sort, *more = (int(x) for x in args.tuning.split(","))
+        streams = more[0] if more else 0
+        ctx.set_tuning(wave, sort, streams=streams)
+        tuning = {"wave_paths": wave, "sort_materials": sort, "streams": streams or 2,
+                  "fixed": True}
     elif not args.no_autotune:
         t, cand_ms = ctx.autotune(sid, cam, params(frame_base + 998))
         tuning = {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials,
-                  "candidates_ms": [round(m, 2) for m in cand_ms]}
+                  "streams": t.streams or 2, "candidates_ms": [round(m, 2) for m in cand_ms]}
     for i in range(args.warmup):
         ctx.render_device(sid, cam, params(frame_base + i), out.data_ptr())
     torch.cuda.synchronize()
+
+    # the timed steps: the render as a user runs it (no profiling: ticks alternate over two
+    # streams); then the same number of profiled steps (per-launch CUDA events, one stream) give
+    # the kernel split and the traversal launch durations of the roofline
+    ctx.set_profiling(0)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    step_ms = []
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank if "CUDA_VISIBLE_DEVICES" not in os.environ else 0) as clk:
+        for i in range(args.steps):
+            flush.zero_()                       # L2 flush outside the timed events
+            ev0.record(stream)
+            ctx.render_device(sid, cam, params(frame_base + args.warmup + i), out.data_ptr())
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            step_ms.append(ev0.elapsed_time(ev1))
+    torch.cuda.synchronize()
+    ms = float(np.mean(step_ms))
 
     # untimed instrumented pass: CWBVH nodes / triangles per closest-hit ray of this workload
     ctx.set_profiling(2)
@@ -296,33 +323,27 @@ def run_gbpt(args):
     bytes_per_ray = 48.0 + 80.0 * nodes_per_ray + 48.0 * tris_per_ray
     ctx.set_profiling(1)
 
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
     torch.cuda.synchronize()
-    step_ms, trace_ms, trace_rays, trace_launches, launches, rays = [], 0.0, 0, 0, 0, 0
+    prof_ms, trace_ms, trace_rays, trace_launches, launches, rays = [], 0.0, 0, 0, 0, 0
     cls_ms = {"trace": 0.0, "shade": 0.0, "shadow": 0.0, "primary_finalize": 0.0}
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local_rank if "CUDA_VISIBLE_DEVICES" not in os.environ else 0) as clk:
-        for i in range(args.steps):
-            flush.zero_()                       # L2 flush outside the timed events
-            ev0.record(stream)
-            st = ctx.render_device(sid, cam, params(frame_base + args.warmup + i),
-                                   out.data_ptr(), stats=True)
-            ev1.record(stream)
-            torch.cuda.synchronize()
-            step_ms.append(ev0.elapsed_time(ev1))
-            trace_ms += st.trace_ms
-            cls_ms["trace"] += st.trace_ms
-            cls_ms["shade"] += st.shade_ms
-            cls_ms["shadow"] += st.shadow_ms
-            cls_ms["primary_finalize"] += st.other_ms
-            trace_rays += st.trace_rays
-            trace_launches += st.trace_launches
-            launches += st.kernel_launches
-            rays += st.rays
+    for i in range(args.steps):
+        flush.zero_()
+        ev0.record(stream)
+        st = ctx.render_device(sid, cam, params(frame_base + args.warmup + i),
+                               out.data_ptr(), stats=True)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        prof_ms.append(ev0.elapsed_time(ev1))
+        trace_ms += st.trace_ms
+        cls_ms["trace"] += st.trace_ms
+        cls_ms["shade"] += st.shade_ms
+        cls_ms["shadow"] += st.shadow_ms
+        cls_ms["primary_finalize"] += st.other_ms
+        trace_rays += st.trace_rays
+        trace_launches += st.trace_launches
+        launches += st.kernel_launches
+        rays += st.rays
     torch.cuda.synchronize()
-    ms = float(np.mean(step_ms))
 
     # end to end through the public API with a host output buffer (D2H inside the call)
     ctx.set_profiling(0)
@@ -384,7 +405,10 @@ def run_gbpt(args):
                          "tris_per_ray": round(tris_per_ray, 3),
                          "launches_per_step": trace_launches // max(args.steps, 1),
                          "trace_rays_per_step": trace_rays // max(args.steps, 1),
-                         "trace_share_of_step": round(trace_ms / args.steps / ms, 4)},
+                         "trace_share_of_step": round(trace_ms / float(np.sum(prof_ms)), 4),
+                         "kernel_times": "CUDA events per launch over the profiled steps "
+                                         "(one stream)"},
+            "profiled_ms_per_step": round(float(np.mean(prof_ms)), 3),
         }
         if tuning is not None:
             line["config"]["tuning"] = tuning
@@ -414,7 +438,10 @@ def run_batch_mix(args):
     torch.cuda.set_device(0)
     n = args.scenes or 256
     specs, reqs = WL.batch_mix(S.BASE_SEED, n)
-    stream = torch.cuda.current_stream()
+    # the context renders on this stream (gbpt_create with 0 would make a private one): events
+    # recorded on it order with every launch of a step, including the second tick stream's
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = S.Context(0, stream.cuda_stream)
     t0 = time.perf_counter()
     sids = WL.upload_all(ctx, specs)
@@ -510,7 +537,10 @@ def run_instanced(args):
     W_, H_, frames, spp, L = 3840, 2160, 16, 16, 16
     t0 = time.perf_counter()
     sc = W.instanced_scene(S.BASE_SEED)
-    stream = torch.cuda.current_stream()
+    # the context renders on this stream (gbpt_create with 0 would make a private one): events
+    # recorded on it order with every launch of a step, including the second tick stream's
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = S.Context(0, stream.cuda_stream)
     sid = ctx.upload(sc)
     setup_s = time.perf_counter() - t0

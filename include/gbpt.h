@@ -325,7 +325,11 @@ typedef struct gbpt_tuning {
     int32_t sort_materials; /* -1: as each request's params ask; 0 / 1: force off / on */
     int32_t use_graphs;     /* gbpt_render_batch replays ticks from CUDA graphs */
     int32_t bvh_build;      /* scenes created after it: GBPT_BVH_* */
-    int32_t reserved;
+    int32_t streams;        /* gbpt_render / gbpt_render_device: 2 (and 0, the default) = ticks
+                               alternate between the context stream and a second stream with its
+                               own work buffers, so one tick's last launches overlap the next
+                               tick's first (not while profiling); 1 = ticks in order on the
+                               context stream */
 } gbpt_tuning;
 
 /* BVH build of gbpt_scene_create (the traversal finds the same hits in every case). */

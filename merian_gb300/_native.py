@@ -136,7 +136,7 @@ class ServerStats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("wave_paths", C.c_uint64), ("sort_materials", C.c_int32),
-                ("use_graphs", C.c_int32), ("bvh_build", C.c_int32), ("reserved", C.c_int32)]
+                ("use_graphs", C.c_int32), ("bvh_build", C.c_int32), ("streams", C.c_int32)]
 
 
 BVH_SPLIT, BVH_FAST, BVH_MEDIUM = 0, 1, 2

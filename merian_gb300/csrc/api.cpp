@@ -232,6 +232,11 @@ GBPT_API int gbpt_destroy(gbpt_ctx* ctx) {
     for (auto& kv : ctx->scenes) free_scene(kv.second);
     ctx->batch.release();
     work_free(ctx->work);
+    if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
+    work_free(ctx->work2);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     ctx->prof.destroy();
     if (ctx->d_misc) cudaFree(ctx->d_misc);
     if (ctx->d_hits) cudaFree(ctx->d_hits);
@@ -758,7 +763,33 @@ int gbpt::validate_params(const gbpt_camera* cam, const gbpt_render_params* p) {
 extern "C" {
 
 static int read_stats(gbpt_ctx* ctx, uint64_t samples, uint64_t launches, Profile* prof,
-                      gbpt_render_stats* stats);
+                      gbpt_render_stats* stats, bool two);
+// Whether this render alternates its ticks over two streams (gbpt_tuning.streams 0 or 2, not
+// while profiling): creates the second stream, its events and work counters at first use.
+static int use_two_streams(gbpt_ctx* ctx, const Profile* prof, bool* two) {
+    *two = false;
+    if (ctx->tuning.streams == 1 || prof) return GBPT_OK;
+    if (!ctx->stream2 &&
+        cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking) != cudaSuccess) {
+        ctx->stream2 = nullptr;
+        set_error("render: cannot create the second tick stream");
+        return GBPT_ERR_CUDA;
+    }
+    for (cudaEvent_t* e : {&ctx->ev_fork, &ctx->ev_join}) {
+        if (!*e && cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) {
+            *e = nullptr;
+            set_error("render: cannot create the tick stream events");
+            return GBPT_ERR_CUDA;
+        }
+    }
+    const int rc = work_reserve(ctx->work2, 0, 0);
+    if (rc != GBPT_OK) {
+        set_error("render: work buffer allocation failed");
+        return rc;
+    }
+    *two = true;
+    return GBPT_OK;
+}
 
 static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
                        const gbpt_render_params* p, float* out_dev, float* out_host,
@@ -819,7 +850,14 @@ static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
     const uint64_t wave = ctx->tuning.wave_paths
                               ? std::max<uint64_t>(ctx->tuning.wave_paths, (uint64_t)p->spp)
                               : 0;
-    rc = render_frame(it->second, w, a, ctx->stream, &launches, prof, ctx->d_misc, wave);
+    bool two = false;
+    if ((rc = use_two_streams(ctx, prof, &two)) != GBPT_OK) return rc;
+    if (two && stats)
+        GBPT_CUDA_CHECK(cudaMemsetAsync(ctx->work2.stats, 0, 4 * sizeof(unsigned long long),
+                                        ctx->stream));
+    rc = two ? render_frame(it->second, w, a, ctx->stream, &launches, prof, ctx->d_misc, wave,
+                            &ctx->work2, ctx->stream2, ctx->ev_fork, ctx->ev_join)
+             : render_frame(it->second, w, a, ctx->stream, &launches, prof, ctx->d_misc, wave);
     if (rc != GBPT_OK) {
         set_error(rc == GBPT_ERR_NO_MEMORY ? "render: work buffer allocation failed"
                                            : "render: kernel launch failed: " +
@@ -834,18 +872,24 @@ static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
     if (stats || out_host) {
         if ((rc = check_device_error(ctx))) return rc;
     }
-    if (stats) return read_stats(ctx, (uint64_t)n_pix * (uint64_t)p->spp, launches, prof, stats);
+    if (stats)
+        return read_stats(ctx, (uint64_t)n_pix * (uint64_t)p->spp, launches, prof, stats, two);
     return GBPT_OK;
 }
 
 // Fills stats after a synchronised render: device counters, the event pair ev0/ev1 and, when
 // profiling, the per-class kernel times.
 static int read_stats(gbpt_ctx* ctx, uint64_t samples, uint64_t launches, Profile* prof,
-                      gbpt_render_stats* stats) {
+                      gbpt_render_stats* stats, bool two) {
     Work& w = ctx->work;
     {
         unsigned long long st[3] = {0, 0, 0}, wk[2] = {0, 0};
         GBPT_CUDA_CHECK(cudaMemcpy(st, w.stats, sizeof(st), cudaMemcpyDeviceToHost));
+        if (two) {
+            unsigned long long st2[3] = {0, 0, 0};
+            GBPT_CUDA_CHECK(cudaMemcpy(st2, ctx->work2.stats, sizeof(st2), cudaMemcpyDeviceToHost));
+            for (int k = 0; k < 3; ++k) st[k] += st2[k];
+        }
         GBPT_CUDA_CHECK(cudaMemcpy(wk, ctx->d_misc, sizeof(wk), cudaMemcpyDeviceToHost));
         float ms = 0.f;
         GBPT_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
@@ -1032,7 +1076,7 @@ GBPT_API int gbpt_render_batch(gbpt_ctx* ctx, const gbpt_request* reqs, uint32_t
                                         cudaMemcpyDeviceToHost, ctx->stream));
     }
     if ((rc = check_device_error(ctx))) return rc;
-    if (stats) return read_stats(ctx, samples, launches, prof, stats);
+    if (stats) return read_stats(ctx, samples, launches, prof, stats, false);
     return GBPT_OK;
 }
 
@@ -1049,9 +1093,9 @@ GBPT_API int gbpt_set_graphs(gbpt_ctx* ctx, int enable) {
 static int check_tuning(const gbpt_tuning* t) {
     if (!t || t->wave_paths > (1ull << 24) || (t->wave_paths && t->wave_paths < 1024) ||
         t->sort_materials < -1 || t->sort_materials > 1 || t->bvh_build < GBPT_BVH_SPLIT ||
-        t->bvh_build > GBPT_BVH_MEDIUM) {
+        t->bvh_build > GBPT_BVH_MEDIUM || t->streams < 0 || t->streams > 2) {
         set_error("tuning: wave_paths must be 0 or in [1024, 2^24], sort_materials in {-1, 0, 1}, "
-                  "bvh_build a GBPT_BVH_* value");
+                  "bvh_build a GBPT_BVH_* value, streams in {0, 1, 2}");
         return GBPT_ERR_INVALID;
     }
     return GBPT_OK;
@@ -1146,6 +1190,7 @@ GBPT_API int gbpt_autotune(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam
     if ((rc = check_device_error(ctx))) return rc;
     best.use_graphs = ctx->tuning.use_graphs;
     best.bvh_build = ctx->tuning.bvh_build;
+    best.streams = ctx->tuning.streams;
     ctx->tuning = best;
     ctx->batch.wave = best.wave_paths;
     ctx->batch.release();

@@ -34,6 +34,11 @@ struct gbpt_ctx {
     uint32_t next_scene = 1;
     gbpt::Work work;
     gbpt::TickEngine batch; // gbpt_render_batch, over `work`
+    // gbpt_tuning.streams = 2: the second tick stream, its work buffers, and the events that
+    // order it after and before the context stream
+    gbpt::Work work2;
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // schedule of gbpt_render* and gbpt_render_batch: paths per tick (0 = default), material sort
     // override (-1 = as each request asks), CUDA graphs
     gbpt_tuning tuning{0, -1, 0, GBPT_BVH_SPLIT, 0};

@@ -180,10 +180,13 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
 // other items in the batch, bit for bit.
 int render_batch(TickEngine& e, const BatchItem* items, uint32_t n_items, uint64_t* launches,
                  Profile* prof, unsigned long long* work_ctr);
-// wave: paths per tick, 0 = kWavePaths
+// wave: paths per tick, 0 = kWavePaths. With work2, ticks alternate between stream (even) and
+// stream2 (odd, over work2): stream2 starts after `fork` is recorded on stream, and stream waits
+// for `join` recorded on stream2 at the end.
 int render_frame(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
                  uint64_t* launches, Profile* prof, unsigned long long* work_ctr,
-                 uint64_t wave = 0);
+                 uint64_t wave = 0, Work* work2 = nullptr, cudaStream_t stream2 = nullptr,
+                 cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 int primary_points(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
                    float* out_device);
 // Bytes of tick tables for ticks of at most max_chunks requests.

@@ -1074,7 +1074,8 @@ int render_batch(TickEngine& e, const BatchItem* items, uint32_t n_items, uint64
 }
 
 int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStream_t st,
-                 uint64_t* launches, Profile* prof, unsigned long long* work_ctr, uint64_t wave) {
+                 uint64_t* launches, Profile* prof, unsigned long long* work_ctr, uint64_t wave,
+                 Work* w2, cudaStream_t st2, cudaEvent_t fork, cudaEvent_t join) {
     BatchItem it;
     it.scene = &scene;
     it.camera = args.camera;
@@ -1086,9 +1087,34 @@ int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStr
     e.work = &w;
     e.stream = st;
     if (wave) e.wave = wave;
-    const int rc = render_batch(e, &it, 1, launches, prof, work_ctr);
+    if (!w2) {
+        const int rc = render_batch(e, &it, 1, launches, prof, work_ctr);
+        e.release();
+        return rc;
+    }
+    // two streams: ticks cover disjoint pixels, each over its own work buffers, so they only
+    // share the scene (read), the output (disjoint texels) and atomic counters
+    e.wave = std::max<uint64_t>(e.wave, (uint64_t)std::max(it.params.spp, 0));
+    TickEngine e2;
+    e2.work = w2;
+    e2.stream = st2;
+    e2.wave = e.wave;
+    if (cudaEventRecord(fork, st) != cudaSuccess || cudaStreamWaitEvent(st2, fork, 0) != cudaSuccess)
+        return GBPT_ERR_CUDA;
+    TickItem ti;
+    static_cast<BatchItem&>(ti) = it;
+    TickItem* ptr = &ti;
+    int rc = GBPT_OK;
+    for (uint64_t k = 0;; ++k) {
+        uint64_t n = 0;
+        rc = tick_enqueue((k & 1) ? e2 : e, &ptr, 1, &n, nullptr, launches, prof, work_ctr);
+        if (rc != GBPT_OK || n == 0) break;
+    }
+    const bool joined = cudaEventRecord(join, st2) == cudaSuccess &&
+                        cudaStreamWaitEvent(st, join, 0) == cudaSuccess;
     e.release();
-    return rc;
+    e2.release();
+    return rc != GBPT_OK ? rc : (joined ? GBPT_OK : GBPT_ERR_CUDA);
 }
 
 // The primary shading points of the listed pixels (the first tick's k_primary only).

@@ -370,8 +370,9 @@ class Context:
         N.check(self.lib.gbpt_set_graphs(self.handle, int(enable)))
 
     def set_tuning(self, wave_paths: int = 0, sort_materials: int = -1,
-                   use_graphs: bool = False, bvh_build: int = N.BVH_SPLIT) -> None:
-        t = N.Tuning(wave_paths, sort_materials, int(use_graphs), bvh_build, 0)
+                   use_graphs: bool = False, bvh_build: int = N.BVH_SPLIT,
+                   streams: int = 0) -> None:
+        t = N.Tuning(wave_paths, sort_materials, int(use_graphs), bvh_build, streams)
         N.check(self.lib.gbpt_set_tuning(self.handle, C.byref(t)))
 
     def get_tuning(self) -> N.Tuning:

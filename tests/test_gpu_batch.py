@@ -246,23 +246,28 @@ def test_material_sorted_shading_same_result(gpu_ctx, scenes):
 
 
 def test_tuning_and_autotune_same_result(gpu_ctx, scenes):
-    """The context's tuning (tick size, forced material sort, graphs) and the autotuner's choice
-    change only the schedule: every output is bit-identical to the default schedule's."""
+    """The context's tuning (tick size, forced material sort, graphs, two tick streams) and the
+    autotuner's choice change only the schedule: every output is bit-identical to the default schedule's."""
     from merian_gb300 import scene as S
     jobs = _jobs(scenes, S)
     ref = _alone(gpu_ctx, jobs)
     corn, soup, cams = scenes
     try:
-        for wave, sort, graphs in ((1 << 12, 1, False), (1 << 20, 0, True), (1 << 24, -1, False)):
-            gpu_ctx.set_tuning(wave, sort, graphs)
+        for wave, sort, graphs, streams in ((1 << 12, 1, False, 2), (1 << 20, 0, True, 0),
+                                           (1 << 24, -1, False, 2), (1 << 16, 0, False, 2)):
+            gpu_ctx.set_tuning(wave, sort, graphs, streams=streams)
             t = gpu_ctx.get_tuning()
-            assert (t.wave_paths, t.sort_materials, t.use_graphs) == (wave, sort, int(graphs))
+            assert (t.wave_paths, t.sort_materials, t.use_graphs, t.streams) == \
+                (wave, sort, int(graphs), streams)
             assert all(_same(a, b) for a, b in zip(ref, _alone(gpu_ctx, jobs)))
             outs = gpu_ctx.render_batch([(s, c, p) for s, c, p, _ in jobs if p.spp <= wave])
             kept = [r for r, j in zip(ref, jobs) if j[2].spp <= wave]
             assert all(_same(a, b) for a, b in zip(kept, outs))
         with pytest.raises(N.GbptError):
             gpu_ctx.set_tuning(100, 0, False)  # below the smallest tick
+        with pytest.raises(N.GbptError):
+            gpu_ctx.set_tuning(1 << 20, 0, False, streams=3)
+        gpu_ctx.set_tuning(0, -1, False)
         p, _ = S.render_params(320, 180, 16, 8, nee=True, rr_depth=3, frame=1)
         t, ms = gpu_ctx.autotune(soup, cams[soup], p)
         assert len(ms) == 8 and all(m > 0 for m in ms)
