@@ -231,6 +231,7 @@ GBPT_API int gbpt_destroy(gbpt_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     for (auto& kv : ctx->scenes) free_scene(kv.second);
     ctx->batch.release();
+    ctx->batch2.release();
     work_free(ctx->work);
     if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
     work_free(ctx->work2);
@@ -1061,7 +1062,18 @@ GBPT_API int gbpt_render_batch(gbpt_ctx* ctx, const gbpt_request* reqs, uint32_t
     }
     ctx->batch.work = &w;
     ctx->batch.stream = ctx->stream;
-    rc = render_batch(ctx->batch, items.data(), n, &launches, prof, ctx->d_misc);
+    bool two = false;
+    if ((rc = use_two_streams(ctx, prof, &two)) != GBPT_OK) return rc;
+    if (two) {
+        ctx->batch2.work = &ctx->work2;
+        ctx->batch2.stream = ctx->stream2;
+        ctx->batch2.use_graphs = ctx->batch.use_graphs;
+        if (stats)
+            GBPT_CUDA_CHECK(cudaMemsetAsync(ctx->work2.stats, 0, 4 * sizeof(unsigned long long),
+                                            ctx->stream));
+    }
+    rc = render_batch(ctx->batch, items.data(), n, &launches, prof, ctx->d_misc,
+                      two ? &ctx->batch2 : nullptr, ctx->ev_fork, ctx->ev_join);
     if (rc != GBPT_OK) {
         set_error(rc == GBPT_ERR_NO_MEMORY ? "gbpt_render_batch: work buffer allocation failed"
                                            : "gbpt_render_batch: launch failed: " +
@@ -1076,7 +1088,7 @@ GBPT_API int gbpt_render_batch(gbpt_ctx* ctx, const gbpt_request* reqs, uint32_t
                                         cudaMemcpyDeviceToHost, ctx->stream));
     }
     if ((rc = check_device_error(ctx))) return rc;
-    if (stats) return read_stats(ctx, samples, launches, prof, stats, false);
+    if (stats) return read_stats(ctx, samples, launches, prof, stats, two);
     return GBPT_OK;
 }
 
@@ -1085,8 +1097,12 @@ GBPT_API int gbpt_set_graphs(gbpt_ctx* ctx, int enable) {
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->batch.use_graphs = enable != 0;
+    ctx->batch2.use_graphs = enable != 0;
     ctx->tuning.use_graphs = enable != 0;
-    if (!enable) ctx->batch.release();
+    if (!enable) {
+        ctx->batch.release();
+        ctx->batch2.release();
+    }
     return GBPT_OK;
 }
 
@@ -1111,6 +1127,7 @@ GBPT_API int gbpt_set_tuning(gbpt_ctx* ctx, const gbpt_tuning* t) {
     ctx->batch.wave = t->wave_paths ? t->wave_paths : kWavePaths;
     ctx->batch.use_graphs = t->use_graphs != 0;
     ctx->batch.release();
+    ctx->batch2.release();
     return GBPT_OK;
 }
 
@@ -1194,6 +1211,7 @@ GBPT_API int gbpt_autotune(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam
     ctx->tuning = best;
     ctx->batch.wave = best.wave_paths;
     ctx->batch.release();
+    ctx->batch2.release();
     if (out) *out = best;
     return GBPT_OK;
 }

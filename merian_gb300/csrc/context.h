@@ -37,6 +37,7 @@ struct gbpt_ctx {
     // gbpt_tuning.streams = 2: the second tick stream, its work buffers, and the events that
     // order it after and before the context stream
     gbpt::Work work2;
+    gbpt::TickEngine batch2; // gbpt_render_batch's odd ticks, over `work2`
     cudaStream_t stream2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // schedule of gbpt_render* and gbpt_render_batch: paths per tick (0 = default), material sort

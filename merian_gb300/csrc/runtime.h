@@ -178,8 +178,11 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
                  unsigned long long* work_ctr);
 // Renders every item (ticks until all pixels are scheduled); results are independent of the
 // other items in the batch, bit for bit.
+// With e2, ticks alternate between e (even) and e2 (odd; its own stream and work buffers):
+// e2's stream starts after `fork` is recorded on e's, and e's waits for `join` recorded on e2's.
 int render_batch(TickEngine& e, const BatchItem* items, uint32_t n_items, uint64_t* launches,
-                 Profile* prof, unsigned long long* work_ctr);
+                 Profile* prof, unsigned long long* work_ctr, TickEngine* e2 = nullptr,
+                 cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 // wave: paths per tick, 0 = kWavePaths. With work2, ticks alternate between stream (even) and
 // stream2 (odd, over work2): stream2 starts after `fork` is recorded on stream, and stream waits
 // for `join` recorded on stream2 at the end.

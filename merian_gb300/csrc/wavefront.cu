@@ -1055,7 +1055,8 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
 }
 
 int render_batch(TickEngine& e, const BatchItem* items, uint32_t n_items, uint64_t* launches,
-                 Profile* prof, unsigned long long* work_ctr) {
+                 Profile* prof, unsigned long long* work_ctr, TickEngine* e2, cudaEvent_t fork,
+                 cudaEvent_t join) {
     std::vector<TickItem> ti(n_items);
     std::vector<TickItem*> ptr(n_items);
     uint64_t max_spp = 0;
@@ -1065,12 +1066,31 @@ int render_batch(TickEngine& e, const BatchItem* items, uint32_t n_items, uint64
         max_spp = std::max<uint64_t>(max_spp, (uint64_t)std::max(items[i].params.spp, 0));
     }
     if (!e.work->fixed) e.wave = std::max<uint64_t>(e.wave, max_spp);
-    while (true) {
-        uint64_t n = 0;
-        const int rc = tick_enqueue(e, ptr.data(), n_items, &n, nullptr, launches, prof, work_ctr);
-        if (rc != GBPT_OK) return rc;
-        if (n == 0) return GBPT_OK;
+    if (!e2) {
+        while (true) {
+            uint64_t n = 0;
+            const int rc =
+                tick_enqueue(e, ptr.data(), n_items, &n, nullptr, launches, prof, work_ctr);
+            if (rc != GBPT_OK) return rc;
+            if (n == 0) return GBPT_OK;
+        }
     }
+    // two streams: ticks cover disjoint pixels, each over its own work buffers, so they only
+    // share the scenes (read), the outputs (disjoint texels) and atomic counters
+    e2->wave = e.wave;
+    if (cudaEventRecord(fork, e.stream) != cudaSuccess ||
+        cudaStreamWaitEvent(e2->stream, fork, 0) != cudaSuccess)
+        return GBPT_ERR_CUDA;
+    int rc = GBPT_OK;
+    for (uint64_t k = 0;; ++k) {
+        uint64_t n = 0;
+        rc = tick_enqueue((k & 1) ? *e2 : e, ptr.data(), n_items, &n, nullptr, launches, prof,
+                          work_ctr);
+        if (rc != GBPT_OK || n == 0) break;
+    }
+    const bool joined = cudaEventRecord(join, e2->stream) == cudaSuccess &&
+                        cudaStreamWaitEvent(e.stream, join, 0) == cudaSuccess;
+    return rc != GBPT_OK ? rc : (joined ? GBPT_OK : GBPT_ERR_CUDA);
 }
 
 int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStream_t st,
@@ -1087,34 +1107,14 @@ int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStr
     e.work = &w;
     e.stream = st;
     if (wave) e.wave = wave;
-    if (!w2) {
-        const int rc = render_batch(e, &it, 1, launches, prof, work_ctr);
-        e.release();
-        return rc;
-    }
-    // two streams: ticks cover disjoint pixels, each over its own work buffers, so they only
-    // share the scene (read), the output (disjoint texels) and atomic counters
-    e.wave = std::max<uint64_t>(e.wave, (uint64_t)std::max(it.params.spp, 0));
     TickEngine e2;
     e2.work = w2;
     e2.stream = st2;
-    e2.wave = e.wave;
-    if (cudaEventRecord(fork, st) != cudaSuccess || cudaStreamWaitEvent(st2, fork, 0) != cudaSuccess)
-        return GBPT_ERR_CUDA;
-    TickItem ti;
-    static_cast<BatchItem&>(ti) = it;
-    TickItem* ptr = &ti;
-    int rc = GBPT_OK;
-    for (uint64_t k = 0;; ++k) {
-        uint64_t n = 0;
-        rc = tick_enqueue((k & 1) ? e2 : e, &ptr, 1, &n, nullptr, launches, prof, work_ctr);
-        if (rc != GBPT_OK || n == 0) break;
-    }
-    const bool joined = cudaEventRecord(join, st2) == cudaSuccess &&
-                        cudaStreamWaitEvent(st, join, 0) == cudaSuccess;
+    const int rc = render_batch(e, &it, 1, launches, prof, work_ctr, w2 ? &e2 : nullptr, fork,
+                                join);
     e.release();
     e2.release();
-    return rc != GBPT_OK ? rc : (joined ? GBPT_OK : GBPT_ERR_CUDA);
+    return rc;
 }
 
 // The primary shading points of the listed pixels (the first tick's k_primary only).
