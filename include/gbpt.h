@@ -436,7 +436,8 @@ GBPT_API int gbpt_image_read_png(const char* path, uint8_t* rgba, uint32_t* widt
  * Plot", "GLTF Scene" and "PBRT Scene" (the loaders below; the scene is made resident when the
  * graph first runs), with merian's connector names, property keys and defaults, from a graph JSON in
  * merian's layout (examples/renderers/pt.json). A graph created with ctx = NULL is checked
- * (types, properties, edges) but cannot run. Not thread-safe: one caller per graph.
+ * (types, properties, edges) but cannot run. Not thread-safe: one caller per graph. Destroy a
+ * graph before its context (its buffers and scene nodes' scenes live on that context).
  * Properties: gbpt_graph_set_property takes one JSON value ("group/key" for a property in a
  * group such as Image Write's "advanced") and returns merian's NodeStatusFlags (1 =
  * NEEDS_RECONNECT); unknown keys are errors there and warnings in the graph JSON. Outputs are
