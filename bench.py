@@ -155,6 +155,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def host_threads() -> int:
+    """Every host thread this process may run on (torchrun's OMP_NUM_THREADS=1 is overridden:
+    the CPU legs use the whole host)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
 def cpu_baseline(scene, camera, w, cpu_seconds: float, kind_label: str = "port"):
     """FP32 oracle on every host thread, on a bounded pixel sample of the same workload."""
     from merian_gb300 import scene as S
@@ -166,14 +175,14 @@ def cpu_baseline(scene, camera, w, cpu_seconds: float, kind_label: str = "port")
     p, keep = S.render_params(w["width"], w["height"], w["spp"], w["max_path_length"],
                               pixels=probe, nee=w["nee"], rr_depth=w["rr_depth"], frame=0)
     t0 = time.perf_counter()
-    osc.render(camera, p, fp64=False)
+    osc.render(camera, p, fp64=False, threads=host_threads())
     dt = time.perf_counter() - t0
     n_px = int(min(n_total, max(32, 32 * cpu_seconds / max(dt, 1e-3))))
     pix = np.sort(rng.choice(n_total, n_px, replace=False)).astype(np.uint32)
     p, keep = S.render_params(w["width"], w["height"], w["spp"], w["max_path_length"],
                               pixels=pix, nee=w["nee"], rr_depth=w["rr_depth"], frame=0)
     t0 = time.perf_counter()
-    _, _, rays = osc.render(camera, p, fp64=False)
+    _, _, rays = osc.render(camera, p, fp64=False, threads=host_threads())
     dt = time.perf_counter() - t0
     samples = n_px * w["spp"]
     threads = O.num_threads()
@@ -200,7 +209,11 @@ def run_reference(args):
         return
     from oracle import binding as O
     from merian_gb300 import scene as S
-    w, sc, cam = build_workload(args.workload)
+    # the scene and camera come from the oracle library (its own camera basis and the seeded
+    # generators compiled into it): this arm maps no CUDA library of the package
+    w = S.WORKLOADS[args.workload]
+    sc = S.workload_scene(args.workload, lib=O.generator())
+    cam = O.workload_camera(args.workload)
     osc = O.OracleScene(sc)
     n_total = w["width"] * w["height"]
     rng = np.random.default_rng(7)
@@ -209,9 +222,10 @@ def run_reference(args):
     p, keep = S.render_params(w["width"], w["height"], w["spp"], w["max_path_length"],
                               pixels=probe, nee=w["nee"], rr_depth=w["rr_depth"])
     t0 = time.perf_counter()
-    osc.render(cam, p, fp64=False)
+    osc.render(cam, p, fp64=False, threads=host_threads())
     per_px = (time.perf_counter() - t0) / 16
-    budget = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    # about 4 x --cpu-seconds of CPU work over the whole run (60 s by default)
+    budget = max(0.5, 4.0 * args.cpu_seconds / max(1, args.steps + args.warmup))
     n_px = int(min(n_total, max(16, budget / max(per_px, 1e-6))))
     times, rays_total = [], 0
     for i in range(args.warmup + args.steps):
@@ -219,7 +233,7 @@ def run_reference(args):
         p, keep = S.render_params(w["width"], w["height"], w["spp"], w["max_path_length"],
                                   pixels=pix, nee=w["nee"], rr_depth=w["rr_depth"], frame=i)
         t0 = time.perf_counter()
-        _, _, rays = osc.render(cam, p, fp64=False)
+        _, _, rays = osc.render(cam, p, fp64=False, threads=host_threads())
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             times.append(dt)
@@ -718,8 +732,36 @@ def run_served(args):
     ctx.close()
 
 
+def _free_port() -> int:
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def launch_ranks(args) -> int | None:
+    """--gpus N outside torchrun: start N ranks of this script with torch.distributed.run (one
+    process per GPU, rendezvous on 127.0.0.1) and return their exit status. Under torchrun,
+    --gpus must equal WORLD_SIZE. None: run this process as the only rank."""
+    world_env = os.environ.get("WORLD_SIZE")
+    if world_env is not None:
+        if int(world_env) != args.gpus:
+            print(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world_env}", file=sys.stderr)
+            return 2
+        return None
+    if args.gpus <= 1:
+        return None
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+           f"--nproc-per-node={args.gpus}", "--master-addr", "127.0.0.1",
+           "--master-port", str(_free_port()), str(Path(__file__).resolve()), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
 def main():
     args = parse()
+    rc = launch_ranks(args)
+    if rc is not None:
+        sys.exit(rc)
     mixed = args.workload in ("batch-256", "served-stream", "instanced-4k")
     if args.steps is None:
         args.steps = 1 if mixed else 5

@@ -283,8 +283,10 @@ GBPT_API int gbpt_render_device(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera
  * until the process exits; this call allocates nothing. The scene must already be resident
  * (gbpt_scene_create, an earlier set-up step) and out_rgba_device is caller-owned device memory.
  * Limits: spp at most the paths one pass over the array holds (225,815), a pixel
- * subset of at most 65,536 entries; larger requests return GBPT_ERR_INVALID. The first call on a
- * device looks up the array's device address, so make it before any stream capture. All calls
+ * subset of at most 65,536 entries; larger requests return GBPT_ERR_INVALID. Every call looks up
+ * the array's device address (no allocation; nothing cached, so a device reset between calls is
+ * harmless); the first lookup on a device may load the library's module, so make the first call
+ * on each device before any stream capture. All calls
  * share the array: calls that overlap on the GPU (other streams or threads) race on it. The call
  * waits for its work to finish before it returns.
  * (No counterpart in the reference: merian's node always renders into graph-allocated images.) */

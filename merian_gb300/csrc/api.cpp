@@ -161,19 +161,26 @@ void set_split(BuildInput& in, int32_t bvh_build, bool blas) {
     }
 }
 
-// Reads and clears the kernels' error word; returns GBPT_ERR_DEVICE when it was set.
+// Reads and clears the kernels' error words (the context's work buffers, the second tick
+// stream's, and the per-ray entry points'); returns GBPT_ERR_DEVICE when one was set. The
+// second stream's ticks have joined the context stream before any caller gets here.
 int check_device_error(gbpt_ctx* ctx) {
-    uint32_t flags[2] = {0, 0};
+    uint32_t flags[3] = {0, 0, 0};
     if (ctx->work.counters) {
         GBPT_CUDA_CHECK(cudaMemcpyAsync(&flags[0], ctx->work.counters + 3, 4,
+                                        cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (ctx->work2.counters) {
+        GBPT_CUDA_CHECK(cudaMemcpyAsync(&flags[2], ctx->work2.counters + 3, 4,
                                         cudaMemcpyDeviceToHost, ctx->stream));
     }
     unsigned long long misc = 0;
     GBPT_CUDA_CHECK(cudaMemcpyAsync(&misc, ctx->d_misc + 2, 8, cudaMemcpyDeviceToHost, ctx->stream));
     GBPT_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     flags[1] = (uint32_t)misc;
-    if (flags[0] | flags[1]) {
+    if (flags[0] | flags[1] | flags[2]) {
         if (ctx->work.counters) cudaMemsetAsync(ctx->work.counters + 3, 0, 4, ctx->stream);
+        if (ctx->work2.counters) cudaMemsetAsync(ctx->work2.counters + 3, 0, 4, ctx->stream);
         cudaMemsetAsync(ctx->d_misc + 2, 0, 8, ctx->stream);
         cudaStreamSynchronize(ctx->stream);
         set_error("kernel error flag raised (traversal stack overflow)");

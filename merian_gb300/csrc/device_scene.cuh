@@ -194,7 +194,16 @@ GBPT_DI bool intersect_tri(const RayPre& p, float4 a4, float4 b4, float4 c4, uin
 }
 
 // ---- CWBVH traversal ----------------------------------------------------------------------------
-constexpr int kStackSize = 48;
+// Traversal stack entries per ray. The builder bounds the tree depth (24 levels), which with
+// postponed triangle groups and instance entries stays below the default. A build with a smaller
+// GBPT_STACK_SIZE makes deep traversals overflow: the overflow sets the kernels' error word
+// (GBPT_ERR_DEVICE on the host) and finishes the ray with what it found, never a fault, so the
+// error path can be exercised on purpose.
+#ifndef GBPT_STACK_SIZE
+#define GBPT_STACK_SIZE 48
+#endif
+constexpr int kStackSize = GBPT_STACK_SIZE;
+static_assert(kStackSize >= 1, "the traversal needs a stack entry");
 constexpr uint32_t kNoInst = 0xFFFFFFFFu;
 
 struct TraceCounters {

@@ -6,7 +6,6 @@
 
 #include <algorithm>
 #include <cstdio>
-#include <mutex>
 #include <type_traits>
 
 namespace gbpt {
@@ -199,20 +198,15 @@ constexpr uint64_t kStaticBytesPerPath =
 // alignment padding of the carved arrays, and the tick tables of a one-request render
 constexpr uint64_t kStaticSlackBytes = 16 * 256 + 1024;
 
-std::mutex g_static_mu;
-void* g_static_ptr[64] = {};
-
-// The array's device address on the current device, looked up on the first call per device.
-int static_scratch_address(int dev, unsigned char** out) {
-    if (dev < 0 || dev >= 64) return GBPT_ERR_INVALID;
-    std::lock_guard<std::mutex> lk(g_static_mu);
-    if (!g_static_ptr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-        if (e != cudaSuccess || !p) return GBPT_ERR_CUDA;
-        g_static_ptr[dev] = p;
-    }
-    *out = (unsigned char*)g_static_ptr[dev];
+// The array's device address on the current device. Host code cannot use the symbol itself (it
+// names a host-side stand-in), so every call asks the runtime: the lookup allocates nothing, and
+// an address cached across calls would dangle after a device reset reloads the module. The first
+// lookup on a device may load the module, which is why the first call belongs before any capture.
+int static_scratch_address(unsigned char** out) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess || !p) return GBPT_ERR_CUDA;
+    *out = (unsigned char*)p;
     return GBPT_OK;
 }
 } // namespace
@@ -225,13 +219,8 @@ uint64_t static_scratch_paths() {
 
 int render_frame_static(const SceneGPU& scene, const RenderArgs& args, const uint32_t* pixels_host,
                         cudaStream_t st, std::string& err) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) {
-        err = "cudaGetDevice failed";
-        return GBPT_ERR_CUDA;
-    }
     unsigned char* base = nullptr;
-    int rc = static_scratch_address(dev, &base);
+    int rc = static_scratch_address(&base);
     if (rc != GBPT_OK) {
         err = "cudaGetSymbolAddress of the static scratch array failed";
         return rc;

@@ -82,19 +82,27 @@ class SceneData:
         return d, keep
 
 
-def cornell(seed: int = BASE_SEED, tess: int = 1) -> SceneData:
+def _gen_check(lib, rc: int, what: str) -> None:
+    if rc != N.GBPT_OK:
+        raise N.GbptError(rc, f"{what} failed")
+
+
+def cornell(seed: int = BASE_SEED, tess: int = 1, lib=None) -> SceneData:
     """The Cornell box: 1,024 triangles (gbpt_gen_cornell), or every grid refined `tess` times per
-    side, 1,024 tess^2 triangles (gbpt_gen_cornell_tess)."""
-    lib = N.load()
+    side, 1,024 tess^2 triangles (gbpt_gen_cornell_tess). `lib`: the library whose gbpt_gen_*
+    to call (default libgbpt.so)."""
+    lib = lib or N.load()
     nt = 1024 * tess * tess
     v = np.zeros(3 * nt, N.VERTEX_DTYPE)
     i = np.zeros((nt, 3), np.uint32)
     g = np.zeros(8, N.GEOMETRY_DTYPE)
     m = np.zeros(8, N.MATERIAL_DTYPE)
     if tess == 1:
-        N.check(lib.gbpt_gen_cornell(seed, N.ptr(v), N.ptr(i), N.ptr(g), N.ptr(m)))
+        _gen_check(lib, lib.gbpt_gen_cornell(seed, N.ptr(v), N.ptr(i), N.ptr(g), N.ptr(m)),
+                   "gbpt_gen_cornell")
     else:
-        N.check(lib.gbpt_gen_cornell_tess(seed, tess, N.ptr(v), N.ptr(i), N.ptr(g), N.ptr(m)))
+        _gen_check(lib, lib.gbpt_gen_cornell_tess(seed, tess, N.ptr(v), N.ptr(i), N.ptr(g),
+                                                  N.ptr(m)), "gbpt_gen_cornell_tess")
     return SceneData(v, i, g, m)
 
 
@@ -114,25 +122,25 @@ def noise_texture(seed: int, width: int = 512, height: int = 512) -> np.ndarray:
     return t
 
 
-def env_lobes(seed: int, width: int = 2048, height: int = 1024) -> np.ndarray:
-    lib = N.load()
+def env_lobes(seed: int, width: int = 2048, height: int = 1024, lib=None) -> np.ndarray:
+    lib = lib or N.load()
     t = np.zeros((height, width, 4), np.float32)
-    N.check(lib.gbpt_gen_env(seed, width, height, N.ptr(t)))
+    _gen_check(lib, lib.gbpt_gen_env(seed, width, height, N.ptr(t)), "gbpt_gen_env")
     return t
 
 
 def soup(seed: int = BASE_SEED, n_triangles: int = 1_000_000, n_geometries: int = 4096,
-         env_size: tuple[int, int] | None = (2048, 1024)) -> SceneData:
+         env_size: tuple[int, int] | None = (2048, 1024), lib=None) -> SceneData:
     """Triangle soup with an optional Gaussian-lobe lat-long environment (gbpt_gen_soup)."""
-    lib = N.load()
+    lib = lib or N.load()
     n_geometries = max(1, min(n_geometries, n_triangles))
     v = np.zeros(3 * n_triangles, N.VERTEX_DTYPE)
     i = np.zeros((n_triangles, 3), np.uint32)
     g = np.zeros(n_geometries, N.GEOMETRY_DTYPE)
     m = np.zeros(n_geometries, N.MATERIAL_DTYPE)
-    N.check(lib.gbpt_gen_soup(seed, n_triangles, n_geometries, N.ptr(v), N.ptr(i), N.ptr(g),
-                              N.ptr(m)))
-    env = env_lobes(seed ^ 0xE27, *env_size) if env_size else None
+    _gen_check(lib, lib.gbpt_gen_soup(seed, n_triangles, n_geometries, N.ptr(v), N.ptr(i),
+                                      N.ptr(g), N.ptr(m)), "gbpt_gen_soup")
+    env = env_lobes(seed ^ 0xE27, *env_size, lib=lib) if env_size else None
     return SceneData(v, i, g, m, env)
 
 
@@ -245,12 +253,12 @@ def _load_file(entry: str, path: str):
         lib.gbpt_loaded_scene_free(h)
 
 
-def workload_scene(name: str, seed: int = BASE_SEED, **overrides) -> SceneData:
+def workload_scene(name: str, seed: int = BASE_SEED, lib=None, **overrides) -> SceneData:
     w = dict(WORKLOADS[name], **overrides)
     if w["scene"] == "cornell":
-        return cornell(seed)
+        return cornell(seed, lib=lib)
     return soup(seed, w.get("n_triangles", 1_000_000), w.get("n_geometries", 4096),
-                w.get("env_size", (2048, 1024)))
+                w.get("env_size", (2048, 1024)), lib=lib)
 
 
 def workload_camera(name: str, width: int | None = None, height: int | None = None) -> N.Camera:
@@ -264,11 +272,18 @@ def workload_camera(name: str, width: int | None = None, height: int | None = No
 class Context:
     """One gbpt_ctx on one CUDA device; scenes stay resident in HBM until destroyed."""
 
-    def __init__(self, device: int = 0, stream: int = 0):
-        self.lib = N.load()
+    def __init__(self, device: int = 0, stream: int = 0, lib=None):
+        """`lib`: a build of the library loaded with _native.load(path) (a variant with other
+        compile-time constants); default libgbpt.so."""
+        self.lib = lib or N.load()
         h = C.c_void_p()
-        N.check(self.lib.gbpt_create(device, stream, C.byref(h)))
+        self._check(self.lib.gbpt_create(device, stream, C.byref(h)))
         self.handle = h
+
+    def _check(self, rc: int) -> None:
+        if rc != N.GBPT_OK:
+            msg = self.lib.gbpt_last_error()
+            raise N.GbptError(rc, msg.decode() if msg else "")
 
     def close(self) -> None:
         if self.handle:
@@ -284,17 +299,17 @@ class Context:
     def upload(self, scene: SceneData) -> int:
         d, keep = scene.desc()
         sid = C.c_uint32()
-        N.check(self.lib.gbpt_scene_create(self.handle, C.byref(d), C.byref(sid)))
+        self._check(self.lib.gbpt_scene_create(self.handle, C.byref(d), C.byref(sid)))
         del keep
         return sid.value
 
     def destroy_scene(self, sid: int) -> None:
-        N.check(self.lib.gbpt_scene_destroy(self.handle, sid))
+        self._check(self.lib.gbpt_scene_destroy(self.handle, sid))
 
     def scene_stats(self, sid: int) -> dict:
         n, t, b = C.c_uint64(), C.c_uint64(), C.c_uint64()
         dp = C.c_uint32()
-        N.check(self.lib.gbpt_scene_stats(self.handle, sid, C.byref(n), C.byref(t), C.byref(b),
+        self._check(self.lib.gbpt_scene_stats(self.handle, sid, C.byref(n), C.byref(t), C.byref(b),
                                           C.byref(dp)))
         return dict(nodes=n.value, tris=t.value, bytes=b.value, depth=dp.value)
 
@@ -303,21 +318,21 @@ class Context:
         n = params.pixel_count or params.width * params.height
         out = np.empty((n, 4), np.float32)
         st = N.RenderStats()
-        N.check(self.lib.gbpt_render(self.handle, sid, C.byref(camera), C.byref(params),
+        self._check(self.lib.gbpt_render(self.handle, sid, C.byref(camera), C.byref(params),
                                      N.ptr(out), C.byref(st) if stats else None))
         return (out, st) if stats else out
 
     def render_device(self, sid: int, camera: N.Camera, params: N.RenderParams, out_ptr: int,
                       stats: bool = False):
         st = N.RenderStats()
-        N.check(self.lib.gbpt_render_device(self.handle, sid, C.byref(camera), C.byref(params),
+        self._check(self.lib.gbpt_render_device(self.handle, sid, C.byref(camera), C.byref(params),
                                             out_ptr, C.byref(st) if stats else None))
         return st if stats else None
 
     def trace_primary(self, sid: int, camera: N.Camera, width: int, height: int,
                       mask: int = 0xFF) -> np.ndarray:
         hits = np.zeros(width * height, N.HIT_DTYPE)
-        N.check(self.lib.gbpt_trace_primary(self.handle, sid, C.byref(camera), width, height, mask,
+        self._check(self.lib.gbpt_trace_primary(self.handle, sid, C.byref(camera), width, height, mask,
                                             N.ptr(hits)))
         return hits
 
@@ -325,21 +340,21 @@ class Context:
               any_hit: bool = False, counted: bool = False):
         if counted:
             a, b = C.c_double(), C.c_double()
-            N.check(self.lib.gbpt_trace_counted(self.handle, sid, rays_dev, n, mask, int(any_hit),
+            self._check(self.lib.gbpt_trace_counted(self.handle, sid, rays_dev, n, mask, int(any_hit),
                                                 hits_dev, C.byref(a), C.byref(b)))
             return a.value, b.value
-        N.check(self.lib.gbpt_trace(self.handle, sid, rays_dev, n, mask, int(any_hit), hits_dev))
+        self._check(self.lib.gbpt_trace(self.handle, sid, rays_dev, n, mask, int(any_hit), hits_dev))
         return None
 
     def synchronize(self) -> None:
-        N.check(self.lib.gbpt_synchronize(self.handle))
+        self._check(self.lib.gbpt_synchronize(self.handle))
 
     def set_profiling(self, level: int) -> None:
-        N.check(self.lib.gbpt_set_profiling(self.handle, level))
+        self._check(self.lib.gbpt_set_profiling(self.handle, level))
 
     def memory_info(self) -> dict:
         f, t, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
-        N.check(self.lib.gbpt_memory_info(self.handle, C.byref(f), C.byref(t), C.byref(c)))
+        self._check(self.lib.gbpt_memory_info(self.handle, C.byref(f), C.byref(t), C.byref(c)))
         return dict(free=f.value, total=t.value, ctx=c.value)
 
     # ---- batches and the request server ----------------------------------------------------
@@ -362,22 +377,22 @@ class Context:
             outs.append(np.empty((n, 4), np.float32))
             reqs[i] = self.request(sid, cam, params, out_host=outs[-1])
         st = N.RenderStats()
-        N.check(self.lib.gbpt_render_batch(self.handle, reqs, len(jobs),
+        self._check(self.lib.gbpt_render_batch(self.handle, reqs, len(jobs),
                                            C.byref(st) if stats else None))
         return (outs, st) if stats else outs
 
     def set_graphs(self, enable: bool) -> None:
-        N.check(self.lib.gbpt_set_graphs(self.handle, int(enable)))
+        self._check(self.lib.gbpt_set_graphs(self.handle, int(enable)))
 
     def set_tuning(self, wave_paths: int = 0, sort_materials: int = -1,
                    use_graphs: bool = False, bvh_build: int = N.BVH_SPLIT,
                    streams: int = 0) -> None:
         t = N.Tuning(wave_paths, sort_materials, int(use_graphs), bvh_build, streams)
-        N.check(self.lib.gbpt_set_tuning(self.handle, C.byref(t)))
+        self._check(self.lib.gbpt_set_tuning(self.handle, C.byref(t)))
 
     def get_tuning(self) -> N.Tuning:
         t = N.Tuning()
-        N.check(self.lib.gbpt_get_tuning(self.handle, C.byref(t)))
+        self._check(self.lib.gbpt_get_tuning(self.handle, C.byref(t)))
         return t
 
     def autotune(self, sid: int, camera: N.Camera, params: N.RenderParams):
@@ -385,7 +400,7 @@ class Context:
         tuning and the candidates' times (ms, tick size major, sorting minor)."""
         t = N.Tuning()
         ms = (C.c_double * 8)(*([float("nan")] * 8))
-        N.check(self.lib.gbpt_autotune(self.handle, sid, C.byref(camera), C.byref(params),
+        self._check(self.lib.gbpt_autotune(self.handle, sid, C.byref(camera), C.byref(params),
                                        C.byref(t), ms))
         return t, [v for v in ms if v == v]
 
@@ -395,17 +410,17 @@ class Context:
     def server_start(self, wave_paths: int = 0, arena_bytes: int = 0, use_graphs: bool = False,
                      max_active: int = 0) -> None:
         cfg = N.ServerConfig(wave_paths, arena_bytes, int(use_graphs), max_active)
-        N.check(self.lib.gbpt_server_start(self.handle, C.byref(cfg)))
+        self._check(self.lib.gbpt_server_start(self.handle, C.byref(cfg)))
 
     def server_stop(self) -> None:
-        N.check(self.lib.gbpt_server_stop(self.handle))
+        self._check(self.lib.gbpt_server_stop(self.handle))
 
     def submit(self, sid: int, camera: N.Camera, params: N.RenderParams,
                out_host: np.ndarray | None = None, out_device: int | None = None) -> int:
         """Queues a request; out_host (or the device buffer) must stay alive until it finishes."""
         t = C.c_uint64()
         r = self.request(sid, camera, params, out_host, out_device)
-        N.check(self.lib.gbpt_server_submit(self.handle, C.byref(r), C.byref(t)))
+        self._check(self.lib.gbpt_server_submit(self.handle, C.byref(r), C.byref(t)))
         return t.value
 
     def poll(self, ticket: int) -> tuple[int, N.RequestStatus]:
@@ -419,12 +434,12 @@ class Context:
         return rc, st
 
     def cancel(self, ticket: int) -> None:
-        N.check(self.lib.gbpt_server_cancel(self.handle, ticket))
+        self._check(self.lib.gbpt_server_cancel(self.handle, ticket))
 
     def release(self, ticket: int) -> None:
-        N.check(self.lib.gbpt_server_release(self.handle, ticket))
+        self._check(self.lib.gbpt_server_release(self.handle, ticket))
 
     def server_info(self) -> dict:
         st = N.ServerStats()
-        N.check(self.lib.gbpt_server_info(self.handle, C.byref(st)))
+        self._check(self.lib.gbpt_server_info(self.handle, C.byref(st)))
         return {k: getattr(st, k) for k, _ in N.ServerStats._fields_}

@@ -14,7 +14,9 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
-SOURCES = [HERE / "oracle.cpp", HERE / "oracle_math.h", HERE.parent / "include" / "gbpt.h"]
+SOURCES = [HERE / "oracle.cpp", HERE / "oracle_math.h", HERE.parent / "include" / "gbpt.h",
+           HERE.parent / "merian_gb300" / "csrc" / "scenegen.cpp",
+           HERE.parent / "merian_gb300" / "csrc" / "host_common.h"]
 
 _lib = None
 
@@ -38,13 +40,23 @@ def load() -> C.CDLL:
         lib.oracle_scene_destroy.argtypes = [vp]
         lib.oracle_trace_primary.argtypes = [vp, vp, u32, u32, u32, i32, vp, vp]
         lib.oracle_trace_rays.argtypes = [vp, vp, u32, u32, i32, i32, vp, vp, vp]
-        lib.oracle_render.argtypes = [vp, vp, vp, i32, i32, vp, vp, vp]
+        lib.oracle_render.argtypes = [vp, vp, vp, i32, i32, vp, vp, vp, vp]
         lib.oracle_num_threads.restype = i32
         lib.oracle_gbuffer.argtypes = [vp, vp, u32, u32, u32, vp]
         lib.oracle_scene_set_instances.argtypes = [vp, vp, u32, vp, u32]
         lib.oracle_scene_set_textures.argtypes = [vp, vp, u32]
         lib.oracle_bsdf_check.argtypes = [i32, vp, vp, f32, f32, vp, f32, f32, u32, u32, vp]
         lib.oracle_material_samples.argtypes = [vp, i32, f32, vp, u32, u32, vp]
+        fp = C.POINTER(C.c_float)
+        lib.oracle_camera_look_at.argtypes = [fp, fp, fp, f32, f32, f32, f32, vp]
+        lib.oracle_camera_look_at.restype = i32
+        # the seeded scene generators, compiled into this library from the package's source
+        from merian_gb300 import _native as N
+        for name, res, args in N.EXPORTS:
+            if name.startswith("gbpt_gen_"):
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
         _lib = lib
     return _lib
 
@@ -110,15 +122,49 @@ class OracleScene:
         load().oracle_gbuffer(self.h, C.addressof(camera), width, height, mask, _p(out))
         return out
 
-    def render(self, camera, params, fp64: bool = True, threads: int = 0):
-        """(rgba (n,4) float64, mean of squared per-sample rgb (n,3), traced rays)."""
+    def render(self, camera, params, fp64: bool = True, threads: int = 0, lum4: bool = False):
+        """(rgba (n,4) float64, mean of squared per-sample rgb (n,3), traced rays); with lum4 a
+        fourth element, the per-pixel mean of luminance^4 (n,): the second moment of the samples
+        the `a` channel (mean luminance^2) averages."""
         n = params.pixel_count or params.width * params.height
         rgba = np.zeros((n, 4), np.float64)
         sq = np.zeros((n, 3), np.float64)
+        l4 = np.zeros(n, np.float64) if lum4 else None
         rays = C.c_uint64()
         load().oracle_render(self.h, C.addressof(camera), C.addressof(params), int(fp64), threads,
-                             _p(rgba), _p(sq), C.addressof(rays))
+                             _p(rgba), _p(sq), _p(l4) if lum4 else None, C.addressof(rays))
+        if lum4:
+            return rgba, sq, rays.value, l4
         return rgba, sq, rays.value
+
+
+def generator() -> C.CDLL:
+    """This library as the source of the seeded scene generators (gbpt_gen_*): pass it as
+    ``lib=`` to ``merian_gb300.scene``'s factories to build a scene without the CUDA library."""
+    return load()
+
+
+def look_at(position, target, up=(0.0, 1.0, 0.0), vfov_deg: float = 40.0, aspect: float = 1.0,
+            near: float = 0.1, far: float = 1000.0):
+    """merian's pinhole basis from the oracle's own restatement (oracle_camera_look_at)."""
+    import math
+    from merian_gb300 import _native as N
+    cam = N.Camera()
+    f3 = C.c_float * 3
+    rc = load().oracle_camera_look_at(f3(*position), f3(*target), f3(*up), math.radians(vfov_deg),
+                                      aspect, near, far, C.addressof(cam))
+    if rc != 0:
+        raise ValueError("oracle_camera_look_at: bad arguments")
+    return cam
+
+
+def workload_camera(name: str, width: int | None = None, height: int | None = None):
+    """The camera of a named workload (merian_gb300.scene.WORKLOADS), from look_at above."""
+    from merian_gb300 import scene as S
+    w = S.WORKLOADS[name]
+    c = w["camera"]
+    return look_at(c["position"], c["target"], (0.0, 1.0, 0.0), c["vfov_deg"],
+                   (width or w["width"]) / (height or w["height"]))
 
 
 def num_threads() -> int:

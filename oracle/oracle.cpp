@@ -14,6 +14,7 @@
 #include <atomic>
 #include <cfloat>
 #include <chrono>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -1158,7 +1159,7 @@ V3<R> trace_path(const Scene& s, const PathCfg& cfg, Ray<R> ray, SP<R> sp, Pcg& 
 template <class R>
 void render_pixel(const Scene& s, const gbpt_camera& cam, const gbpt_render_params& p,
                   const PathCfg& cfg, uint32_t px, uint32_t py, double* rgba, double* sq,
-                  PathCounters& ctr) {
+                  double* lum4, PathCounters& ctr) {
     const Ray<R> primary = camera_ray<R>(cam, px, py, p.width, p.height);
     ctr.rays++;
     const HitRec h = trace<R>(s, primary, cfg.mask, false);
@@ -1171,7 +1172,7 @@ void render_pixel(const Scene& s, const gbpt_camera& cam, const gbpt_render_para
         const V3<R> a = g.has_material ? g.bsdf.get_albedo(g.frame.to_local(-primary.d)) : g.emission;
         demod = mk(maxr(a.x, R(1e-2f)), maxr(a.y, R(1e-2f)), maxr(a.z, R(1e-2f)));
     }
-    double acc[3] = {0, 0, 0}, sm = 0.0, s2[3] = {0, 0, 0};
+    double acc[3] = {0, 0, 0}, sm = 0.0, s2[3] = {0, 0, 0}, s4 = 0.0;
     for (int smp = 0; smp < p.spp; ++smp) {
         Pcg rng{pcg4d16(px, py, p.frame, (uint32_t)smp)};
         const V3<R> c = trace_path<R>(s, cfg, primary, psp, rng, ctr) / demod;
@@ -1186,6 +1187,7 @@ void render_pixel(const Scene& s, const gbpt_camera& cam, const gbpt_render_para
         s2[2] += (double)c.z * (double)c.z;
         const double l = (double)yuv_luminance(c);
         sm += l * l;
+        s4 += (l * l) * (l * l);
     }
     const double inv = p.spp > 0 ? 1.0 / p.spp : 0.0;
     rgba[0] = acc[0] * inv;
@@ -1197,16 +1199,19 @@ void render_pixel(const Scene& s, const gbpt_camera& cam, const gbpt_render_para
         sq[1] = s2[1] * inv;
         sq[2] = s2[2] * inv;
     }
+    // the second moment of the `a` channel's samples: its variance is E[l^4] - E[l^2]^2
+    if (lum4) *lum4 = s4 * inv;
 }
 
 } // namespace oracle
 
 // Renders the listed pixels (or all) at p->spp. out_rgba: 4 doubles per pixel (mean rgb, mean
-// luminance^2); out_sq (optional): 3 doubles per pixel, mean of the squared per-sample rgb.
-// threads <= 0 uses every host thread. Returns the number of traced rays in *out_rays.
+// luminance^2); out_sq (optional): 3 doubles per pixel, mean of the squared per-sample rgb;
+// out_lum4 (optional): 1 double per pixel, mean of luminance^4. threads <= 0 uses every host
+// thread. Returns the number of traced rays in *out_rays.
 ORACLE_API int oracle_render(void* sp, const gbpt_camera* cam, const gbpt_render_params* p,
                              int fp64, int threads, double* out_rgba, double* out_sq,
-                             uint64_t* out_rays) {
+                             double* out_lum4, uint64_t* out_rays) {
     const Scene& s = *(const Scene*)sp;
     PathCfg cfg{p->max_path_length, p->emission_on_primary != 0, p->instance_mask & 0xFFu,
                 p->nee != 0, p->rr_depth};
@@ -1225,10 +1230,11 @@ ORACLE_API int oracle_render(void* sp, const gbpt_camera* cam, const gbpt_render
             const uint32_t pix = p->pixel_count ? p->pixels[i] : (uint32_t)i;
             const uint32_t px = pix % p->width, py = pix / p->width;
             double* sq = out_sq ? out_sq + 3 * i : nullptr;
+            double* l4 = out_lum4 ? out_lum4 + i : nullptr;
             if (fp64)
-                render_pixel<double>(s, *cam, *p, cfg, px, py, out_rgba + 4 * i, sq, ctr);
+                render_pixel<double>(s, *cam, *p, cfg, px, py, out_rgba + 4 * i, sq, l4, ctr);
             else
-                render_pixel<float>(s, *cam, *p, cfg, px, py, out_rgba + 4 * i, sq, ctr);
+                render_pixel<float>(s, *cam, *p, cfg, px, py, out_rgba + 4 * i, sq, l4, ctr);
         }
         rays += ctr.rays;
     }
@@ -1334,6 +1340,45 @@ ORACLE_API int oracle_gbuffer(void* sp, const gbpt_camera* cam, uint32_t w, uint
     }
     return 0;
 }
+
+// The pinhole camera basis of merian's Camera (camera.cpp:263-266 recompute_ray_basis,
+// :349-367 write_to), in float as the host computes it: forward = normalize(target - position),
+// right = normalize(cross(forward, up)), focus = |target - position|, h = tan(vfov / 2);
+// U = right * h * aspect * focus, V = cross(right, forward) * h * focus, W = forward * focus.
+// The oracle's own restatement, so the CPU baseline and the fixtures can set up a camera
+// without the product library.
+ORACLE_API int oracle_camera_look_at(const float* position, const float* target, const float* up,
+                                     float vfov, float aspect, float near_plane, float far_plane,
+                                     gbpt_camera* out) {
+    using namespace oracle;
+    if (!position || !target || !up || !out) return -1;
+    const V3<float> o = mk(position[0], position[1], position[2]);
+    const V3<float> to_target = mk(target[0], target[1], target[2]) - o;
+    const V3<float> forward = normalize(to_target);
+    const V3<float> right = normalize(cross(forward, mk(up[0], up[1], up[2])));
+    const float focus = std::sqrt(dot(to_target, to_target));
+    const float h = std::tan(vfov * 0.5f);
+    const V3<float> basis[4] = {o, (h * aspect * focus) * right,
+                                (h * focus) * cross(right, forward), focus * forward};
+    std::memset(out, 0, sizeof(*out));
+    float* dst[4] = {out->position, out->U, out->V, out->W};
+    for (int k = 0; k < 4; ++k) {
+        dst[k][0] = basis[k].x;
+        dst[k][1] = basis[k].y;
+        dst[k][2] = basis[k].z;
+    }
+    out->near_plane = near_plane;
+    out->far_plane = far_plane;
+    return 0;
+}
+
+// The scene generators compiled into this library report argument errors through
+// gbpt::set_error; here the message is kept for oracle_last_error.
+namespace gbpt {
+static thread_local std::string g_oracle_error;
+void set_error(const std::string& msg) { g_oracle_error = msg; }
+} // namespace gbpt
+ORACLE_API const char* oracle_last_error(void) { return gbpt::g_oracle_error.c_str(); }
 
 ORACLE_API int oracle_num_threads(void) {
 #ifdef _OPENMP

@@ -3,7 +3,10 @@
 The reference (merian's Vulkan/Slang `pt`) cannot run here, so its estimator is pinned by the
 FP64 CPU oracle (oracle/oracle.cpp, a restatement of render_pt.slang): each fixture holds, for a
 seeded subset of pixels, the oracle's per-pixel mean radiance over many BSDF-only samples and the
-per-sample variance, plus a hash of the scene arrays it was computed on.
+per-sample variance, the output's `a` channel (mean squared luminance) with the variance of its
+samples, plus a hash of the scene arrays it was computed on. Scenes and cameras come from the
+oracle library (the seeded generators compiled into it and its own camera basis), so making a
+fixture never loads the CUDA library; the GPU tests re-hash the scene the package generates.
 
     python tests/golden/make_golden.py [--quick]
 """
@@ -37,15 +40,22 @@ def scene_hash(sc) -> str:
 
 # name -> (scene factory, camera, width, height, max_path_length, n_pixels, spp)
 def cases():
+    gen = O.generator()
     return {
         "cornell": dict(
-            scene=lambda: S.cornell(S.BASE_SEED),
-            camera=lambda: S.workload_camera("cornell-256-16spp"),
+            scene=lambda: S.cornell(S.BASE_SEED, lib=gen),
+            camera=lambda: O.workload_camera("cornell-256-16spp"),
             width=256, height=256, max_path_length=5, n_pixels=1024, spp=65536),
         "soup_small": dict(
-            scene=lambda: S.soup(S.BASE_SEED, 200_000, 256, (256, 128)),
-            camera=lambda: S.look_at((0.5, 0.5, -1.2), (0.5, 0.5, 0.5), (0, 1, 0), 45.0, 16 / 9),
+            scene=lambda: S.soup(S.BASE_SEED, 200_000, 256, (256, 128), lib=gen),
+            camera=lambda: O.look_at((0.5, 0.5, -1.2), (0.5, 0.5, 0.5), (0, 1, 0), 45.0, 16 / 9),
             width=320, height=180, max_path_length=8, n_pixels=512, spp=16384),
+        # the headline configuration: the benchmarked 1M-triangle soup with its 2048x1024
+        # environment, seen by the 1080p camera
+        "soup_1m": dict(
+            scene=lambda: S.workload_scene("soup-1m-1080p-64spp", lib=gen),
+            camera=lambda: O.workload_camera("soup-1m-1080p-64spp"),
+            width=1920, height=1080, max_path_length=8, n_pixels=1024, spp=65536),
     }
 
 
@@ -59,12 +69,14 @@ def make(name: str, c: dict, spp_scale: float = 1.0) -> Path:
     params, keep = S.render_params(w, h, spp, c["max_path_length"], pixels=pixels)
     osc = O.OracleScene(sc)
     t0 = time.time()
-    rgba, sq, rays = osc.render(cam, params, fp64=True)
+    rgba, sq, rays, lum4 = osc.render(cam, params, fp64=True, lum4=True)
     dt = time.time() - t0
     mean = rgba[:, :3]
     var = np.maximum(sq - mean * mean, 0.0)
+    var_lum2 = np.maximum(lum4 - rgba[:, 3] ** 2, 0.0)
     out = HERE / f"{name}.npz"
-    np.savez_compressed(out, pixels=pixels, mean=mean, var=var, lum2=rgba[:, 3], spp=spp,
+    np.savez_compressed(out, pixels=pixels, mean=mean, var=var, lum2=rgba[:, 3],
+                        var_lum2=var_lum2, spp=spp,
                         width=w, height=h, max_path_length=c["max_path_length"],
                         scene_hash=scene_hash(sc), oracle_seconds=dt, rays=rays)
     print(f"{name}: {len(pixels)} px x {spp} spp in {dt:.1f} s -> {out}")

@@ -8,7 +8,12 @@ Tolerances:
   * per-pixel mean radiance vs the FP64 oracle fixture: |z| > 3 on at most 2% of the channels and
     mean z^2 < 1.5 (z = difference over the combined standard error of both estimators, floored
     at 1e-5 relative for FP32 round-off); the relative RMSE must be explained by that noise
-    (at most 1.25x the noise RMSE).
+    (at most 1.25x the noise RMSE);
+  * the output's `a` channel (mean squared YUV luminance, render_pt.slang:110-129) vs the
+    fixture's, by the same z test, for the BSDF-only estimator: the fixtures hold the reference's
+    BSDF-only estimator, and a second moment, unlike the mean, depends on the estimator (NEE and
+    roulette change the distribution of the samples, not their expectation).
+The relative RMSE against the fixture is printed per configuration and estimator.
 """
 import numpy as np
 import pytest
@@ -38,6 +43,17 @@ def cornell(gpu_ctx):
     _check_scene_hash(sc, "cornell")
     sid = gpu_ctx.upload(sc)
     yield sc, sid, O.OracleScene(sc), S.workload_camera("cornell-256-16spp")
+    gpu_ctx.destroy_scene(sid)
+
+
+@pytest.fixture(scope="module")
+def soup_1m(gpu_ctx):
+    """The benchmarked 1M-triangle soup with its 2048x1024 environment and the 1080p camera."""
+    from merian_gb300 import scene as S
+    sc = S.workload_scene("soup-1m-1080p-64spp")
+    _check_scene_hash(sc, "soup_1m")
+    sid = gpu_ctx.upload(sc)
+    yield sc, sid, None, S.workload_camera("soup-1m-1080p-64spp")
     gpu_ctx.destroy_scene(sid)
 
 
@@ -118,20 +134,13 @@ def test_incoherent_rays_match_oracle(gpu_ctx, which, request):
     assert np.array_equal(ga["geometry_index"] != 0xFFFFFFFF, o["geometry_index"] != 0xFFFFFFFF)
 
 
-def _stat_compare(gpu_ctx, sid, cam, g, nee, rr, frames=8, spp=4096):
-    """GPU per-pixel means (frames x spp samples, variance across frames) vs the FP64 fixture."""
-    from merian_gb300 import scene as S
-    pixels = g["pixels"]
-    w, h, L = int(g["width"]), int(g["height"]), int(g["max_path_length"])
-    outs = []
-    for f in range(frames):
-        params, keep = S.render_params(w, h, spp, L, pixels=pixels, nee=nee, rr_depth=rr,
-                                       frame=1000 + f)
-        outs.append(gpu_ctx.render(sid, cam, params)[:, :3].astype(np.float64))
-    outs = np.stack(outs)
-    m = outs.mean(0)
-    se_g = outs.std(0, ddof=1) / np.sqrt(frames)
-    gm, gv, gn = g["mean"], g["var"], int(g["spp"])
+def _z_rmse(samples, gm, gv, gn):
+    """z scores, relative RMSE and the RMSE sampling noise alone explains, of the per-frame GPU
+    estimates `samples` (frames x pixels [x channels]) against the fixture's mean gm, per-sample
+    variance gv over gn samples."""
+    frames = samples.shape[0]
+    m = samples.mean(0)
+    se_g = samples.std(0, ddof=1) / np.sqrt(frames)
     se_o = np.sqrt(gv / gn)
     # FP32 floor: a zero-variance pixel (the environment seen directly) still differs from the
     # FP64 value by float round-off of the radiance itself
@@ -146,6 +155,26 @@ def _stat_compare(gpu_ctx, sid, cam, g, nee, rr, frames=8, spp=4096):
     return z, rel_rmse, noise_rmse
 
 
+def _stat_compare(gpu_ctx, sid, cam, g, nee, rr, frames=8, spp=4096, lum2=False):
+    """GPU per-pixel means (frames x spp samples; the standard error from the spread across
+    frames, 16 frames so that it is itself well estimated) vs the FP64 fixture;
+    with lum2 also the `a` channel against the fixture's mean squared luminance."""
+    from merian_gb300 import scene as S
+    pixels = g["pixels"]
+    w, h, L = int(g["width"]), int(g["height"]), int(g["max_path_length"])
+    outs = []
+    for f in range(frames):
+        params, keep = S.render_params(w, h, spp, L, pixels=pixels, nee=nee, rr_depth=rr,
+                                       frame=1000 + f)
+        outs.append(gpu_ctx.render(sid, cam, params).astype(np.float64))
+    outs = np.stack(outs)
+    gn = int(g["spp"])
+    rgb = _z_rmse(outs[:, :, :3], g["mean"], g["var"], gn)
+    if not lum2:
+        return rgb
+    return rgb, _z_rmse(outs[:, :, 3], g["lum2"], g["var_lum2"], gn)
+
+
 def _assert_converged(z, rel_rmse, noise_rmse):
     # bias check: the RMSE is explained by the two estimators' sampling noise
     assert np.mean(np.abs(z) > 3) < 0.02
@@ -153,24 +182,41 @@ def _assert_converged(z, rel_rmse, noise_rmse):
     assert rel_rmse < 1.25 * noise_rmse + 1e-4
 
 
+def _check_estimator(gpu_ctx, which, sid, cam, nee, rr, frames, spp):
+    g = golden(which)
+    bsdf_only = not nee and rr == 0
+    res = _stat_compare(gpu_ctx, sid, cam, g, nee, rr, frames=frames, spp=spp, lum2=bsdf_only)
+    rgb, a = (res if bsdf_only else (res, None))
+    z, rel_rmse, noise = rgb
+    print(f"{which} nee={nee} rr={rr}: rel RMSE {rel_rmse:.4%} (noise {noise:.4%}), "
+          f"max|z| {np.abs(z).max():.2f}")
+    _assert_converged(z, rel_rmse, noise)
+    if a is not None:
+        za, rel_a, noise_a = a
+        print(f"{which} a channel (mean luminance^2): rel RMSE {rel_a:.4%} "
+              f"(noise {noise_a:.4%}), max|z| {np.abs(za).max():.2f}")
+        _assert_converged(za, rel_a, noise_a)
+
+
 @pytest.mark.parametrize("nee,rr", [(False, 0), (True, 0), (True, 3)],
                          ids=["bsdf", "nee", "nee_rr"])
 def test_render_cornell_converges_to_oracle(gpu_ctx, cornell, nee, rr):
     sc, sid, osc, cam = cornell
-    z, rel_rmse, noise = _stat_compare(gpu_ctx, sid, cam, golden("cornell"), nee, rr)
-    print(f"cornell nee={nee} rr={rr}: rel RMSE {rel_rmse:.4%} (noise {noise:.4%}), "
-          f"max|z| {np.abs(z).max():.2f}")
-    _assert_converged(z, rel_rmse, noise)
+    _check_estimator(gpu_ctx, "cornell", sid, cam, nee, rr, frames=16, spp=2048)
 
 
 @pytest.mark.parametrize("nee,rr", [(False, 0), (True, 3)], ids=["bsdf", "nee_rr"])
 def test_render_soup_converges_to_oracle(gpu_ctx, soup_small, nee, rr):
     sc, sid, osc, cam = soup_small
-    g = golden("soup_small")
-    z, rel_rmse, noise = _stat_compare(gpu_ctx, sid, cam, g, nee, rr, frames=8, spp=2048)
-    print(f"soup nee={nee} rr={rr}: rel RMSE {rel_rmse:.4%} (noise {noise:.4%}), "
-          f"max|z| {np.abs(z).max():.2f}")
-    _assert_converged(z, rel_rmse, noise)
+    _check_estimator(gpu_ctx, "soup_small", sid, cam, nee, rr, frames=16, spp=1024)
+
+
+@pytest.mark.parametrize("nee,rr", [(False, 0), (True, 3)], ids=["bsdf", "nee_rr"])
+def test_render_headline_soup_converges_to_oracle(gpu_ctx, soup_1m, nee, rr):
+    """The benchmarked configuration (1M triangles, 2048x1024 environment, 1080p camera, path
+    length 8) against its 65,536-spp FP64 fixture."""
+    sc, sid, osc, cam = soup_1m
+    _check_estimator(gpu_ctx, "soup_1m", sid, cam, nee, rr, frames=16, spp=4096)
 
 
 def test_render_deterministic_and_subset_consistent(gpu_ctx, cornell):
