@@ -44,15 +44,18 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tuning", default=None,
-                    help="WAVE_PATHS,SORT[,STREAMS]: a fixed schedule instead of the "
-                         "autotuner's")
+                    help="WAVE_PATHS,SORT[,STREAMS[,REFILL,POSTPONE,BLOCKS_PER_SM]]: a fixed "
+                         "schedule instead of the autotuner's (0 = default)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default schedule instead of gbpt_autotune's choice of tick "
                          "size and material sorting (made before the warm-up, untimed)")
     # the mixed workloads (--workload batch-256 | served-stream)
     ap.add_argument("--scenes", type=int, default=None, help="scenes of a mixed workload")
-    ap.add_argument("--requests", type=int, default=96, help="requests per served-stream rate")
-    ap.add_argument("--rates", default="50,200,2000", help="served-stream arrival rates, req/s")
+    ap.add_argument("--requests", type=int, default=None,
+                    help="requests per served rate (served-stream 96, served-small 512)")
+    ap.add_argument("--rates", default=None,
+                    help="served arrival rates, req/s (served-stream 50,200,2000; served-small "
+                         "2000,10000,50000)")
     return ap.parse_args()
 
 
@@ -195,6 +198,46 @@ def cpu_baseline(scene, camera, w, cpu_seconds: float, kind_label: str = "port")
             "grays_per_s": round(rays / dt / 1e9, 6)}
 
 
+def parity_vs_fixtures(ctx, sid, cam, w):
+    """Relative RMSE of the GPU estimate (headline estimator: NEE + roulette) against the FP64
+    oracle fixtures of this workload (tests/golden, BSDF-only estimator: the reference's), on the
+    fixtures' seeded pixels, untimed:
+      * frame: one frame at the workload's spp on the 1,024 pixels of soup_1m.npz (65,536 spp);
+      * converged: the 64 pixels of soup_1m_deep.npz (2^22 spp each) at the same 2^22 spp.
+    `oracle_noise` is the relative RMSE the fixture's own sampling noise explains; relative RMSE
+    is RMSE over the pixels' rgb divided by the fixture's mean."""
+    from merian_gb300 import scene as S
+    out = {}
+    gold = ROOT / "tests" / "golden"
+    for key, fname, spp, frame in (("frame", "soup_1m.npz", w["spp"], 777),
+                                   ("converged", "soup_1m_deep.npz", None, 778)):
+        f = gold / fname
+        if not f.exists():
+            continue
+        g = np.load(f)
+        pix = g["pixels"].astype(np.uint32)
+        n_spp = int(g["spp"]) if spp is None else spp
+        p, keep = S.render_params(int(g["width"]), int(g["height"]), n_spp,
+                                  int(g["max_path_length"]), pixels=pix, nee=w["nee"],
+                                  rr_depth=w["rr_depth"], frame=frame)
+        est = ctx.render(sid, cam, p)[:, :3].astype(np.float64)
+        scale = float(np.mean(g["mean"]))
+        out[key] = {"fixture": fname, "pixels": int(len(pix)), "spp": n_spp,
+                    "fixture_spp": int(g["spp"]),
+                    "rel_rmse": round(float(np.sqrt(np.mean((est - g["mean"]) ** 2)) / scale), 5),
+                    "oracle_noise": round(float(np.sqrt(np.mean(g["var"] / int(g["spp"])))
+                                                / scale), 5)}
+    return out
+
+
+def tuning_dict(t) -> dict:
+    """The schedule a gbpt_tuning selects, as reported in config.tuning (0 = default)."""
+    return {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials,
+            "streams": t.streams or 2, "trace_refill_lanes": t.trace_refill_lanes or 20,
+            "trace_postpone_lanes": t.trace_postpone_lanes or 6,
+            "trace_blocks_per_sm": t.trace_blocks_per_sm or "all resident"}
+
+
 def build_workload(name):
     from merian_gb300 import scene as S
     w = S.WORKLOADS[name]
@@ -296,14 +339,14 @@ def run_gbpt(args):
     tuning = None
     if args.tuning:
         wave, sort, *more = (int(x) for x in args.tuning.split(","))
-        streams = more[0] if more else 0
-        ctx.set_tuning(wave, sort, streams=streams)
-        tuning = {"wave_paths": wave, "sort_materials": sort, "streams": streams or 2,
-                  "fixed": True}
+        more += [0] * (4 - len(more))
+        streams, refill, postpone, bps = more[:4]
+        ctx.set_tuning(wave, sort, streams=streams, refill_lanes=refill,
+                       postpone_lanes=postpone, blocks_per_sm=bps)
+        tuning = dict(tuning_dict(ctx.get_tuning()), fixed=True)
     elif not args.no_autotune:
         t, cand_ms = ctx.autotune(sid, cam, params(frame_base + 998))
-        tuning = {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials,
-                  "streams": t.streams or 2, "candidates_ms": [round(m, 2) for m in cand_ms]}
+        tuning = dict(tuning_dict(t), candidates_ms=[round(m, 2) for m in cand_ms])
     for i in range(args.warmup):
         ctx.render_device(sid, cam, params(frame_base + i), out.data_ptr())
     torch.cuda.synchronize()
@@ -334,6 +377,10 @@ def run_gbpt(args):
     cst = ctx.render_device(sid, cam, params(frame_base + 999), out.data_ptr(), stats=True)
     nodes_per_ray = cst.nodes_visited / max(cst.trace_rays, 1)
     tris_per_ray = cst.tris_tested / max(cst.trace_rays, 1)
+    simt = {"node_lanes_per_step": round(cst.node_lanes / max(cst.node_steps, 1), 2),
+            "tri_lanes_per_step": round(cst.tri_lanes / max(cst.tri_steps, 1), 2),
+            "node_steps_per_ray": round(cst.node_steps / max(cst.trace_rays, 1), 3),
+            "tri_steps_per_ray": round(cst.tri_steps / max(cst.trace_rays, 1), 3)}
     bytes_per_ray = 48.0 + 80.0 * nodes_per_ray + 48.0 * tris_per_ray
     ctx.set_profiling(1)
 
@@ -358,6 +405,8 @@ def run_gbpt(args):
         launches += st.kernel_launches
         rays += st.rays
     torch.cuda.synchronize()
+
+    parity = parity_vs_fixtures(ctx, sid, cam, w) if args.workload == WORKLOAD else None
 
     # end to end through the public API with a host output buffer (D2H inside the call)
     ctx.set_profiling(0)
@@ -417,6 +466,7 @@ def run_gbpt(args):
                          "bytes_per_ray": round(bytes_per_ray, 1),
                          "nodes_per_ray": round(nodes_per_ray, 3),
                          "tris_per_ray": round(tris_per_ray, 3),
+                         "simt": simt,
                          "launches_per_step": trace_launches // max(args.steps, 1),
                          "trace_rays_per_step": trace_rays // max(args.steps, 1),
                          "trace_share_of_step": round(trace_ms / float(np.sum(prof_ms)), 4),
@@ -426,6 +476,8 @@ def run_gbpt(args):
         }
         if tuning is not None:
             line["config"]["tuning"] = tuning
+        if parity:
+            line["rel_rmse_vs_fp64"] = parity
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(sc, cam, w, args.cpu_seconds)
         print(json.dumps(line), flush=True)
@@ -444,14 +496,17 @@ def run_batch_mix(args):
     """Config 3: independent scenes (triangles log-uniform 1k-2M), one request each, rendered
     by plain per-request gbpt_render_device launches and by one gbpt_render_batch call (with and
     without CUDA-graph replay of the ticks). All outputs stay in HBM; the outputs of both paths
-    are compared bit for bit."""
+    are compared bit for bit. batch-256: requests of 256^2-1024^2 at 1-64 spp; batch-small: the
+    same scenes with requests of 64^2-512^2 at 1-4 spp, where one request alone cannot fill the
+    GPU, timed per resolution bucket as well."""
     import torch
     from merian_gb300 import _native as N
     from merian_gb300 import scene as S
     from merian_gb300 import workloads as WL
     torch.cuda.set_device(0)
     n = args.scenes or 256
-    specs, reqs = WL.batch_mix(S.BASE_SEED, n)
+    small = args.workload == "batch-small"
+    specs, reqs = (WL.batch_small if small else WL.batch_mix)(S.BASE_SEED, n)
     # the context renders on this stream (gbpt_create with 0 would make a private one): events
     # recorded on it order with every launch of a step, including the second tick stream's
     stream = torch.cuda.Stream()
@@ -476,15 +531,20 @@ def run_batch_mix(args):
         # one schedule for both arms, tuned on the batch's largest whole-frame request
         k = max(range(n), key=lambda i: reqs[i].width * reqs[i].height * reqs[i].spp)
         t, cand = ctx.autotune(*jobs[k])
-        tuning = {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials,
-                  "tuned_on_request": k, "candidates_ms": [round(m, 2) for m in cand]}
+        tuning = dict(tuning_dict(t), tuned_on_request=k,
+                      candidates_ms=[round(m, 2) for m in cand])
 
-    def plain():
-        for (sid, cam, p), o in zip(jobs, out_plain):
-            ctx.render_device(sid, cam, p, o.data_ptr())
+    def plain(sel=None):
+        for i in (range(n) if sel is None else sel):
+            sid, cam, p = jobs[i]
+            ctx.render_device(sid, cam, p, out_plain[i].data_ptr())
 
-    def batched():
-        N.check(ctx.lib.gbpt_render_batch(ctx.handle, creqs, n, None))
+    def batched(sel=None):
+        if sel is None:
+            N.check(ctx.lib.gbpt_render_batch(ctx.handle, creqs, n, None))
+            return
+        sub = (N.Request * len(sel))(*[creqs[i] for i in sel])
+        N.check(ctx.lib.gbpt_render_batch(ctx.handle, sub, len(sel), None))
 
     def timed(fn):
         for _ in range(args.warmup):
@@ -501,12 +561,31 @@ def run_batch_mix(args):
             ts.append(e0.elapsed_time(e1))
         return float(np.mean(ts))
 
+    per_bucket = {}
     with ClockSampler(0) as clk:
         ms_plain = timed(plain)
         ms_batch = timed(batched)
         ctx.set_graphs(True)
         ms_graph = timed(batched)
         ctx.set_graphs(False)
+        if small:
+            for res in WL.SMALL_RESOLUTIONS:
+                sel = [i for i, r in enumerate(reqs) if (r.width, r.height) == res]
+                if not sel:
+                    continue
+                smp = sum(reqs[i].width * reqs[i].height * reqs[i].spp for i in sel)
+                bp = timed(lambda: plain(sel))
+                bb = timed(lambda: batched(sel))
+                ctx.set_graphs(True)
+                bg = timed(lambda: batched(sel))
+                ctx.set_graphs(False)
+                rate = lambda ms: round(smp / (ms / 1e3) / 1e6, 3)
+                per_bucket[f"{res[0]}x{res[1]}"] = {
+                    "requests": len(sel), "samples": smp,
+                    "plain": {"value": rate(bp), "ms": round(bp, 3)},
+                    "batched": {"value": rate(bb), "ms": round(bb, 3)},
+                    "batched_graphs": {"value": rate(bg), "ms": round(bg, 3)},
+                    "speedup_vs_plain": round(bp / min(bb, bg), 3)}
     identical = all(torch.equal(a.view(torch.int32), b.view(torch.int32))
                     for a, b in zip(out_plain, out_batch))
     mps = lambda ms: round(samples / (ms / 1e3) / 1e6, 3)
@@ -514,25 +593,30 @@ def run_batch_mix(args):
     line = {
         "metric": "Msamples/s of a request batch: one tick engine for all requests vs plain "
                   "per-request launches (same outputs, bit for bit)",
-        "workload": "batch-256", "value": mps(best), "unit": "Msamples/s",
+        "workload": args.workload, "value": mps(best), "unit": "Msamples/s",
         "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(best, 3), "dtype": "f32", "data": "synthetic",
         "plain": {"value": mps(ms_plain), "ms_per_step": round(ms_plain, 3)},
         "batched": {"value": mps(ms_batch), "ms_per_step": round(ms_batch, 3)},
         "batched_graphs": {"value": mps(ms_graph), "ms_per_step": round(ms_graph, 3)},
         "speedup_vs_plain": round(ms_plain / best, 3),
+        "target": "batched >= 2x plain samples/s",
         "outputs_identical": identical,
         "clocks": clk.summary(),
-        "config": {"workload": "batch-256", "scenes": n, "requests": n,
+        "config": {"workload": args.workload, "scenes": n, "requests": n,
                    "triangles_total": sum(s.triangles for s in specs),
                    "cornell_scenes": sum(s.kind == "cornell" for s in specs),
                    "samples_per_step": samples,
-                   "resolutions": "256^2 / 512^2 / 1024^2", "spp": "uniform 1..64",
+                   "resolutions": ("64^2 / 128^2 / 256^2 / 512^2" if small
+                                   else "256^2 / 512^2 / 1024^2"),
+                   "spp": "1 / 2 / 4" if small else "uniform 1..64",
                    "estimator": "NEE + RR from 3; path length 5 (Cornell) / 8 (soup)",
                    "scene_setup_s": round(setup_s, 1),
                    "l2": "flushed between timed steps (256 MiB write)",
                    "tuning": tuning},
     }
+    if per_bucket:
+        line["per_resolution"] = per_bucket
     print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -570,8 +654,7 @@ def run_instanced(args):
     if not args.no_autotune:
         p0, _ = S.render_params(W_, H_, spp, L, nee=True, rr_depth=3, frame=999_999)
         t, cand = ctx.autotune(sid, cam, p0)
-        tuning = {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials,
-                  "candidates_ms": [round(m, 2) for m in cand]}
+        tuning = dict(tuning_dict(t), candidates_ms=[round(m, 2) for m in cand])
 
     def step(base):
         for f in range(frames):
@@ -634,7 +717,11 @@ def run_served(args):
     from merian_gb300 import workloads as WL
     torch.cuda.set_device(0)
     n_scenes = args.scenes or 32
-    rates = [float(x) for x in args.rates.split(",") if x]
+    small = args.workload == "served-small"
+    rates = [float(x) for x in (args.rates or ("2000,10000,50000" if small else "50,200,2000"))
+             .split(",") if x]
+    n_requests = args.requests or (512 if small else 96)
+    mix = WL.served_small if small else WL.served_stream
     specs, _ = WL.served_stream(S.BASE_SEED, n_scenes, 0)
     ctx = S.Context(0)
     t0 = time.perf_counter()
@@ -643,7 +730,7 @@ def run_served(args):
     results = []
 
     def prepare(rate):
-        _, reqs = WL.served_stream(S.BASE_SEED, n_scenes, args.requests, rate)
+        _, reqs = mix(S.BASE_SEED, n_scenes, n_requests, rate)
         new_scenes = {i: r.upload.build() for i, r in enumerate(reqs) if r.upload}
         return reqs, new_scenes
 
@@ -654,11 +741,10 @@ def run_served(args):
     tuning = None
     if not args.no_autotune:
         # one schedule for the server and the serial queue, tuned on the largest request
-        _, reqs0 = WL.served_stream(S.BASE_SEED, n_scenes, args.requests, rates[0])
+        _, reqs0 = mix(S.BASE_SEED, n_scenes, n_requests, rates[0])
         big = max((r for r in reqs0 if not r.upload), key=lambda r: r.width * r.height * r.spp)
         t, cand = ctx.autotune(*job(big, sids[big.scene]))
-        tuning = {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials,
-                  "candidates_ms": [round(m, 2) for m in cand]}
+        tuning = dict(tuning_dict(t), candidates_ms=[round(m, 2) for m in cand])
 
     with ClockSampler(0) as clk:
         for rate in rates:
@@ -716,15 +802,19 @@ def run_served(args):
     line = {
         "metric": "served p50/p99 latency and Msamples/s: request server (continuous batching) "
                   "vs a serial queue of plain gbpt_render calls, same arrivals",
-        "workload": "served-stream", "value": best["served"]["msamples_per_s"],
+        "workload": args.workload, "value": best["served"]["msamples_per_s"],
         "unit": "Msamples/s", "higher_is_better": True, "n_gpus": 1, "dtype": "f32",
         "data": "synthetic", "rates": results, "clocks": clk.summary(),
-        "config": {"workload": "served-stream", "resident_scenes": n_scenes,
+        "target": "served >= 2x the serial plain queue's samples/s",
+        "config": {"workload": args.workload, "resident_scenes": n_scenes,
                    "triangles_resident": sum(s.triangles for s in specs),
-                   "requests_per_rate": args.requests,
-                   "resolutions": "512^2 / 1024^2 / 1920x1080", "spp": "1 / 4 / 16 / 64",
-                   "uploads": "5 % of requests bring a new 100k-triangle soup (BVH build + "
-                              "upload inside the request's latency)",
+                   "requests_per_rate": n_requests,
+                   "resolutions": ("64^2 / 128^2 / 256^2 / 512^2" if small
+                                   else "512^2 / 1024^2 / 1920x1080"),
+                   "spp": "1 / 2 / 4" if small else "1 / 4 / 16 / 64",
+                   "uploads": ("none" if small else
+                               "5 % of requests bring a new 100k-triangle soup (BVH build + "
+                               "upload inside the request's latency)"),
                    "estimator": "NEE + RR from 3; path length 5 (Cornell) / 8 (soup)",
                    "scene_setup_s": round(setup_s, 1), "tuning": tuning},
     }
@@ -762,7 +852,8 @@ def main():
     rc = launch_ranks(args)
     if rc is not None:
         sys.exit(rc)
-    mixed = args.workload in ("batch-256", "served-stream", "instanced-4k")
+    mixed = args.workload in ("batch-256", "batch-small", "served-stream", "served-small",
+                              "instanced-4k")
     if args.steps is None:
         args.steps = 1 if mixed else 5
     if args.warmup is None:
@@ -771,9 +862,9 @@ def main():
         if mixed:  # the CPU reference is timed on the headline frame only
             args.workload = WORKLOAD
         run_reference(args)
-    elif args.workload == "batch-256":
+    elif args.workload in ("batch-256", "batch-small"):
         run_batch_mix(args)
-    elif args.workload == "served-stream":
+    elif args.workload in ("served-stream", "served-small"):
         run_served(args)
     elif args.workload == "instanced-4k":
         run_instanced(args)

@@ -30,7 +30,7 @@ extern "C" {
 #define GBPT_API __attribute__((visibility("default")))
 #endif
 
-#define GBPT_ABI_VERSION 1u
+#define GBPT_ABI_VERSION 2u
 
 /* ---- status codes ------------------------------------------------------------------------ */
 #define GBPT_OK 0
@@ -195,6 +195,10 @@ typedef struct gbpt_render_stats {
     uint64_t trace_rays;   /* rays through the closest-hit traversal launches */
     uint64_t nodes_visited; /* level 2: CWBVH nodes visited by those rays */
     uint64_t tris_tested;   /* level 2: triangles tested by those rays */
+    /* level 2, SIMT activity of those launches: warp-wide node steps and triangle-test steps,
+     * and the lanes active in them (lanes / steps = active lanes of 32 per step) */
+    uint64_t node_steps, node_lanes;
+    uint64_t tri_steps, tri_lanes;
 } gbpt_render_stats;
 
 /* Closest hit of one ray, merian Hit (hit.slang:25-65) plus the distance. Misses have
@@ -332,6 +336,13 @@ typedef struct gbpt_tuning {
                                own work buffers, so one tick's last launches overlap the next
                                tick's first (not while profiling); 1 = ticks in order on the
                                context stream */
+    /* warp scheduling of the persistent traversal launches, 0 = default each */
+    int32_t trace_refill_lanes;   /* a warp refills its idle lanes with new rays once fewer than
+                                     this many lanes are busy: [1, 32], default 20 */
+    int32_t trace_postpone_lanes; /* a lane pushes its triangle group for later when fewer than
+                                     this many lanes have triangles to test: [1, 32], default 6 */
+    int32_t trace_blocks_per_sm;  /* 128-thread blocks per SM of the traversal launches: [1, 64],
+                                     capped at what is resident; default all resident */
 } gbpt_tuning;
 
 /* BVH build of gbpt_scene_create (the traversal finds the same hits in every case). */
@@ -342,10 +353,15 @@ typedef struct gbpt_tuning {
 
 GBPT_API int gbpt_set_tuning(gbpt_ctx* ctx, const gbpt_tuning* tuning);
 GBPT_API int gbpt_get_tuning(gbpt_ctx* ctx, gbpt_tuning* tuning);
-/* Autotuner: renders the frame (camera, params: a whole frame, no pixel list) under each
- * candidate tick size (2^21 .. 2^24 paths) with material sorting off and on, keeps the fastest as
- * the context's tuning and returns it. ms_out, when non-NULL, receives the time of each candidate
- * (up to 8, ordered tick size major, sorting minor). Outputs are discarded. */
+/* Autotuner: renders the frame (camera, params: a whole frame, no pixel list) under candidate
+ * schedules and keeps the fastest as the context's tuning, returning it. Stage 1: each tick size
+ * (2^21 .. 2^24 paths) with material sorting off and on (8 candidates); then, from the best so far,
+ * one parameter at a time: trace_refill_lanes in {12, 16, 20, 24, 28} (5), trace_postpone_lanes in
+ * {2, 4, 6, 8, 12} (5), trace_blocks_per_sm in {6, 7, all resident} (3). ms_out, when non-NULL,
+ * receives GBPT_AUTOTUNE_CANDIDATES times in that order (NaN for candidates not run). Results are
+ * cached per (scene size, frame size, path length, estimator) bucket: a repeated call for the same
+ * bucket applies the cached tuning without rendering. Outputs are discarded. */
+#define GBPT_AUTOTUNE_CANDIDATES 32
 GBPT_API int gbpt_autotune(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
                            const gbpt_render_params* params, gbpt_tuning* out, double* ms_out);
 

@@ -84,7 +84,9 @@ class RenderStats(C.Structure):
                 ("trace_ms", C.c_double), ("shade_ms", C.c_double), ("shadow_ms", C.c_double),
                 ("other_ms", C.c_double), ("trace_launches", C.c_uint64),
                 ("trace_rays", C.c_uint64), ("nodes_visited", C.c_uint64),
-                ("tris_tested", C.c_uint64)]
+                ("tris_tested", C.c_uint64), ("node_steps", C.c_uint64),
+                ("node_lanes", C.c_uint64), ("tri_steps", C.c_uint64),
+                ("tri_lanes", C.c_uint64)]
 
 
 class EnvMap(C.Structure):
@@ -136,7 +138,12 @@ class ServerStats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("wave_paths", C.c_uint64), ("sort_materials", C.c_int32),
-                ("use_graphs", C.c_int32), ("bvh_build", C.c_int32), ("streams", C.c_int32)]
+                ("use_graphs", C.c_int32), ("bvh_build", C.c_int32), ("streams", C.c_int32),
+                ("trace_refill_lanes", C.c_int32), ("trace_postpone_lanes", C.c_int32),
+                ("trace_blocks_per_sm", C.c_int32)]
+
+
+AUTOTUNE_CANDIDATES = 32
 
 
 BVH_SPLIT, BVH_FAST, BVH_MEDIUM = 0, 1, 2

@@ -7,6 +7,7 @@
 #include "runtime.h"
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -68,6 +69,13 @@ cudaError_t device_malloc(void** p, size_t bytes) {
     const cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) *p = nullptr;
     return e;
+}
+TraceSched sched_of(const gbpt_tuning& t) {
+    TraceSched s;
+    if (t.trace_refill_lanes > 0) s.refill_lanes = (uint32_t)t.trace_refill_lanes;
+    if (t.trace_postpone_lanes > 0) s.postpone_lanes = (uint32_t)t.trace_postpone_lanes;
+    if (t.trace_blocks_per_sm > 0) s.blocks_per_sm = (uint32_t)t.trace_blocks_per_sm;
+    return s;
 }
 } // namespace gbpt
 
@@ -218,8 +226,8 @@ GBPT_API int gbpt_create(int device, uint64_t stream, gbpt_ctx** out_ctx) {
         GBPT_CUDA_CHECK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
         ctx->own_stream = true;
     }
-    GBPT_CUDA_CHECK(device_malloc((void**)&ctx->d_misc, 4 * sizeof(unsigned long long)));
-    GBPT_CUDA_CHECK(cudaMemset(ctx->d_misc, 0, 4 * sizeof(unsigned long long)));
+    GBPT_CUDA_CHECK(device_malloc((void**)&ctx->d_misc, 8 * sizeof(unsigned long long)));
+    GBPT_CUDA_CHECK(cudaMemset(ctx->d_misc, 0, 8 * sizeof(unsigned long long)));
     GBPT_CUDA_CHECK(cudaEventCreate(&ctx->ev0));
     GBPT_CUDA_CHECK(cudaEventCreate(&ctx->ev1));
     const int rc = work_reserve(ctx->work, 0, 0);
@@ -851,6 +859,8 @@ static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
     if (stats) {
         GBPT_CUDA_CHECK(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
         GBPT_CUDA_CHECK(cudaMemsetAsync(ctx->d_misc, 0, 2 * sizeof(unsigned long long), ctx->stream));
+        GBPT_CUDA_CHECK(cudaMemsetAsync(ctx->d_misc + 4, 0, 4 * sizeof(unsigned long long),
+                                        ctx->stream));
         GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev0, ctx->stream));
         if (prof) prof->reset();
     }
@@ -863,9 +873,11 @@ static int render_impl(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam,
     if (two && stats)
         GBPT_CUDA_CHECK(cudaMemsetAsync(ctx->work2.stats, 0, 4 * sizeof(unsigned long long),
                                         ctx->stream));
+    const TraceSched sched = sched_of(ctx->tuning);
     rc = two ? render_frame(it->second, w, a, ctx->stream, &launches, prof, ctx->d_misc, wave,
-                            &ctx->work2, ctx->stream2, ctx->ev_fork, ctx->ev_join)
-             : render_frame(it->second, w, a, ctx->stream, &launches, prof, ctx->d_misc, wave);
+                            &ctx->work2, ctx->stream2, ctx->ev_fork, ctx->ev_join, sched)
+             : render_frame(it->second, w, a, ctx->stream, &launches, prof, ctx->d_misc, wave,
+                            nullptr, nullptr, nullptr, nullptr, sched);
     if (rc != GBPT_OK) {
         set_error(rc == GBPT_ERR_NO_MEMORY ? "render: work buffer allocation failed"
                                            : "render: kernel launch failed: " +
@@ -891,7 +903,7 @@ static int read_stats(gbpt_ctx* ctx, uint64_t samples, uint64_t launches, Profil
                       gbpt_render_stats* stats, bool two) {
     Work& w = ctx->work;
     {
-        unsigned long long st[3] = {0, 0, 0}, wk[2] = {0, 0};
+        unsigned long long st[3] = {0, 0, 0}, wk[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         GBPT_CUDA_CHECK(cudaMemcpy(st, w.stats, sizeof(st), cudaMemcpyDeviceToHost));
         if (two) {
             unsigned long long st2[3] = {0, 0, 0};
@@ -923,6 +935,10 @@ static int read_stats(gbpt_ctx* ctx, uint64_t samples, uint64_t launches, Profil
             if (prof->level >= 2) {
                 stats->nodes_visited = wk[0];
                 stats->tris_tested = wk[1];
+                stats->node_steps = wk[4];
+                stats->node_lanes = wk[5];
+                stats->tri_steps = wk[6];
+                stats->tri_lanes = wk[7];
             }
         }
     }
@@ -1064,6 +1080,8 @@ GBPT_API int gbpt_render_batch(gbpt_ctx* ctx, const gbpt_request* reqs, uint32_t
     if (stats) {
         GBPT_CUDA_CHECK(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), ctx->stream));
         GBPT_CUDA_CHECK(cudaMemsetAsync(ctx->d_misc, 0, 2 * sizeof(unsigned long long), ctx->stream));
+        GBPT_CUDA_CHECK(cudaMemsetAsync(ctx->d_misc + 4, 0, 4 * sizeof(unsigned long long),
+                                        ctx->stream));
         GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev0, ctx->stream));
         if (prof) prof->reset();
     }
@@ -1116,9 +1134,13 @@ GBPT_API int gbpt_set_graphs(gbpt_ctx* ctx, int enable) {
 static int check_tuning(const gbpt_tuning* t) {
     if (!t || t->wave_paths > (1ull << 24) || (t->wave_paths && t->wave_paths < 1024) ||
         t->sort_materials < -1 || t->sort_materials > 1 || t->bvh_build < GBPT_BVH_SPLIT ||
-        t->bvh_build > GBPT_BVH_MEDIUM || t->streams < 0 || t->streams > 2) {
+        t->bvh_build > GBPT_BVH_MEDIUM || t->streams < 0 || t->streams > 2 ||
+        t->trace_refill_lanes < 0 || t->trace_refill_lanes > 32 || t->trace_postpone_lanes < 0 ||
+        t->trace_postpone_lanes > 32 || t->trace_blocks_per_sm < 0 ||
+        t->trace_blocks_per_sm > 64) {
         set_error("tuning: wave_paths must be 0 or in [1024, 2^24], sort_materials in {-1, 0, 1}, "
-                  "bvh_build a GBPT_BVH_* value, streams in {0, 1, 2}");
+                  "bvh_build a GBPT_BVH_* value, streams in {0, 1, 2}, trace_refill_lanes and "
+                  "trace_postpone_lanes in [0, 32], trace_blocks_per_sm in [0, 64]");
         return GBPT_ERR_INVALID;
     }
     return GBPT_OK;
@@ -1133,6 +1155,7 @@ GBPT_API int gbpt_set_tuning(gbpt_ctx* ctx, const gbpt_tuning* t) {
     ctx->tuning = *t;
     ctx->batch.wave = t->wave_paths ? t->wave_paths : kWavePaths;
     ctx->batch.use_graphs = t->use_graphs != 0;
+    ctx->batch.sched = sched_of(*t);
     ctx->batch.release();
     ctx->batch2.release();
     return GBPT_OK;
@@ -1150,9 +1173,12 @@ GBPT_API int gbpt_get_tuning(gbpt_ctx* ctx, gbpt_tuning* t) {
     return GBPT_OK;
 }
 
-// The autotuner: the candidate tunings rendered on one representative request and the fastest
-// kept. Outputs do not depend on the tuning (tick size and shading order only change the
-// schedule), so only time is compared.
+// The autotuner: candidate tunings rendered on one representative request, the fastest kept.
+// Outputs do not depend on the tuning (tick size, shading order and warp scheduling only change
+// the schedule), so only time is compared. Stage 1 crosses tick size and material sorting; the
+// traversal's refill and postponement thresholds and its blocks per SM are then searched one at a
+// time from the best so far. Results are cached per bucket of scene size, frame size, path length
+// and estimator.
 GBPT_API int gbpt_autotune(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
                            const gbpt_render_params* p, gbpt_tuning* out, double* ms_out) {
     int rc = check_ctx(ctx);
@@ -1168,8 +1194,40 @@ GBPT_API int gbpt_autotune(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam
         set_error("gbpt_autotune: unknown scene id");
         return GBPT_ERR_NOT_FOUND;
     }
-    Work& w = ctx->work;
+    if (ms_out)
+        for (int i = 0; i < GBPT_AUTOTUNE_CANDIDATES; ++i) ms_out[i] = std::nan("");
     const uint32_t n_pix = p->width * p->height;
+    auto log2_bucket = [](uint64_t x) {
+        int b = 0;
+        while (x > 1) {
+            x >>= 1;
+            ++b;
+        }
+        return b;
+    };
+    const std::array<int, 5> key{log2_bucket(std::max<uint64_t>(it->second.n_tris, 1)),
+                                 log2_bucket(std::max<uint64_t>((uint64_t)n_pix * p->spp, 1)),
+                                 p->max_path_length, p->nee ? 1 : 0, p->rr_depth};
+    auto apply = [&](const gbpt_tuning& t) {
+        ctx->tuning = t;
+        ctx->batch.wave = t.wave_paths;
+        ctx->batch.sched = sched_of(t);
+        ctx->batch.release();
+        ctx->batch2.release();
+        if (out) *out = t;
+    };
+    const auto cached = ctx->tune_cache.find(key);
+    if (cached != ctx->tune_cache.end()) {
+        gbpt_tuning t = cached->second.tuning;
+        t.use_graphs = ctx->tuning.use_graphs;
+        t.bvh_build = ctx->tuning.bvh_build;
+        t.streams = ctx->tuning.streams;
+        if (ms_out)
+            for (int i = 0; i < GBPT_AUTOTUNE_CANDIDATES; ++i) ms_out[i] = cached->second.ms[i];
+        apply(t);
+        return GBPT_OK;
+    }
+    Work& w = ctx->work;
     if (n_pix > w.out_cap) {
         if (w.out) cudaFree(w.out);
         w.out = nullptr;
@@ -1177,49 +1235,90 @@ GBPT_API int gbpt_autotune(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* cam
         GBPT_CUDA_CHECK(device_malloc((void**)&w.out, (size_t)n_pix * sizeof(float4)));
         w.out_cap = n_pix;
     }
-    const uint64_t waves[4] = {1ull << 21, 1ull << 22, 1ull << 23, 1ull << 24};
-    gbpt_tuning best{};
-    double best_ms = 1e300;
-    int idx = 0;
-    for (uint64_t wave : waves) {
-        if (wave < (uint64_t)p->spp) continue;
-        for (int sort = 0; sort < 2; ++sort, ++idx) {
-            RenderArgs a;
-            a.camera = *camera;
-            a.params = *p;
-            a.params.sort_materials = sort;
-            a.pixel_count = n_pix;
-            a.pixels_device = nullptr;
-            a.out_device = w.out;
-            float ms = 0.f;
-            for (int rep = 0; rep < 2; ++rep) { // the first run allocates and warms the caches
-                GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev0, ctx->stream));
-                rc = render_frame(it->second, w, a, ctx->stream, nullptr, nullptr, nullptr, wave);
-                if (rc != GBPT_OK) {
-                    set_error("gbpt_autotune: render failed");
-                    return rc;
-                }
-                GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev1, ctx->stream));
-                GBPT_CUDA_CHECK(cudaEventSynchronize(ctx->ev1));
-                GBPT_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    std::array<double, GBPT_AUTOTUNE_CANDIDATES> ms_all;
+    ms_all.fill(std::nan(""));
+    // one candidate: a warm-up render (it also allocates), then the timed one
+    auto time_one = [&](const gbpt_tuning& t, int idx, double* ms_res) -> int {
+        RenderArgs a;
+        a.camera = *camera;
+        a.params = *p;
+        a.params.sort_materials = t.sort_materials;
+        a.pixel_count = n_pix;
+        a.pixels_device = nullptr;
+        a.out_device = w.out;
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; ++rep) {
+            GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev0, ctx->stream));
+            const int r = render_frame(it->second, w, a, ctx->stream, nullptr, nullptr, nullptr,
+                                       t.wave_paths, nullptr, nullptr, nullptr, nullptr,
+                                       sched_of(t));
+            if (r != GBPT_OK) {
+                set_error("gbpt_autotune: render failed");
+                return r;
             }
-            if (ms_out && idx < 8) ms_out[idx] = ms;
-            if (ms < best_ms) {
-                best_ms = ms;
-                best.wave_paths = wave;
-                best.sort_materials = sort;
-            }
+            GBPT_CUDA_CHECK(cudaEventRecord(ctx->ev1, ctx->stream));
+            GBPT_CUDA_CHECK(cudaEventSynchronize(ctx->ev1));
+            GBPT_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
         }
+        ms_all[idx] = ms;
+        *ms_res = ms;
+        return GBPT_OK;
+    };
+    gbpt_tuning best = ctx->tuning;
+    {
+        const TraceSched defaults;
+        best.trace_refill_lanes = (int32_t)defaults.refill_lanes;
+        best.trace_postpone_lanes = (int32_t)defaults.postpone_lanes;
+        best.trace_blocks_per_sm = 0; // every resident block
+    }
+    double best_ms = 1e300;
+    auto consider = [&](const gbpt_tuning& t, int idx) -> int {
+        double ms = 0.0;
+        const int r = time_one(t, idx, &ms);
+        if (r == GBPT_OK && ms < best_ms) {
+            best_ms = ms;
+            best = t;
+        }
+        return r;
+    };
+    const uint64_t waves[4] = {1ull << 21, 1ull << 22, 1ull << 23, 1ull << 24};
+    for (int wi = 0; wi < 4; ++wi) {
+        if (waves[wi] < (uint64_t)p->spp) continue;
+        for (int sort = 0; sort < 2; ++sort) {
+            gbpt_tuning t = best;
+            t.wave_paths = waves[wi];
+            t.sort_materials = sort;
+            if ((rc = consider(t, 2 * wi + sort))) return rc;
+        }
+    }
+    const int refill[5] = {12, 16, 20, 24, 28}, postpone[5] = {2, 4, 6, 8, 12};
+    const int blocks[3] = {6, 7, 0};
+    const gbpt_tuning stage1 = best;
+    for (int k = 0; k < 5; ++k) {
+        gbpt_tuning t = stage1;
+        t.trace_refill_lanes = refill[k];
+        if ((rc = consider(t, 8 + k))) return rc;
+    }
+    const gbpt_tuning stage2 = best;
+    for (int k = 0; k < 5; ++k) {
+        gbpt_tuning t = stage2;
+        t.trace_postpone_lanes = postpone[k];
+        if ((rc = consider(t, 13 + k))) return rc;
+    }
+    const gbpt_tuning stage3 = best;
+    for (int k = 0; k < 3; ++k) {
+        gbpt_tuning t = stage3;
+        t.trace_blocks_per_sm = blocks[k];
+        if ((rc = consider(t, 18 + k))) return rc;
     }
     if ((rc = check_device_error(ctx))) return rc;
     best.use_graphs = ctx->tuning.use_graphs;
     best.bvh_build = ctx->tuning.bvh_build;
     best.streams = ctx->tuning.streams;
-    ctx->tuning = best;
-    ctx->batch.wave = best.wave_paths;
-    ctx->batch.release();
-    ctx->batch2.release();
-    if (out) *out = best;
+    ctx->tune_cache[key] = gbpt_ctx::TuneResult{best, ms_all};
+    if (ms_out)
+        for (int i = 0; i < GBPT_AUTOTUNE_CANDIDATES; ++i) ms_out[i] = ms_all[i];
+    apply(best);
     return GBPT_OK;
 }
 

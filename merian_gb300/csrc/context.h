@@ -5,6 +5,7 @@
 #include "gbpt.h"
 #include "runtime.h"
 
+#include <array>
 #include <cstdint>
 #include <map>
 #include <memory>
@@ -42,8 +43,14 @@ struct gbpt_ctx {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // schedule of gbpt_render* and gbpt_render_batch: paths per tick (0 = default), material sort
     // override (-1 = as each request asks), CUDA graphs
-    gbpt_tuning tuning{0, -1, 0, GBPT_BVH_SPLIT, 0};
-    unsigned long long* d_misc = nullptr; // [0] nodes, [1] tris, [2] error word
+    gbpt_tuning tuning{0, -1, 0, GBPT_BVH_SPLIT, 0, 0, 0, 0};
+    // gbpt_autotune's results by (log2 triangles, log2 paths, path length, NEE, roulette depth)
+    struct TuneResult {
+        gbpt_tuning tuning;
+        std::array<double, GBPT_AUTOTUNE_CANDIDATES> ms;
+    };
+    std::map<std::array<int, 5>, TuneResult> tune_cache;
+    unsigned long long* d_misc = nullptr; // [0] nodes, [1] tris, [2] error word, [4..7] SIMT steps
     gbpt_hit* d_hits = nullptr;
     uint64_t hits_cap = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -62,6 +69,8 @@ namespace gbpt {
         }                                                                                          \
     } while (0)
 
+// The traversal schedule a tuning asks for (0 fields: the defaults).
+TraceSched sched_of(const gbpt_tuning& t);
 // Null check and cudaSetDevice for the context's device.
 int check_ctx(gbpt_ctx* ctx);
 // Camera / parameter validation shared by every render entry point.

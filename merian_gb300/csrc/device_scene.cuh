@@ -206,9 +206,19 @@ constexpr int kStackSize = GBPT_STACK_SIZE;
 static_assert(kStackSize >= 1, "the traversal needs a stack entry");
 constexpr uint32_t kNoInst = 0xFFFFFFFFu;
 
+// Work of the instrumented traversal (COUNT): nodes visited and triangles tested per lane, and
+// on the first active lane of each warp-wide step the step and its active lanes.
 struct TraceCounters {
     uint32_t nodes, tris;
+    uint32_t node_steps, node_lanes, tri_steps, tri_lanes;
 };
+GBPT_DI void count_step(uint32_t& steps, uint32_t& lanes) {
+    const uint32_t m = __activemask();
+    if ((threadIdx.x & 31u) == (uint32_t)(__ffs(m) - 1)) {
+        steps++;
+        lanes += __popc(m);
+    }
+}
 
 GBPT_DI float safe_rcp(float d) {
     const float m = 1e-20f;
@@ -234,9 +244,9 @@ GBPT_DI float3 xform_vector(float4 r0, float4 r1, float4 r2, float3 v) {
 // ---- traversal state and loop ------------------------------------------------------------------
 // One loop serves the per-thread queries (trace_ray) and the persistent warps (trace_persistent).
 // In the persistent form a lane postpones its pending triangle tests (pushes the triangle group
-// onto its stack) when fewer than kPostponeLanes lanes of the warp have triangles to test, so node
-// steps and triangle steps stay in lockstep across the warp, and the warp leaves the loop to refill
-// idle lanes once fewer than kRefillLanes lanes are busy. Two-level scenes: a top-level leaf is an
+// onto its stack) when fewer than `postpone_lanes` lanes of the warp have triangles to test, so
+// node steps and triangle steps stay in lockstep across the warp, and the warp leaves the loop to
+// refill idle lanes once fewer than `refill_lanes` lanes are busy (both launch arguments). Two-level scenes: a top-level leaf is an
 // instance; entering it pushes what is left of the top level, transforms the ray to object space
 // (t is unchanged: the direction is not renormalised) and continues from the BLAS root; when the
 // stack drops back to the entry depth the world ray is restored. The closest hit and the tie rule
@@ -244,14 +254,6 @@ GBPT_DI float3 xform_vector(float4 r0, float4 r1, float4 r2, float3 v) {
 #ifndef GBPT_SMEM_STACK
 #define GBPT_SMEM_STACK 0
 #endif
-#ifndef GBPT_REFILL_LANES
-#define GBPT_REFILL_LANES 20
-#endif
-#ifndef GBPT_POSTPONE_LANES
-#define GBPT_POSTPONE_LANES 6
-#endif
-constexpr int kRefillLanes = GBPT_REFILL_LANES;
-constexpr int kPostponeLanes = GBPT_POSTPONE_LANES;
 
 
 struct TraceState {
@@ -318,24 +320,31 @@ GBPT_DI void exit_instance(TraceState& s) {
     s.inst_sp = -1;
 }
 
-// Byte j of w as a float. With GBPT_BOX_PRMT the byte is placed in the mantissa of 2^23 with
-// one byte permute and 2^23 subtracted (exact), instead of a shift, a mask and an int-to-float
-// conversion.
-#ifndef GBPT_BOX_PRMT
-#define GBPT_BOX_PRMT 0
+// Child box planes. Byte j of a plane word w is the quantised plane q of child j; the slab
+// distance is t = q * a + o, a = 2^e / d and o = (p - origin) / d per node and axis.
+// GBPT_BOX_BIAS (the default): one byte permute writes q into bits 8..15 of the float 32768.0,
+// which makes the float 32768 + q exactly, and the per-node offsets absorb the bias
+// (o' = o - 32768 a), so a plane costs a permute and an FMA. The rounding of o' is at most
+// 2^-9 |a| (a 512th of a quantisation step); the slack below covers it. Without it: shift, mask
+// and integer-to-float conversion, then the FMA.
+#ifndef GBPT_BOX_BIAS
+#define GBPT_BOX_BIAS 1
 #endif
-GBPT_DI float qbyte(uint32_t w, int j) {
-#if GBPT_BOX_PRMT
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (uint32_t)j)) - 8388608.0f;
-#else
-    return (float)((w >> (8 * j)) & 0xFFu);
-#endif
+#if GBPT_BOX_BIAS
+constexpr float kPlaneBias = 32768.0f;
+GBPT_DI float qplane(uint32_t w, int j) {
+    return __uint_as_float(__byte_perm(w, 0x47000000u, 0x7504u | ((uint32_t)j << 4)));
 }
+#else
+constexpr float kPlaneBias = 0.0f;
+GBPT_DI float qplane(uint32_t w, int j) { return (float)((w >> (8 * j)) & 0xFFu); }
+#endif
 
 // Intersects the 8 children of node `ni`; returns the hit mask (inner children in bits 24..31 in
 // traversal order, triangles in bits 0..23) and the node's child / triangle bases and imask.
 // The quantised planes are dequantised with a per-axis slack of 2^-20 of the plane distance
-// magnitude, so rounding never loses a child the exact box would keep.
+// magnitude (plus 2^-8 of a quantisation step for the biased planes), so rounding never loses a
+// child the exact box would keep.
 template <bool COUNT>
 GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& child_base,
                                 uint32_t& tri_base, uint32_t& imask, TraceCounters* ctr) {
@@ -346,18 +355,19 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
     const uint4 n3 = __ldg(&s.nodes[5 * ni + 3]);
     const uint4 n4 = __ldg(&s.nodes[5 * ni + 4]);
     const float kErr = 1.0f / 1048576.0f;
+    const float kBiasErr = GBPT_BOX_BIAS ? 1.0f / 256.0f : 0.0f;
     const float aix = __uint_as_float((n0.w & 0xFFu) << 23) * s.inv.x;
     const float aiy = __uint_as_float(((n0.w >> 8) & 0xFFu) << 23) * s.inv.y;
     const float aiz = __uint_as_float(((n0.w >> 16) & 0xFFu) << 23) * s.inv.z;
     const float aox = (__uint_as_float(n0.x) - s.o.x) * s.inv.x;
     const float aoy = (__uint_as_float(n0.y) - s.o.y) * s.inv.y;
     const float aoz = (__uint_as_float(n0.z) - s.o.z) * s.inv.z;
-    const float ex = (fabsf(aox) + 255.0f * fabsf(aix)) * kErr;
-    const float ey = (fabsf(aoy) + 255.0f * fabsf(aiy)) * kErr;
-    const float ez = (fabsf(aoz) + 255.0f * fabsf(aiz)) * kErr;
-    const float nox = aox - ex, fox = aox + ex;
-    const float noy = aoy - ey, foy = aoy + ey;
-    const float noz = aoz - ez, foz = aoz + ez;
+    const float ex = (fabsf(aox) + 255.0f * fabsf(aix)) * kErr + kBiasErr * fabsf(aix);
+    const float ey = (fabsf(aoy) + 255.0f * fabsf(aiy)) * kErr + kBiasErr * fabsf(aiy);
+    const float ez = (fabsf(aoz) + 255.0f * fabsf(aiz)) * kErr + kBiasErr * fabsf(aiz);
+    const float nox = fmaf(-kPlaneBias, aix, aox - ex), fox = fmaf(-kPlaneBias, aix, aox + ex);
+    const float noy = fmaf(-kPlaneBias, aiy, aoy - ey), foy = fmaf(-kPlaneBias, aiy, aoy + ey);
+    const float noz = fmaf(-kPlaneBias, aiz, aoz - ez), foz = fmaf(-kPlaneBias, aiz, aoz + ez);
     imask = n0.w >> 24;
     child_base = n1.x;
     tri_base = n1.y;
@@ -378,12 +388,12 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const uint32_t sh = 8u * j;
-            const float tnx = fmaf(qbyte(nqx, j), aix, nox);
-            const float tny = fmaf(qbyte(nqy, j), aiy, noy);
-            const float tnz = fmaf(qbyte(nqz, j), aiz, noz);
-            const float tfx = fmaf(qbyte(fqx, j), aix, fox);
-            const float tfy = fmaf(qbyte(fqy, j), aiy, foy);
-            const float tfz = fmaf(qbyte(fqz, j), aiz, foz);
+            const float tnx = fmaf(qplane(nqx, j), aix, nox);
+            const float tny = fmaf(qplane(nqy, j), aiy, noy);
+            const float tnz = fmaf(qplane(nqz, j), aiz, noz);
+            const float tfx = fmaf(qplane(fqx, j), aix, fox);
+            const float tfy = fmaf(qplane(fqy, j), aiy, foy);
+            const float tfz = fmaf(qplane(fqz, j), aiz, foz);
             const float cmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, s.tmin));
             const float cmax = fminf(fminf(tfx, tfy), fminf(tfz, s.best.t));
             if (cmin <= cmax) hitmask |= ((child_bits4 >> sh) & 7u) << ((bit_index4 >> sh) & 31u);
@@ -399,7 +409,8 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
 // `alpha(geom, prim, u, v)` decides the candidate hits of non-opaque triangles (true: skip).
 template <bool ANY, bool COUNT, bool TWO_LEVEL, bool WARP, class StackRef, class Alpha>
 GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32_t* err,
-                        bool pool_empty, const Alpha& alpha) {
+                        bool pool_empty, const Alpha& alpha, int refill_lanes = 0,
+                        int postpone_lanes = 0) {
     while (true) {
         if (s.ngroup.y > 0x00FFFFFFu) {
             const uint32_t hits = s.ngroup.y;
@@ -419,6 +430,7 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
             const uint32_t slot = (bit - 24u) ^ s.oct_inv;
             const uint32_t ni = s.ngroup.x + __popc((hits & 0xFFu) & ((1u << slot) - 1u));
             uint32_t cb, tb, im;
+            if (COUNT) count_step(ctr->node_steps, ctr->node_lanes);
             const uint32_t hm = intersect_node<COUNT>(s, ni, cb, tb, im, ctr);
             s.ngroup = make_uint2(cb, (hm & 0xFF000000u) | im);
             s.tgroup = make_uint2(tb, hm & 0x00FFFFFFu);
@@ -432,7 +444,7 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
         // only groups followed by node work are postponed (a group popped back is tested)
         const bool may_postpone = WARP && s.ngroup.y > 0x00FFFFFFu;
         while (s.tgroup.y != 0u) {
-            if (may_postpone && s.sp < kStackSize && __popc(__activemask()) < kPostponeLanes) {
+            if (may_postpone && s.sp < kStackSize && __popc(__activemask()) < postpone_lanes) {
                 st(s.sp++) = s.tgroup;
                 s.tgroup.y = 0u;
                 break;
@@ -460,7 +472,10 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
             const float4 r2 = __ldg(&s.tris[3 * ti + 2]);
             const uint32_t tfl = __float_as_uint(r2.w);
             if (((tfl & 0xFFu) & s.mask) == 0u) continue;
-            if (COUNT) ctr->tris++;
+            if (COUNT) {
+                ctr->tris++;
+                count_step(ctr->tri_steps, ctr->tri_lanes);
+            }
             float t, u, v;
             if (!intersect_tri(s.pre, r0, r1, r2, tfl, s.tmin, s.best.t, t, u, v)) continue;
             const uint32_t prim = __float_as_uint(r0.w), geom = __float_as_uint(r1.w);
@@ -488,7 +503,7 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
             else s.ngroup = st(--s.sp);
         }
         if (done) break;
-        if (WARP && !pool_empty && __popc(__activemask()) < kRefillLanes) return false;
+        if (WARP && !pool_empty && __popc(__activemask()) < refill_lanes) return false;
     }
     if (!s.found) s.best.geom = s.best.prim = s.best.inst = kNoInst;
     return true;
@@ -522,7 +537,8 @@ __device__ __forceinline__ Hit trace_ray(const DevScene& sc, float3 o, float3 d,
 template <bool ANY, bool COUNT, bool TWO_LEVEL, class Load, class Store, class Alpha>
 __device__ __forceinline__ void trace_persistent(uint32_t n, uint32_t* fetch, Load load,
                                                  Store store, Alpha alpha, TraceCounters* ctr,
-                                                 uint32_t* err) {
+                                                 uint32_t* err, int refill_lanes,
+                                                 int postpone_lanes) {
     const uint32_t lane = threadIdx.x & 31u;
 #if GBPT_SMEM_STACK > 0
     // the first GBPT_SMEM_STACK entries of every thread's stack in shared memory (thread-strided:
@@ -566,7 +582,8 @@ __device__ __forceinline__ void trace_persistent(uint32_t n, uint32_t* fetch, Lo
         const auto ray_alpha = [&](uint32_t g, uint32_t p, float u, float v) {
             return alpha(ray, g, p, u, v);
         };
-        if (trace_loop<ANY, COUNT, TWO_LEVEL, true>(s, st_ref, ctr, err, pool_empty, ray_alpha)) {
+        if (trace_loop<ANY, COUNT, TWO_LEVEL, true>(s, st_ref, ctr, err, pool_empty, ray_alpha,
+                                                    refill_lanes, postpone_lanes)) {
             store(ray, s.best);
             active = false;
         }

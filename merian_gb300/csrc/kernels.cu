@@ -37,7 +37,7 @@ template <bool ANY>
 __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
     k_trace_rays(DevScene sc, const gbpt_ray* rays, uint32_t n, uint32_t mask, gbpt_hit* hits,
                  unsigned long long* work_ctr, uint32_t* fetch, uint32_t* err) {
-    TraceCounters ctr{0, 0};
+    TraceCounters ctr{0, 0, 0, 0, 0, 0};
     auto load = [&](uint32_t i, TraceState& s) {
         const gbpt_ray r = rays[i];
         s.nodes = sc.nodes;
@@ -51,7 +51,9 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
     auto alpha = [&](uint32_t, uint32_t g, uint32_t p, float u, float v) {
         return alpha_discard(sc, g, p, u, v);
     };
-    trace_persistent<ANY, true, true>(n, fetch, load, store, alpha, &ctr, err);
+    const TraceSched sched;
+    trace_persistent<ANY, true, true>(n, fetch, load, store, alpha, &ctr, err,
+                                      (int)sched.refill_lanes, (int)sched.postpone_lanes);
     if (work_ctr) {
         atomicAdd(work_ctr + 0, (unsigned long long)ctr.nodes);
         atomicAdd(work_ctr + 1, (unsigned long long)ctr.tris);

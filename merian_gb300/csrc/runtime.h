@@ -146,12 +146,25 @@ struct TickItem : BatchItem {
     uint32_t cursor = 0;
 };
 
+// Warp scheduling of the persistent traversal kernels, chosen at launch (gbpt_tuning, searched
+// by the autotuner; results never depend on it): a warp leaves its traversal loop to refill its
+// idle lanes with new rays once fewer than refill_lanes lanes are busy; a lane pushes its
+// triangle group for later when fewer than postpone_lanes lanes of the warp have triangles to
+// test; the closest-hit and any-hit launches run blocks_per_sm blocks of 128 threads per SM
+// (0: every block that is resident at once).
+struct TraceSched {
+    uint32_t refill_lanes = 20;
+    uint32_t postpone_lanes = 6;
+    uint32_t blocks_per_sm = 0;
+};
+
 // Plans ticks over requests, uploads each tick's tables and enqueues its kernels on one stream
 // (wavefront.cu). A tick is at most `wave` paths of whole pixels from up to 256 requests.
 struct TickEngine {
     Work* work = nullptr;
     cudaStream_t stream = nullptr;
     uint64_t wave = kWavePaths;
+    TraceSched sched;
     // replay each tick shape (path length, NEE) from a captured CUDA graph; needs a stream that
     // can be captured, and keeps a whole wave of work buffers
     bool use_graphs = false;
@@ -189,7 +202,8 @@ int render_batch(TickEngine& e, const BatchItem* items, uint32_t n_items, uint64
 int render_frame(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
                  uint64_t* launches, Profile* prof, unsigned long long* work_ctr,
                  uint64_t wave = 0, Work* work2 = nullptr, cudaStream_t stream2 = nullptr,
-                 cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
+                 cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr,
+                 const TraceSched& sched = TraceSched{});
 int primary_points(const SceneGPU& scene, Work& work, const RenderArgs& args, cudaStream_t stream,
                    float* out_device);
 // Bytes of tick tables for ticks of at most max_chunks requests.

@@ -422,6 +422,7 @@ GBPT_API int gbpt_server_start(gbpt_ctx* ctx, const gbpt_server_config* cfg) {
                          ? s->cfg.wave_paths
                          : (ctx->tuning.wave_paths ? ctx->tuning.wave_paths : kWavePaths);
     s->sort_override = ctx->tuning.sort_materials;
+    s->engine.sched = sched_of(ctx->tuning);
     s->engine.use_graphs = s->cfg.use_graphs != 0;
     if ((rc = work_reserve(s->work, s->engine.wave, s->engine.wave)) != GBPT_OK) {
         set_error("gbpt_server_start: work buffer allocation failed");

@@ -85,6 +85,7 @@ struct TickArgs {
     const ChunkGPU* chunks;
     const TickHeader* hdr;
     Work w;
+    int refill_lanes, postpone_lanes; // warp scheduling of the persistent traversal
 };
 
 // last chunk whose base <= key
@@ -300,7 +301,7 @@ template <bool COUNT, bool TWO_LEVEL, bool ALPHA>
 __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
     k_trace(TickArgs t, int qi, unsigned long long* work_ctr, int sort) {
     const uint32_t n = t.w.counters[qi];
-    TraceCounters ctr{0, 0};
+    TraceCounters ctr{0, 0, 0, 0, 0, 0};
     // with material-sorted shading: each hit's sort key, counted per block in shared memory
     __shared__ uint32_t key_count[kSortKeys];
     if (threadIdx.x < kSortKeys) key_count[threadIdx.x] = 0u;
@@ -334,7 +335,8 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
                alpha_discard(t.scenes[t.chunks[__ldg(&qp[i]) >> kPathBits].scene], g, p, u, v);
     };
     trace_persistent<false, COUNT, TWO_LEVEL>(n, t.w.counters + 4, load, store, alpha, &ctr,
-                                              t.w.counters + 3);
+                                              t.w.counters + 3, t.refill_lanes,
+                                              t.postpone_lanes);
     if (sort) {
         __syncthreads();
         if (threadIdx.x < kSortKeys && key_count[threadIdx.x])
@@ -343,6 +345,14 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
     if (COUNT) {
         atomicAdd(work_ctr + 0, (unsigned long long)ctr.nodes);
         atomicAdd(work_ctr + 1, (unsigned long long)ctr.tris);
+        if (ctr.node_steps) {
+            atomicAdd(work_ctr + 4, (unsigned long long)ctr.node_steps);
+            atomicAdd(work_ctr + 5, (unsigned long long)ctr.node_lanes);
+        }
+        if (ctr.tri_steps) {
+            atomicAdd(work_ctr + 6, (unsigned long long)ctr.tri_steps);
+            atomicAdd(work_ctr + 7, (unsigned long long)ctr.tri_lanes);
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         atomicAdd(t.w.stats + 0, (unsigned long long)n);
@@ -517,7 +527,7 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM) k_shadow(TickArgs t) {
                                       g, p, u, v);
     };
     trace_persistent<true, false, TWO_LEVEL>(n, t.w.counters + 5, load, store, alpha, nullptr,
-                                             t.w.counters + 3);
+                                             t.w.counters + 3, t.refill_lanes, t.postpone_lanes);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         atomicAdd(t.w.stats + 0, (unsigned long long)n);
         atomicAdd(t.w.stats + 1, (unsigned long long)n);
@@ -1010,6 +1020,8 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
     ta.scenes = (const DevScene*)(tb + lay.scenes);
     ta.chunks = (const ChunkGPU*)(tb + lay.chunks);
     ta.w = w;
+    ta.refill_lanes = (int)e.sched.refill_lanes;
+    ta.postpone_lanes = (int)e.sched.postpone_lanes;
     if (e.grids[0] == 0) {
         const Grids g = launch_grids();
         static_assert(sizeof(Grids) == sizeof(e.grids), "grid cache");
@@ -1017,6 +1029,12 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
     }
     Grids grids;
     std::memcpy(&grids, e.grids, sizeof(grids));
+    if (e.sched.blocks_per_sm > 0) {
+        const int cap = (int)e.sched.blocks_per_sm * num_sms();
+        grids.trace = std::min(grids.trace, cap);
+        grids.trace_c = std::min(grids.trace_c, cap);
+        grids.shadow = std::min(grids.shadow, cap);
+    }
     uint64_t nl = 0;
     if (graph) {
         if (e.graph_generation != w.generation) {
@@ -1078,6 +1096,7 @@ int render_batch(TickEngine& e, const BatchItem* items, uint32_t n_items, uint64
     // two streams: ticks cover disjoint pixels, each over its own work buffers, so they only
     // share the scenes (read), the outputs (disjoint texels) and atomic counters
     e2->wave = e.wave;
+    e2->sched = e.sched;
     if (cudaEventRecord(fork, e.stream) != cudaSuccess ||
         cudaStreamWaitEvent(e2->stream, fork, 0) != cudaSuccess)
         return GBPT_ERR_CUDA;
@@ -1095,7 +1114,8 @@ int render_batch(TickEngine& e, const BatchItem* items, uint32_t n_items, uint64
 
 int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStream_t st,
                  uint64_t* launches, Profile* prof, unsigned long long* work_ctr, uint64_t wave,
-                 Work* w2, cudaStream_t st2, cudaEvent_t fork, cudaEvent_t join) {
+                 Work* w2, cudaStream_t st2, cudaEvent_t fork, cudaEvent_t join,
+                 const TraceSched& sched) {
     BatchItem it;
     it.scene = &scene;
     it.camera = args.camera;
@@ -1106,10 +1126,12 @@ int render_frame(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaStr
     TickEngine e;
     e.work = &w;
     e.stream = st;
+    e.sched = sched;
     if (wave) e.wave = wave;
     TickEngine e2;
     e2.work = w2;
     e2.stream = st2;
+    e2.sched = sched;
     const int rc = render_batch(e, &it, 1, launches, prof, work_ctr, w2 ? &e2 : nullptr, fork,
                                 join);
     e.release();

@@ -386,8 +386,10 @@ class Context:
 
     def set_tuning(self, wave_paths: int = 0, sort_materials: int = -1,
                    use_graphs: bool = False, bvh_build: int = N.BVH_SPLIT,
-                   streams: int = 0) -> None:
-        t = N.Tuning(wave_paths, sort_materials, int(use_graphs), bvh_build, streams)
+                   streams: int = 0, refill_lanes: int = 0, postpone_lanes: int = 0,
+                   blocks_per_sm: int = 0) -> None:
+        t = N.Tuning(wave_paths, sort_materials, int(use_graphs), bvh_build, streams,
+                     refill_lanes, postpone_lanes, blocks_per_sm)
         self._check(self.lib.gbpt_set_tuning(self.handle, C.byref(t)))
 
     def get_tuning(self) -> N.Tuning:
@@ -397,9 +399,10 @@ class Context:
 
     def autotune(self, sid: int, camera: N.Camera, params: N.RenderParams):
         """Times the candidate schedules on one frame and keeps the fastest; returns the chosen
-        tuning and the candidates' times (ms, tick size major, sorting minor)."""
+        tuning and the candidates' times (ms, in gbpt_autotune's order; candidates not run are
+        left out)."""
         t = N.Tuning()
-        ms = (C.c_double * 8)(*([float("nan")] * 8))
+        ms = (C.c_double * N.AUTOTUNE_CANDIDATES)(*([float("nan")] * N.AUTOTUNE_CANDIDATES))
         self._check(self.lib.gbpt_autotune(self.handle, sid, C.byref(camera), C.byref(params),
                                        C.byref(t), ms))
         return t, [v for v in ms if v == v]

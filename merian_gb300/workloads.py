@@ -21,6 +21,9 @@ from . import scene as S
 BATCH_RESOLUTIONS = ((256, 256), (512, 512), (1024, 1024))
 SERVED_RESOLUTIONS = ((512, 512), (1024, 1024), (1920, 1080))
 SERVED_SPP = (1, 4, 16, 64)
+# small requests (previews, tiles, thumbnails): one alone leaves most of the GPU idle
+SMALL_RESOLUTIONS = ((64, 64), (128, 128), (256, 256), (512, 512))
+SMALL_SPP = (1, 2, 4)
 
 
 @dataclass
@@ -79,6 +82,34 @@ def batch_mix(seed: int = S.BASE_SEED, n: int = 256, tri_range=(1e3, 2e6)):
     for i in range(n):
         w, h = BATCH_RESOLUTIONS[rng.integers(len(BATCH_RESOLUTIONS))]
         reqs.append(RequestSpec(i, w, h, int(rng.integers(1, 65)), frame=i))
+    return scenes, reqs
+
+
+def batch_small(seed: int = S.BASE_SEED, n: int = 256, tri_range=(1e3, 2e6)):
+    """The scenes of batch_mix (same seed: the same scenes), one small request each: resolution
+    from {64^2, 128^2, 256^2, 512^2}, spp from {1, 2, 4}."""
+    scenes, _ = batch_mix(seed, n, tri_range)
+    rng = np.random.default_rng(seed ^ 0x5A11)
+    reqs = []
+    for i in range(n):
+        w, h = SMALL_RESOLUTIONS[rng.integers(len(SMALL_RESOLUTIONS))]
+        reqs.append(RequestSpec(i, w, h, int(SMALL_SPP[rng.integers(len(SMALL_SPP))]), frame=i))
+    return scenes, reqs
+
+
+def served_small(seed: int = S.BASE_SEED, n_scenes: int = 32, n_requests: int = 512,
+                 rate: float = 2000.0, tri_range=(1e4, 5e6)):
+    """The resident scenes of served_stream and n_requests Poisson arrivals at `rate` per second
+    of small requests: resolution from {64^2, 128^2, 256^2, 512^2}, spp from {1, 2, 4}."""
+    scenes, _ = served_stream(seed, n_scenes, 0, rate, tri_range)
+    rng = np.random.default_rng(seed ^ 0x5E11)
+    t = 0.0
+    reqs = []
+    for i in range(n_requests):
+        t += float(rng.exponential(1.0 / rate))
+        w, h = SMALL_RESOLUTIONS[rng.integers(len(SMALL_RESOLUTIONS))]
+        spp = int(SMALL_SPP[rng.integers(len(SMALL_SPP))])
+        reqs.append(RequestSpec(int(rng.integers(n_scenes)), w, h, spp, frame=i, arrival_s=t))
     return scenes, reqs
 
 

@@ -31,7 +31,10 @@ def test_library_exports_every_declared_symbol(native):
 
 
 def test_abi_version(native):
-    assert native.gbpt_abi_version() == 1
+    # 2: gbpt_tuning's traversal schedule fields, gbpt_render_stats' SIMT step counts
+    assert native.gbpt_abi_version() == 2
+    from merian_gb300 import _native as N
+    assert C.sizeof(N.Tuning) == 40 and C.sizeof(N.RenderStats) == 136
 
 
 @pytest.mark.skipif(HAS_GPU, reason="checks the no-device error path")

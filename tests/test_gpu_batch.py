@@ -246,19 +246,25 @@ def test_material_sorted_shading_same_result(gpu_ctx, scenes):
 
 
 def test_tuning_and_autotune_same_result(gpu_ctx, scenes):
-    """The context's tuning (tick size, forced material sort, graphs, two tick streams) and the
-    autotuner's choice change only the schedule: every output is bit-identical to the default schedule's."""
+    """The context's tuning (tick size, forced material sort, graphs, two tick streams, the
+    traversal's refill and postponement thresholds and blocks per SM) and the autotuner's choice
+    change only the schedule: every output is bit-identical to the default schedule's."""
     from merian_gb300 import scene as S
     jobs = _jobs(scenes, S)
     ref = _alone(gpu_ctx, jobs)
     corn, soup, cams = scenes
     try:
-        for wave, sort, graphs, streams in ((1 << 12, 1, False, 2), (1 << 20, 0, True, 0),
-                                           (1 << 24, -1, False, 2), (1 << 16, 0, False, 2)):
-            gpu_ctx.set_tuning(wave, sort, graphs, streams=streams)
+        for wave, sort, graphs, streams, refill, postpone, bps in (
+                (1 << 12, 1, False, 2, 0, 0, 0), (1 << 20, 0, True, 0, 32, 1, 1),
+                (1 << 24, -1, False, 2, 1, 32, 3), (1 << 16, 0, False, 2, 12, 12, 7),
+                (1 << 22, 1, True, 1, 28, 2, 64)):
+            gpu_ctx.set_tuning(wave, sort, graphs, streams=streams, refill_lanes=refill,
+                               postpone_lanes=postpone, blocks_per_sm=bps)
             t = gpu_ctx.get_tuning()
             assert (t.wave_paths, t.sort_materials, t.use_graphs, t.streams) == \
                 (wave, sort, int(graphs), streams)
+            assert (t.trace_refill_lanes, t.trace_postpone_lanes, t.trace_blocks_per_sm) == \
+                (refill, postpone, bps)
             assert all(_same(a, b) for a, b in zip(ref, _alone(gpu_ctx, jobs)))
             outs = gpu_ctx.render_batch([(s, c, p) for s, c, p, _ in jobs if p.spp <= wave])
             kept = [r for r, j in zip(ref, jobs) if j[2].spp <= wave]
@@ -267,13 +273,28 @@ def test_tuning_and_autotune_same_result(gpu_ctx, scenes):
             gpu_ctx.set_tuning(100, 0, False)  # below the smallest tick
         with pytest.raises(N.GbptError):
             gpu_ctx.set_tuning(1 << 20, 0, False, streams=3)
+        with pytest.raises(N.GbptError):
+            gpu_ctx.set_tuning(1 << 20, 0, False, refill_lanes=33)
+        with pytest.raises(N.GbptError):
+            gpu_ctx.set_tuning(1 << 20, 0, False, blocks_per_sm=-1)
         gpu_ctx.set_tuning(0, -1, False)
         p, _ = S.render_params(320, 180, 16, 8, nee=True, rr_depth=3, frame=1)
         t, ms = gpu_ctx.autotune(soup, cams[soup], p)
-        assert len(ms) == 8 and all(m > 0 for m in ms)
+        # 8 tick size x sorting candidates, 5 refill, 5 postponement, 3 blocks-per-SM candidates
+        assert len(ms) == 21 and all(m > 0 for m in ms)
         assert t.wave_paths in (1 << 21, 1 << 22, 1 << 23, 1 << 24) and t.sort_materials in (0, 1)
+        assert t.trace_refill_lanes in (12, 16, 20, 24, 28)
+        assert t.trace_postpone_lanes in (2, 4, 6, 8, 12)
+        assert t.trace_blocks_per_sm in (6, 7, 0)
         got = gpu_ctx.get_tuning()
-        assert (got.wave_paths, got.sort_materials) == (t.wave_paths, t.sort_materials)
+        assert (got.wave_paths, got.sort_materials, got.trace_refill_lanes,
+                got.trace_postpone_lanes, got.trace_blocks_per_sm) == \
+            (t.wave_paths, t.sort_materials, t.trace_refill_lanes, t.trace_postpone_lanes,
+             t.trace_blocks_per_sm)
         assert all(_same(a, b) for a, b in zip(ref, _alone(gpu_ctx, jobs)))
+        # the same bucket again: the cached result, no candidate rendered again
+        gpu_ctx.set_tuning(0, -1, False)
+        t2, ms2 = gpu_ctx.autotune(soup, cams[soup], p)
+        assert bytes(t2) == bytes(t) and ms2 == ms
     finally:
         gpu_ctx.set_tuning(0, -1, False)
