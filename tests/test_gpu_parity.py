@@ -219,6 +219,35 @@ def test_render_headline_soup_converges_to_oracle(gpu_ctx, soup_1m, nee, rr):
     _check_estimator(gpu_ctx, "soup_1m", sid, cam, nee, rr, frames=16, spp=4096)
 
 
+def test_headline_estimator_within_one_percent(gpu_ctx, soup_1m):
+    """The benchmarked estimator (NEE + roulette from path length 3) converges to the reference's
+    BSDF-only estimator: on the 64 pixels of the deep FP64 fixture (2^22 spp, its own noise a
+    third of a percent) the GPU at 2^22 spp per pixel lands within 1 % relative RMSE, and every
+    pixel within 4 combined standard errors."""
+    from merian_gb300 import scene as S
+    sc, sid, osc, cam = soup_1m
+    g = golden("soup_1m_deep")
+    n = int(g["spp"])
+    halves = []
+    for f in range(2):  # two independent halves: their spread is the GPU estimate's noise
+        p, keep = S.render_params(int(g["width"]), int(g["height"]), n // 2,
+                                  int(g["max_path_length"]), pixels=g["pixels"], nee=True,
+                                  rr_depth=3, frame=2000 + f)
+        halves.append(gpu_ctx.render(sid, cam, p)[:, :3].astype(np.float64))
+    m = 0.5 * (halves[0] + halves[1])
+    scale = float(np.mean(g["mean"]))
+    rel_rmse = np.sqrt(np.mean((m - g["mean"]) ** 2)) / scale
+    se_o = np.sqrt(g["var"] / n)
+    # the GPU estimate's standard error: the spread of its two halves, at least the oracle's
+    se_g = np.maximum(se_o, 0.5 * np.abs(halves[0] - halves[1]))
+    se = np.sqrt(se_o ** 2 + se_g ** 2 + (1e-5 * np.abs(g["mean"])) ** 2)
+    z = (m - g["mean"]) / np.maximum(se, 1e-12)
+    print(f"soup_1m deep: rel RMSE {rel_rmse:.4%}, oracle noise "
+          f"{np.sqrt(np.mean(se_o ** 2)) / scale:.4%}, max|z| {np.abs(z).max():.2f}")
+    assert rel_rmse < 0.01
+    assert np.abs(z).max() < 4.5
+
+
 def test_render_deterministic_and_subset_consistent(gpu_ctx, cornell):
     from merian_gb300 import scene as S
     sc, sid, osc, cam = cornell
