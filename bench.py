@@ -198,6 +198,30 @@ def cpu_baseline(scene, camera, w, cpu_seconds: float, kind_label: str = "port")
             "grays_per_s": round(rays / dt / 1e9, 6)}
 
 
+def cwbvh_walk_sample(scene, camera, w, frac: float = 0.01):
+    """CWBVH nodes visited and triangles tested per closest-hit bounce ray, from a host walk
+    (the oracle's restatement of the device traversal) of the same tree the device traverses
+    (gbpt_bvh_build), over the bounce rays the FP32 oracle traces for a seeded `frac` of the
+    frame's pixels at the workload's spp and estimator."""
+    from merian_gb300 import _native as N
+    from merian_gb300 import scene as S
+    from oracle import binding as O
+    t0 = time.perf_counter()
+    nodes, tris, _ = S.build_bvh(scene)
+    osc = O.OracleScene(scene)
+    n_total = w["width"] * w["height"]
+    rng = np.random.default_rng(0x5EED)
+    pix = np.sort(rng.choice(n_total, max(1, int(n_total * frac)), replace=False)).astype(np.uint32)
+    p, keep = S.render_params(w["width"], w["height"], w["spp"], w["max_path_length"],
+                              pixels=pix, nee=w["nee"], rr_depth=w["rr_depth"], frame=0)
+    rays = O.bounce_rays(osc, camera, p, N.RAY_DTYPE)
+    _, counts = O.cwbvh_trace(nodes, tris, rays, hit_dtype=N.HIT_DTYPE)
+    osc.close()
+    return {"nodes_per_ray": float(counts[:, 0].mean()), "tris_per_ray": float(counts[:, 1].mean()),
+            "rays": int(len(rays)), "pixels": int(len(pix)),
+            "seconds": round(time.perf_counter() - t0, 1)}
+
+
 def parity_vs_fixtures(ctx, sid, cam, w):
     """Relative RMSE of the GPU estimate (headline estimator: NEE + roulette) against the FP64
     oracle fixtures of this workload (tests/golden, BSDF-only estimator: the reference's), on the
@@ -372,11 +396,19 @@ def run_gbpt(args):
     torch.cuda.synchronize()
     ms = float(np.mean(step_ms))
 
-    # untimed instrumented pass: CWBVH nodes / triangles per closest-hit ray of this workload
+    # untimed instrumented pass: CWBVH nodes / triangles per closest-hit ray of this workload by
+    # the kernel's own counters (with its postponed triangle groups)
     ctx.set_profiling(2)
     cst = ctx.render_device(sid, cam, params(frame_base + 999), out.data_ptr(), stats=True)
-    nodes_per_ray = cst.nodes_visited / max(cst.trace_rays, 1)
-    tris_per_ray = cst.tris_tested / max(cst.trace_rays, 1)
+    kernel_nodes_per_ray = cst.nodes_visited / max(cst.trace_rays, 1)
+    kernel_tris_per_ray = cst.tris_tested / max(cst.trace_rays, 1)
+    # the roofline's per-ray counts: a host walk of the same tree over a 1 % pixel sample's
+    # bounce rays (rank 0 at N = 1 with the CPU legs; else the kernel's counters)
+    walk = None
+    if world == 1 and not args.no_cpu_baseline:
+        walk = cwbvh_walk_sample(sc, cam, w)
+    nodes_per_ray = walk["nodes_per_ray"] if walk else kernel_nodes_per_ray
+    tris_per_ray = walk["tris_per_ray"] if walk else kernel_tris_per_ray
     simt = {"node_lanes_per_step": round(cst.node_lanes / max(cst.node_steps, 1), 2),
             "tri_lanes_per_step": round(cst.tri_lanes / max(cst.tri_steps, 1), 2),
             "node_steps_per_ray": round(cst.node_steps / max(cst.trace_rays, 1), 3),
@@ -466,6 +498,11 @@ def run_gbpt(args):
                          "bytes_per_ray": round(bytes_per_ray, 1),
                          "nodes_per_ray": round(nodes_per_ray, 3),
                          "tris_per_ray": round(tris_per_ray, 3),
+                         "counts_source": (f"host walk of the same CWBVH, {walk['rays']} bounce "
+                                           f"rays of {walk['pixels']} pixels (1 %)" if walk else
+                                           "kernel counters"),
+                         "kernel_nodes_per_ray": round(kernel_nodes_per_ray, 3),
+                         "kernel_tris_per_ray": round(kernel_tris_per_ray, 3),
                          "simt": simt,
                          "launches_per_step": trace_launches // max(args.steps, 1),
                          "trace_rays_per_step": trace_rays // max(args.steps, 1),

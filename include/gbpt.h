@@ -351,6 +351,20 @@ typedef struct gbpt_tuning {
 #define GBPT_BVH_FAST 1   /* one reference per triangle: fastest build, smallest tree */
 #define GBPT_BVH_MEDIUM 2 /* up to 4 references for very loose triangles only */
 
+/* The traversal data gbpt_scene_create builds for a scene (replacing the driver's BLAS / TLAS
+ * build, scene.cpp:1117-1120,1836-1882), built on the host alone, without a context or a device:
+ * for inspection and host-side traversal (CPU walks of the same tree). nodes: 80-byte CWBVH
+ * nodes (origin, exponents and inner-child mask; child and triangle bases; 8 meta bytes; 6 x 8
+ * quantised child planes); tris: 48-byte triangle records (v0 + primitive id, v1 + geometry id,
+ * v2 + flags: instance mask bits 0-7, two-sided bit 8, flip bit 9, alpha test bit 10), in leaf
+ * order. For two-level scenes the top level comes first and a top-level record holds an
+ * instance index. bvh_build is a GBPT_BVH_* value. The tree is the same on every host. */
+typedef struct gbpt_bvh gbpt_bvh;
+GBPT_API int gbpt_bvh_build(const gbpt_scene_desc* desc, int32_t bvh_build, gbpt_bvh** out);
+GBPT_API int gbpt_bvh_info(const gbpt_bvh* bvh, const void** nodes, uint64_t* node_count,
+                           const void** tris, uint64_t* tri_count, uint32_t* depth);
+GBPT_API void gbpt_bvh_free(gbpt_bvh* bvh);
+
 GBPT_API int gbpt_set_tuning(gbpt_ctx* ctx, const gbpt_tuning* tuning);
 GBPT_API int gbpt_get_tuning(gbpt_ctx* ctx, gbpt_tuning* tuning);
 /* Autotuner: renders the frame (camera, params: a whole frame, no pixel list) under candidate
@@ -507,7 +521,9 @@ GBPT_API int gbpt_graph_output(gbpt_graph* graph, const char* connector, float* 
  * gbpt_trace_primary: the hit merian's GBuffer (Raytraced) node stores for each pixel
  * (gbuffer_rt.slang:18-58) with full-precision barycentrics and t, written to a host array of
  * width*height records. gbpt_trace: closest-hit (any_hit = 0) or occlusion (any_hit = 1, only
- * t is written: 0 = occluded, -1 = clear) for n device-resident rays. */
+ * t is written: 0 = occluded, -1 = clear) for n device-resident rays, on the context tuning's
+ * traversal schedule (trace_* fields; with trace_postpone_lanes = 1 no triangle group is
+ * postponed, so nodes and triangles are visited in the order of a one-ray-at-a-time walk). */
 GBPT_API int gbpt_trace_primary(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera* camera,
                                 uint32_t width, uint32_t height, uint32_t instance_mask,
                                 gbpt_hit* out_hits_host);

@@ -235,6 +235,11 @@ EXPORTS = [
     ("gbpt_loaded_scene_warning", C.c_char_p, [C.c_void_p, C.c_uint32]),
     ("gbpt_loaded_scene_free", None, [C.c_void_p]),
     ("gbpt_gen_env", C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p]),
+    ("gbpt_bvh_build", C.c_int, [C.POINTER(SceneDesc), C.c_int32, C.POINTER(C.c_void_p)]),
+    ("gbpt_bvh_info", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
+                                C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
+                                C.POINTER(C.c_uint32)]),
+    ("gbpt_bvh_free", None, [C.c_void_p]),
     ("gbpt_graph_create", C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_void_p)]),
     ("gbpt_graph_destroy", C.c_int, [C.c_void_p]),
     ("gbpt_graph_node_count", C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),

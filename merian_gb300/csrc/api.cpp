@@ -310,10 +310,13 @@ GBPT_API int gbpt_set_profiling(gbpt_ctx* ctx, int level) {
     return GBPT_OK;
 }
 
-GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t* out_scene) {
-    int rc = check_ctx(ctx);
-    if (rc) return rc;
-    if (!d || !out_scene || (d->triangle_count && (!d->vertices || !d->indices)) ||
+// Validates a scene description and builds its traversal data on the host: the CWBVH (the top
+// level over the instances first, then every BLAS, for two-level scenes) and the instance records
+// (28 floats each). Shared by gbpt_scene_create and gbpt_bvh_build.
+static int build_scene_bvh(const gbpt_scene_desc* d, int32_t bvh_build, CwBvh& bvh,
+                           std::vector<float>& inst_rec) {
+    int rc = GBPT_OK;
+    if (!d || (d->triangle_count && (!d->vertices || !d->indices)) ||
         (d->geometry_count && !d->geometries) || (d->material_count && !d->materials)) {
         set_error("gbpt_scene_create: null pointer in scene description");
         return GBPT_ERR_INVALID;
@@ -354,7 +357,7 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
     }
     // validate geometry ranges and gather world-space triangles
     BuildInput bi;
-    set_split(bi, ctx->tuning.bvh_build, false);
+    set_split(bi, bvh_build, false);
     uint64_t total_tris = 0;
     for (uint32_t g = 0; g < d->geometry_count; ++g) {
         const gbpt_geometry& geo = d->geometries[g];
@@ -409,8 +412,6 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
         }
         return GBPT_OK;
     };
-    CwBvh bvh;
-    std::vector<float> inst_rec; // 28 floats per instance
     if (!two_level) {
         bi.v.reserve(9 * total_tris);
         bi.prim.reserve(total_tris);
@@ -427,7 +428,7 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
         std::vector<CwBvh> blas(d->blas_count);
         for (uint32_t b = 0; b < d->blas_count; ++b) {
             BuildInput in;
-            set_split(in, ctx->tuning.bvh_build, true);
+            set_split(in, bvh_build, true);
             if ((rc = gather(d->blas_ranges[b].first_geometry, d->blas_ranges[b].geometry_count, in)))
                 return rc;
             if (in.prim.empty()) {
@@ -495,6 +496,62 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
             inst_rec.insert(inst_rec.end(), rec, rec + 28);
         }
     }
+    return GBPT_OK;
+}
+
+} // extern "C"
+
+struct gbpt_bvh {
+    gbpt::CwBvh bvh;
+    std::vector<float> inst_rec;
+};
+
+extern "C" {
+
+GBPT_API int gbpt_bvh_build(const gbpt_scene_desc* d, int32_t bvh_build, gbpt_bvh** out) {
+    if (!out) {
+        set_error("gbpt_bvh_build: null output");
+        return GBPT_ERR_INVALID;
+    }
+    *out = nullptr;
+    if (bvh_build < GBPT_BVH_SPLIT || bvh_build > GBPT_BVH_MEDIUM) {
+        set_error("gbpt_bvh_build: bvh_build must be a GBPT_BVH_* value");
+        return GBPT_ERR_INVALID;
+    }
+    auto b = std::make_unique<gbpt_bvh>();
+    const int rc = build_scene_bvh(d, bvh_build, b->bvh, b->inst_rec);
+    if (rc) return rc;
+    *out = b.release();
+    return GBPT_OK;
+}
+
+GBPT_API int gbpt_bvh_info(const gbpt_bvh* b, const void** nodes, uint64_t* node_count,
+                           const void** tris, uint64_t* tri_count, uint32_t* depth) {
+    if (!b) {
+        set_error("gbpt_bvh_info: null bvh");
+        return GBPT_ERR_INVALID;
+    }
+    if (nodes) *nodes = b->bvh.nodes.data();
+    if (node_count) *node_count = b->bvh.nodes.size();
+    if (tris) *tris = b->bvh.tris.data();
+    if (tri_count) *tri_count = b->bvh.tris.size();
+    if (depth) *depth = b->bvh.depth;
+    return GBPT_OK;
+}
+
+GBPT_API void gbpt_bvh_free(gbpt_bvh* b) { delete b; }
+
+GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t* out_scene) {
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!out_scene) {
+        set_error("gbpt_scene_create: null out_scene");
+        return GBPT_ERR_INVALID;
+    }
+    const bool two_level = d && d->instance_count != 0;
+    CwBvh bvh;
+    std::vector<float> inst_rec; // 28 floats per instance
+    if ((rc = build_scene_bvh(d, ctx->tuning.bvh_build, bvh, inst_rec))) return rc;
 
     SceneGPU s;
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -1445,7 +1502,8 @@ static int trace_common(gbpt_ctx* ctx, uint32_t scene, const gbpt_ray* rays, uin
         return GBPT_ERR_NOT_FOUND;
     }
     if (npr || tpr) GBPT_CUDA_CHECK(cudaMemsetAsync(ctx->d_misc, 0, 2 * sizeof(unsigned long long), ctx->stream));
-    rc = trace_rays(it->second, rays, n, mask, any_hit, hits, ctx->d_misc, ctx->stream);
+    rc = trace_rays(it->second, rays, n, mask, any_hit, hits, ctx->d_misc, ctx->stream,
+                    sched_of(ctx->tuning));
     if (rc) {
         set_error("gbpt_trace: launch failed");
         return rc;

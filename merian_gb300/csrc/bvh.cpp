@@ -349,10 +349,11 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
     b2.reserve(2 * nref);
     b2.emplace_back();
     // Top levels serially until there are enough independent subtrees, then the subtrees in
-    // parallel into private node arrays that are appended afterwards.
+    // parallel into private node arrays that are appended afterwards. The partition is fixed (32
+    // subtrees whatever the host's core count), so every host builds the same tree.
     {
-        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-        if (nref < 200000 || hw == 1) {
+        constexpr unsigned hw = 16;
+        if (nref < 200000) {
             bld.build_range(b2, 0, 0, (uint32_t)nref);
         } else {
             // split the root range into up to 2*hw pieces by a coarse serial build (depth-limited)
@@ -607,11 +608,12 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
     out.nodes.emplace_back();
     const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     std::vector<Task> stack{{0, 0, 1}};
-    if (nref >= 200000 && hw > 1) {
-        // breadth first until the frontier holds enough subtrees
+    if (nref >= 200000) {
+        // breadth first until the frontier holds enough subtrees (a fixed number, so the layout
+        // does not depend on the host's core count)
         std::vector<Task> frontier{{0, 0, 1}};
         size_t head = 0;
-        while (head < frontier.size() && frontier.size() - head < 8 * (size_t)hw) {
+        while (head < frontier.size() && frontier.size() - head < 128) {
             const Task t = frontier[head++];
             if (!emit(t, out.nodes, out.tris, frontier, out.depth)) return false;
         }

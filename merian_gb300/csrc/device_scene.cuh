@@ -356,18 +356,26 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
     const uint4 n4 = __ldg(&s.nodes[5 * ni + 4]);
     const float kErr = 1.0f / 1048576.0f;
     const float kBiasErr = GBPT_BOX_BIAS ? 1.0f / 256.0f : 0.0f;
-    const float aix = __uint_as_float((n0.w & 0xFFu) << 23) * s.inv.x;
-    const float aiy = __uint_as_float(((n0.w >> 8) & 0xFFu) << 23) * s.inv.y;
-    const float aiz = __uint_as_float(((n0.w >> 16) & 0xFFu) << 23) * s.inv.z;
-    const float aox = (__uint_as_float(n0.x) - s.o.x) * s.inv.x;
-    const float aoy = (__uint_as_float(n0.y) - s.o.y) * s.inv.y;
-    const float aoz = (__uint_as_float(n0.z) - s.o.z) * s.inv.z;
-    const float ex = (fabsf(aox) + 255.0f * fabsf(aix)) * kErr + kBiasErr * fabsf(aix);
-    const float ey = (fabsf(aoy) + 255.0f * fabsf(aiy)) * kErr + kBiasErr * fabsf(aiy);
-    const float ez = (fabsf(aoz) + 255.0f * fabsf(aiz)) * kErr + kBiasErr * fabsf(aiz);
-    const float nox = fmaf(-kPlaneBias, aix, aox - ex), fox = fmaf(-kPlaneBias, aix, aox + ex);
-    const float noy = fmaf(-kPlaneBias, aiy, aoy - ey), foy = fmaf(-kPlaneBias, aiy, aoy + ey);
-    const float noz = fmaf(-kPlaneBias, aiz, aoz - ez), foz = fmaf(-kPlaneBias, aiz, aoz + ez);
+    // every operation rounded once in a fixed order (no contraction choices left to the
+    // compiler), so a host walk of the same tree makes the same box decisions
+    const float aix = __fmul_rn(__uint_as_float((n0.w & 0xFFu) << 23), s.inv.x);
+    const float aiy = __fmul_rn(__uint_as_float(((n0.w >> 8) & 0xFFu) << 23), s.inv.y);
+    const float aiz = __fmul_rn(__uint_as_float(((n0.w >> 16) & 0xFFu) << 23), s.inv.z);
+    const float aox = __fmul_rn(__fsub_rn(__uint_as_float(n0.x), s.o.x), s.inv.x);
+    const float aoy = __fmul_rn(__fsub_rn(__uint_as_float(n0.y), s.o.y), s.inv.y);
+    const float aoz = __fmul_rn(__fsub_rn(__uint_as_float(n0.z), s.o.z), s.inv.z);
+    const float ex = __fmaf_rn(kBiasErr, fabsf(aix),
+                               __fmul_rn(__fmaf_rn(255.0f, fabsf(aix), fabsf(aox)), kErr));
+    const float ey = __fmaf_rn(kBiasErr, fabsf(aiy),
+                               __fmul_rn(__fmaf_rn(255.0f, fabsf(aiy), fabsf(aoy)), kErr));
+    const float ez = __fmaf_rn(kBiasErr, fabsf(aiz),
+                               __fmul_rn(__fmaf_rn(255.0f, fabsf(aiz), fabsf(aoz)), kErr));
+    const float nox = __fmaf_rn(-kPlaneBias, aix, __fsub_rn(aox, ex));
+    const float fox = __fmaf_rn(-kPlaneBias, aix, __fadd_rn(aox, ex));
+    const float noy = __fmaf_rn(-kPlaneBias, aiy, __fsub_rn(aoy, ey));
+    const float foy = __fmaf_rn(-kPlaneBias, aiy, __fadd_rn(aoy, ey));
+    const float noz = __fmaf_rn(-kPlaneBias, aiz, __fsub_rn(aoz, ez));
+    const float foz = __fmaf_rn(-kPlaneBias, aiz, __fadd_rn(aoz, ez));
     imask = n0.w >> 24;
     child_base = n1.x;
     tri_base = n1.y;
@@ -388,12 +396,12 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const uint32_t sh = 8u * j;
-            const float tnx = fmaf(qplane(nqx, j), aix, nox);
-            const float tny = fmaf(qplane(nqy, j), aiy, noy);
-            const float tnz = fmaf(qplane(nqz, j), aiz, noz);
-            const float tfx = fmaf(qplane(fqx, j), aix, fox);
-            const float tfy = fmaf(qplane(fqy, j), aiy, foy);
-            const float tfz = fmaf(qplane(fqz, j), aiz, foz);
+            const float tnx = __fmaf_rn(qplane(nqx, j), aix, nox);
+            const float tny = __fmaf_rn(qplane(nqy, j), aiy, noy);
+            const float tnz = __fmaf_rn(qplane(nqz, j), aiz, noz);
+            const float tfx = __fmaf_rn(qplane(fqx, j), aix, fox);
+            const float tfy = __fmaf_rn(qplane(fqy, j), aiy, foy);
+            const float tfz = __fmaf_rn(qplane(fqz, j), aiz, foz);
             const float cmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, s.tmin));
             const float cmax = fminf(fminf(tfx, tfy), fminf(tfz, s.best.t));
             if (cmin <= cmax) hitmask |= ((child_bits4 >> sh) & 7u) << ((bit_index4 >> sh) & 31u);

@@ -36,7 +36,8 @@ GBPT_DI gbpt_hit to_hit(const DevScene& sc, const Hit& h) {
 template <bool ANY>
 __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
     k_trace_rays(DevScene sc, const gbpt_ray* rays, uint32_t n, uint32_t mask, gbpt_hit* hits,
-                 unsigned long long* work_ctr, uint32_t* fetch, uint32_t* err) {
+                 unsigned long long* work_ctr, uint32_t* fetch, uint32_t* err, int refill_lanes,
+                 int postpone_lanes) {
     TraceCounters ctr{0, 0, 0, 0, 0, 0};
     auto load = [&](uint32_t i, TraceState& s) {
         const gbpt_ray r = rays[i];
@@ -51,9 +52,8 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
     auto alpha = [&](uint32_t, uint32_t g, uint32_t p, float u, float v) {
         return alpha_discard(sc, g, p, u, v);
     };
-    const TraceSched sched;
-    trace_persistent<ANY, true, true>(n, fetch, load, store, alpha, &ctr, err,
-                                      (int)sched.refill_lanes, (int)sched.postpone_lanes);
+    trace_persistent<ANY, true, true>(n, fetch, load, store, alpha, &ctr, err, refill_lanes,
+                                      postpone_lanes);
     if (work_ctr) {
         atomicAdd(work_ctr + 0, (unsigned long long)ctr.nodes);
         atomicAdd(work_ctr + 1, (unsigned long long)ctr.tris);
@@ -149,18 +149,21 @@ CamGPU to_cam(const gbpt_camera& c) {
 } // namespace
 
 int trace_rays(const SceneGPU& scene, const gbpt_ray* rays, uint32_t n, uint32_t mask, int any_hit,
-               gbpt_hit* hits, unsigned long long* work_ctr, cudaStream_t st) {
+               gbpt_hit* hits, unsigned long long* work_ctr, cudaStream_t st,
+               const TraceSched& sched) {
     if (n == 0) return GBPT_OK;
     const DevScene sc = make_dev_scene(scene);
     uint32_t* err = reinterpret_cast<uint32_t*>(work_ctr + 2);
     uint32_t* fetch = reinterpret_cast<uint32_t*>(work_ctr + 3);
     cudaMemsetAsync(fetch, 0, sizeof(uint32_t), st);
+    const int cap = sched.blocks_per_sm ? (int)sched.blocks_per_sm * num_sms() : 1 << 30;
+    const int ra = (int)sched.refill_lanes, po = (int)sched.postpone_lanes;
     if (any_hit)
-        k_trace_rays<true><<<persistent_grid(k_trace_rays<true>), 128, 0, st>>>(
-            sc, rays, n, mask & 0xFFu, hits, work_ctr, fetch, err);
+        k_trace_rays<true><<<std::min(persistent_grid(k_trace_rays<true>), cap), 128, 0, st>>>(
+            sc, rays, n, mask & 0xFFu, hits, work_ctr, fetch, err, ra, po);
     else
-        k_trace_rays<false><<<persistent_grid(k_trace_rays<false>), 128, 0, st>>>(
-            sc, rays, n, mask & 0xFFu, hits, work_ctr, fetch, err);
+        k_trace_rays<false><<<std::min(persistent_grid(k_trace_rays<false>), cap), 128, 0, st>>>(
+            sc, rays, n, mask & 0xFFu, hits, work_ctr, fetch, err, ra, po);
     return cudaGetLastError() == cudaSuccess ? GBPT_OK : GBPT_ERR_CUDA;
 }
 

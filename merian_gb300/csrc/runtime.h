@@ -217,7 +217,8 @@ uint64_t static_scratch_paths();
 int render_frame_static(const SceneGPU& scene, const RenderArgs& args, const uint32_t* pixels_host,
                         cudaStream_t stream, std::string& err);
 int trace_rays(const SceneGPU& scene, const gbpt_ray* rays, uint32_t n, uint32_t mask, int any_hit,
-               gbpt_hit* hits, unsigned long long* counters_device, cudaStream_t stream);
+               gbpt_hit* hits, unsigned long long* counters_device, cudaStream_t stream,
+               const TraceSched& sched = TraceSched{});
 int trace_primary(const SceneGPU& scene, const gbpt_camera& cam, uint32_t w, uint32_t h,
                   uint32_t mask, gbpt_hit* hits_device, uint32_t* err_device, cudaStream_t stream);
 int gbuffer(const SceneGPU& scene, const gbpt_camera& cam, uint32_t w, uint32_t h, uint32_t mask,

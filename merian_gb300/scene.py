@@ -144,6 +144,26 @@ def soup(seed: int = BASE_SEED, n_triangles: int = 1_000_000, n_geometries: int 
     return SceneData(v, i, g, m, env)
 
 
+def build_bvh(scene: SceneData, bvh_build: int = N.BVH_SPLIT):
+    """The traversal data gbpt_scene_create builds for `scene`, built on the host (gbpt_bvh_build,
+    no device): (nodes (n, 80) uint8, triangle records (m, 48) uint8, depth)."""
+    lib = N.load()
+    d, keep = scene.desc()
+    h = C.c_void_p()
+    N.check(lib.gbpt_bvh_build(C.byref(d), bvh_build, C.byref(h)))
+    try:
+        np_, nn, tp, nt, dp = C.c_void_p(), C.c_uint64(), C.c_void_p(), C.c_uint64(), C.c_uint32()
+        N.check(lib.gbpt_bvh_info(h, C.byref(np_), C.byref(nn), C.byref(tp), C.byref(nt),
+                                  C.byref(dp)))
+        nodes = np.ctypeslib.as_array((C.c_uint8 * (80 * nn.value)).from_address(np_.value)) \
+            .reshape(-1, 80).copy() if nn.value else np.zeros((0, 80), np.uint8)
+        tris = np.ctypeslib.as_array((C.c_uint8 * (48 * nt.value)).from_address(tp.value)) \
+            .reshape(-1, 48).copy() if nt.value else np.zeros((0, 48), np.uint8)
+        return nodes, tris, dp.value
+    finally:
+        lib.gbpt_bvh_free(h)
+
+
 def look_at(position, target, up=(0.0, 1.0, 0.0), vfov_deg: float = 40.0, aspect: float = 1.0,
             near: float = 0.1, far: float = 1000.0) -> N.Camera:
     """merian Camera basis (camera.cpp:263-266,349-367); near/far are merian's defaults."""

@@ -167,6 +167,40 @@ def workload_camera(name: str, width: int | None = None, height: int | None = No
                    (width or w["width"]) / (height or w["height"]))
 
 
+def cwbvh_trace(nodes: np.ndarray, tris: np.ndarray, rays: np.ndarray, mask: int = 0xFF,
+                any_hit: bool = False, hit_dtype=None):
+    """Hits of rays through a single-level CWBVH of gbpt_bvh_build (nodes (n, 80) uint8, triangle
+    records (m, 48) uint8), and per ray (nodes visited, triangles tested): a host walk in the
+    device's traversal order with its box decisions (oracle_cwbvh_trace)."""
+    lib = load()
+    lib.oracle_cwbvh_trace.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,
+                                       C.c_void_p, C.c_uint32, C.c_uint32, C.c_int, C.c_void_p,
+                                       C.c_void_p]
+    nodes = np.ascontiguousarray(nodes, np.uint8)
+    tris = np.ascontiguousarray(tris, np.uint8)
+    rays = np.ascontiguousarray(rays)
+    hits = np.zeros(len(rays), hit_dtype)
+    counts = np.zeros((len(rays), 2), np.uint32)
+    rc = lib.oracle_cwbvh_trace(_p(nodes), len(nodes), _p(tris), len(tris), _p(rays), len(rays),
+                                mask, int(any_hit), _p(hits), _p(counts))
+    if rc != 0:
+        raise ValueError("oracle_cwbvh_trace: bad arguments")
+    return hits, counts
+
+
+def bounce_rays(osc: "OracleScene", camera, params, ray_dtype, cap: int = 1 << 24):
+    """The closest-hit bounce rays the FP32 oracle traces for params' pixels (oracle_bounce_rays):
+    a sample of the workload's bounce-ray distribution, as a ray_dtype array."""
+    lib = load()
+    lib.oracle_bounce_rays.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_uint64, C.c_void_p]
+    out = np.zeros(cap, ray_dtype)
+    n = C.c_uint64()
+    lib.oracle_bounce_rays(osc.h, C.addressof(camera), C.addressof(params), _p(out), cap,
+                           C.addressof(n))
+    return out[:min(n.value, cap)]
+
+
 def num_threads() -> int:
     return load().oracle_num_threads()
 

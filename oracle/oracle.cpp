@@ -11,6 +11,7 @@
 #include "oracle_math.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cfloat>
 #include <chrono>
@@ -924,6 +925,201 @@ ORACLE_API int oracle_trace_rays(void* sp, const gbpt_ray* rays, uint32_t n, uin
     return 0;
 }
 
+// ---- a walk of the package's CWBVH (test infrastructure) -------------------------------------
+// A host restatement of the device traversal of one ray (merian_gb300/csrc/device_scene.cuh:
+// set_ray, intersect_node, trace_loop in the per-thread order, i.e. without postponed triangle
+// groups) over the 80-byte nodes and 48-byte triangle records gbpt_bvh_build returns, for
+// single-level trees. Every box-test operation is rounded once in the device's order
+// (__fmul_rn / __fsub_rn / __fmaf_rn there, -ffp-contract=off and std::fma here), so the walk
+// makes the same box decisions: it visits the same nodes and tests the same triangles as the
+// device, and finds the same closest (or any) hit with the watertight test above. It gives the
+// node and triangle counts per ray of the roofline's algorithmic bytes.
+namespace oracle {
+namespace cw {
+constexpr float kErr = 1.0f / 1048576.0f, kBiasErr = 1.0f / 256.0f, kPlaneBias = 32768.0f;
+inline float bits_f(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+inline uint32_t f_bits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+// the device's byte permute: byte j of w in bits 8..15 of the float 32768.0
+inline float qplane(uint32_t w, int j) { return bits_f(0x47000000u | (((w >> (8 * j)) & 0xFFu) << 8)); }
+
+struct Walk {
+    const uint32_t* nodes; // 20 words per node
+    const float* tris;     // 12 floats per record
+    float o[3], inv[3], tmin;
+    uint32_t oct_inv, oct_inv4;
+    bool neg[3];
+    RayPre<float> pre;
+    float best_t, best_u, best_v;
+    uint32_t best_prim, best_geom;
+    bool found;
+};
+
+inline uint32_t intersect_node(const Walk& w, uint32_t ni, uint32_t& cb, uint32_t& tb,
+                               uint32_t& imask) {
+    const uint32_t* n = w.nodes + 20ull * ni;
+    float ai[3], no[3], fo[3];
+    for (int k = 0; k < 3; ++k) {
+        ai[k] = bits_f(((n[3] >> (8 * k)) & 0xFFu) << 23) * w.inv[k];
+        const float ao = (bits_f(n[k]) - w.o[k]) * w.inv[k];
+        const float e = std::fma(kBiasErr, std::fabs(ai[k]),
+                                 std::fma(255.0f, std::fabs(ai[k]), std::fabs(ao)) * kErr);
+        no[k] = std::fma(-kPlaneBias, ai[k], ao - e);
+        fo[k] = std::fma(-kPlaneBias, ai[k], ao + e);
+    }
+    imask = n[3] >> 24;
+    cb = n[4];
+    tb = n[5];
+    uint32_t hitmask = 0;
+    for (int half = 0; half < 2; ++half) {
+        const uint32_t meta4 = n[6 + half];
+        const uint32_t is_inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
+        const uint32_t inner_mask4 = (is_inner4 >> 4) * 0xFFu;
+        const uint32_t bit_index4 = (meta4 ^ (w.oct_inv4 & inner_mask4)) & 0x1F1F1F1Fu;
+        const uint32_t child_bits4 = (meta4 >> 5) & 0x07070707u;
+        // planes: lo x, lo y, lo z, hi x, hi y, hi z words of this half
+        const uint32_t ql[3] = {n[8 + half], n[10 + half], n[12 + half]};
+        const uint32_t qh[3] = {n[14 + half], n[16 + half], n[18 + half]};
+        for (int j = 0; j < 4; ++j) {
+            float tn[3], tf[3];
+            for (int k = 0; k < 3; ++k) {
+                tn[k] = std::fma(qplane(w.neg[k] ? qh[k] : ql[k], j), ai[k], no[k]);
+                tf[k] = std::fma(qplane(w.neg[k] ? ql[k] : qh[k], j), ai[k], fo[k]);
+            }
+            const float cmin = std::fmax(std::fmax(tn[0], tn[1]), std::fmax(tn[2], w.tmin));
+            const float cmax = std::fmin(std::fmin(tf[0], tf[1]), std::fmin(tf[2], w.best_t));
+            const uint32_t sh = 8u * j;
+            if (cmin <= cmax) hitmask |= ((child_bits4 >> sh) & 7u) << ((bit_index4 >> sh) & 31u);
+        }
+    }
+    return hitmask;
+}
+
+// one ray: adds the nodes visited and triangles tested to the counts
+inline void walk_ray(Walk& w, const gbpt_ray& r, uint32_t mask, bool any_hit, uint64_t& nodes,
+                     uint64_t& tris) {
+    for (int k = 0; k < 3; ++k) {
+        const float d = r.direction[k];
+        w.o[k] = r.origin[k];
+        w.inv[k] = 1.0f / (std::fabs(d) > 1e-20f ? d : std::copysign(1e-20f, d));
+        w.neg[k] = (f_bits(d) >> 31) != 0u;
+    }
+    const uint32_t oct = (f_bits(r.direction[0]) >> 31) | ((f_bits(r.direction[1]) >> 31) << 1) |
+                         ((f_bits(r.direction[2]) >> 31) << 2);
+    w.oct_inv = 7u - oct;
+    w.oct_inv4 = w.oct_inv * 0x01010101u;
+    w.pre = ray_pre<float>(Ray<float>{mk<float>(r.origin[0], r.origin[1], r.origin[2]),
+                                      mk<float>(r.direction[0], r.direction[1], r.direction[2]),
+                                      r.tmin, r.tmax});
+    w.tmin = r.tmin;
+    w.best_t = r.tmax;
+    w.best_u = w.best_v = 0.0f;
+    w.best_prim = w.best_geom = kNoInst;
+    w.found = false;
+    uint32_t ng[2] = {0u, 0x80000000u}, tg[2] = {0u, 0u};
+    std::vector<std::array<uint32_t, 2>> stack;
+    while (true) {
+        if (ng[1] > 0x00FFFFFFu) {
+            const uint32_t hits = ng[1];
+            const uint32_t bit = 31u - (uint32_t)__builtin_clz(hits & 0xFF000000u);
+            ng[1] &= ~(1u << bit);
+            if (ng[1] > 0x00FFFFFFu) stack.push_back({ng[0], ng[1]});
+            const uint32_t slot = (bit - 24u) ^ w.oct_inv;
+            const uint32_t ni =
+                ng[0] + (uint32_t)__builtin_popcount((hits & 0xFFu) & ((1u << slot) - 1u));
+            uint32_t cb, tb, im;
+            ++nodes;
+            const uint32_t hm = intersect_node(w, ni, cb, tb, im);
+            ng[0] = cb;
+            ng[1] = (hm & 0xFF000000u) | im;
+            tg[0] = tb;
+            tg[1] = hm & 0x00FFFFFFu;
+        } else {
+            tg[0] = ng[0];
+            tg[1] = ng[1];
+            ng[0] = ng[1] = 0u;
+        }
+        bool done = false;
+        while (tg[1] != 0u) {
+            const uint32_t b = (uint32_t)__builtin_ctz(tg[1]);
+            tg[1] &= tg[1] - 1u;
+            const float* rec = w.tris + 12ull * (tg[0] + b);
+            const uint32_t tfl = f_bits(rec[11]);
+            if (((tfl & 0xFFu) & mask) == 0u) continue;
+            ++tris;
+            const float tv[9] = {rec[0], rec[1], rec[2], rec[4], rec[5], rec[6], rec[8], rec[9],
+                                 rec[10]};
+            const uint32_t flags = ((tfl & (1u << 8)) ? GBPT_MESH_TWO_SIDED : 0u) |
+                                   ((tfl & (1u << 9)) ? GBPT_MESH_FLIP_FACING : 0u);
+            float t, u, v;
+            if (!intersect<float>(w.pre, tv, flags, w.tmin, w.best_t, t, u, v)) continue;
+            const uint32_t prim = f_bits(rec[3]), geom = f_bits(rec[7]);
+            if (t < w.best_t || geom < w.best_geom || (geom == w.best_geom && prim < w.best_prim)) {
+                w.best_t = t;
+                w.best_u = u;
+                w.best_v = v;
+                w.best_prim = prim;
+                w.best_geom = geom;
+                w.found = true;
+                if (any_hit) {
+                    done = true;
+                    break;
+                }
+            }
+        }
+        if (done) break;
+        if (ng[1] <= 0x00FFFFFFu) {
+            if (stack.empty()) break;
+            ng[0] = stack.back()[0];
+            ng[1] = stack.back()[1];
+            stack.pop_back();
+        }
+    }
+}
+} // namespace cw
+} // namespace oracle
+
+// Closest (or any) hits of n rays through a single-level CWBVH of gbpt_bvh_build (node and
+// triangle arrays as it returns them), in the gbpt_hit layout of the device's gbpt_trace, and per
+// ray the nodes visited and triangles tested (counts_out: 2 per ray, may be null).
+ORACLE_API int oracle_cwbvh_trace(const void* nodes, uint64_t n_nodes, const void* tris,
+                                  uint64_t n_tris, const gbpt_ray* rays, uint32_t n, uint32_t mask,
+                                  int any_hit, gbpt_hit* out, uint32_t* counts_out) {
+    using namespace oracle;
+    if (!nodes || !n_nodes || !tris || !rays || !out) return -1;
+    (void)n_tris;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        cw::Walk w;
+        w.nodes = (const uint32_t*)nodes;
+        w.tris = (const float*)tris;
+        uint64_t a = 0, b = 0;
+        cw::walk_ray(w, rays[i], mask & 0xFFu, any_hit != 0, a, b);
+        gbpt_hit& h = out[i];
+        const bool ok = w.found;
+        h.instance_id = ok ? 0u : kNoInst;
+        h.instance_index = ok ? 0u : kNoInst;
+        h.primitive_id = ok ? w.best_prim : kNoInst;
+        h.geometry_index = ok ? w.best_geom : kNoInst;
+        h.barycentrics[0] = ok ? w.best_u : 0.f;
+        h.barycentrics[1] = ok ? w.best_v : 0.f;
+        h.t = ok ? w.best_t : -1.0f;
+        h.reserved = 0;
+        if (counts_out) {
+            counts_out[2 * i] = (uint32_t)a;
+            counts_out[2 * i + 1] = (uint32_t)b;
+        }
+    }
+    return 0;
+}
+
 // ---- the path tracer ------------------------------------------------------------------------
 namespace oracle {
 
@@ -937,6 +1133,8 @@ struct PathCfg {
 
 struct PathCounters {
     uint64_t rays = 0;
+    // when set, the closest-hit bounce rays (path segments 2..L, not camera or shadow rays)
+    std::vector<gbpt_ray>* bounce = nullptr;
 };
 
 template <class R> struct LightSample {
@@ -1135,6 +1333,18 @@ V3<R> trace_path(const Scene& s, const PathCfg& cfg, Ray<R> ray, SP<R> sp, Pcg& 
         ray.tmin = R(0);
         ray.tmax = R(1e7f);
         ctr.rays++;
+        if (ctr.bounce) {
+            gbpt_ray g{};
+            g.origin[0] = (float)ray.o.x;
+            g.origin[1] = (float)ray.o.y;
+            g.origin[2] = (float)ray.o.z;
+            g.direction[0] = (float)ray.d.x;
+            g.direction[1] = (float)ray.d.y;
+            g.direction[2] = (float)ray.d.z;
+            g.tmin = (float)ray.tmin;
+            g.tmax = (float)ray.tmax;
+            ctr.bounce->push_back(g);
+        }
         const HitRec h = trace<R>(s, ray, cfg.mask, false);
         sp = shading_point<R>(s, ray, h, current_ior, bounce + 1 < cfg.max_path_length, false);
         V3<R> e = throughput * sp.emission;
@@ -1239,6 +1449,35 @@ ORACLE_API int oracle_render(void* sp, const gbpt_camera* cam, const gbpt_render
         rays += ctr.rays;
     }
     if (out_rays) *out_rays = rays;
+    return 0;
+}
+
+// The closest-hit bounce rays (segments 2..L of every path) the FP32 build traces for the listed
+// pixels at p->spp: a sample of a workload's bounce-ray distribution. Writes up to `cap` rays,
+// in pixel order, and their number in *n_out (the total, which may exceed cap).
+ORACLE_API int oracle_bounce_rays(void* sp, const gbpt_camera* cam, const gbpt_render_params* p,
+                                  gbpt_ray* out, uint64_t cap, uint64_t* n_out) {
+    const Scene& s = *(const Scene*)sp;
+    PathCfg cfg{p->max_path_length, p->emission_on_primary != 0, p->instance_mask & 0xFFu,
+                p->nee != 0, p->rr_depth};
+    const uint32_t n = p->pixel_count ? p->pixel_count : p->width * p->height;
+    std::vector<std::vector<gbpt_ray>> per(n);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        const uint32_t pix = p->pixel_count ? p->pixels[i] : (uint32_t)i;
+        PathCounters ctr;
+        ctr.bounce = &per[i];
+        double rgba[4];
+        render_pixel<float>(s, *cam, *p, cfg, pix % p->width, pix / p->width, rgba, nullptr,
+                            nullptr, ctr);
+    }
+    uint64_t k = 0;
+    for (const auto& v : per)
+        for (const gbpt_ray& r : v) {
+            if (k < cap && out) out[k] = r;
+            ++k;
+        }
+    if (n_out) *n_out = k;
     return 0;
 }
 
