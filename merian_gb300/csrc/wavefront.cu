@@ -783,30 +783,7 @@ struct Grids {
     int shade_p;
     int shade;
 };
-// The traversal kernels keep their stacks in local memory and reread nodes and triangles
-// through L1; they use almost no shared memory, so they ask for the largest L1 share.
-#ifndef GBPT_TRACE_MAX_L1
-#define GBPT_TRACE_MAX_L1 1
-#endif
-template <class K> void prefer_l1(K kernel) {
-    if (GBPT_TRACE_MAX_L1)
-        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             cudaSharedmemCarveoutMaxL1);
-}
-
 Grids launch_grids() {
-    prefer_l1(k_trace<false, false, false>);
-    prefer_l1(k_trace<false, false, true>);
-    prefer_l1(k_trace<false, true, false>);
-    prefer_l1(k_trace<false, true, true>);
-    prefer_l1(k_trace<true, false, false>);
-    prefer_l1(k_trace<true, false, true>);
-    prefer_l1(k_trace<true, true, false>);
-    prefer_l1(k_trace<true, true, true>);
-    prefer_l1(k_shadow<false, false>);
-    prefer_l1(k_shadow<false, true>);
-    prefer_l1(k_shadow<true, false>);
-    prefer_l1(k_shadow<true, true>);
     Grids g;
     g.grid = num_sms() * 8;
     // the two-level and alpha variants have the same launch bounds, hence the same residency
