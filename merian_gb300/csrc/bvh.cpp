@@ -11,6 +11,7 @@
 #include "host_common.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cfloat>
 #include <cmath>
@@ -63,6 +64,17 @@ constexpr size_t kMaxReferences = size_t(1) << 28;
 constexpr int kBins = GBPT_BVH_BINS;
 constexpr float kCostTraverse = GBPT_BVH_TRAVERSE_COST; // relative to one triangle test
 constexpr uint32_t kMaxLeaf = 3;      // CWBVH leaf children hold up to three triangles
+// The collapse to 8-wide nodes: SAH-optimal by dynamic programming over the binary tree (1), or
+// greedy, opening the largest child until eight slots are taken (0). The DP weighs a visit of a
+// wide node (its eight box tests) against one triangle test; 1.3 is the ratio the traversal
+// kernel's time shows per node visited and per triangle tested.
+#ifndef GBPT_BVH_DP_COLLAPSE
+#define GBPT_BVH_DP_COLLAPSE 1
+#endif
+#ifndef GBPT_BVH_NODE_COST
+#define GBPT_BVH_NODE_COST 1.3f
+#endif
+constexpr float kWideNodeCost = GBPT_BVH_NODE_COST;
 
 struct Builder {
     const std::vector<Box>& pbox;
@@ -432,11 +444,91 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
         }
     }
 
+    // ---- SAH-optimal collapse (Ylitie, Karras and Laine 2017, section 3.1) -----------------
+    // cost[n][i-1]: the least SAH cost of the subtree of binary node n when it fills at most i
+    // child slots of a wide node (i = 1..7), in units of one triangle test; a slot holds a leaf
+    // of at most three triangles or an inner child that becomes a wide node itself. choice[n]:
+    // [0] 1 when n as one slot is an inner child (0: a leaf), [i-1] for i >= 2 the slots given to
+    // the left child (0: the best with i - 1 slots), [7] the left child's slots when n is a wide
+    // node of its own (eight slots between its two children). Children have larger indices than
+    // their parents, so one pass from the back visits children first.
+    bool use_dp = GBPT_BVH_DP_COLLAPSE != 0;
+    std::vector<std::array<float, 7>> dp_cost;
+    std::vector<std::array<uint8_t, 8>> dp_choice;
+    if (use_dp) {
+        dp_cost.resize(b2.size());
+        dp_choice.assign(b2.size(), std::array<uint8_t, 8>{});
+        for (size_t q = b2.size(); q-- > 0;) {
+            const B2Node& nd = b2[q];
+            const float area = nd.box.area();
+            std::array<float, 7>& C = dp_cost[q];
+            std::array<uint8_t, 8>& D = dp_choice[q];
+            if (nd.leaf) {
+                C.fill(area * (float)nd.count);
+                continue;
+            }
+            const std::array<float, 7>& L = dp_cost[nd.left];
+            const std::array<float, 7>& R = dp_cost[nd.right];
+            float d8 = INFINITY;
+            for (int k = 1; k <= 7; ++k) {
+                const float v = L[k - 1] + R[8 - k - 1];
+                if (v < d8) {
+                    d8 = v;
+                    D[7] = (uint8_t)k;
+                }
+            }
+            const float as_node = area * kWideNodeCost + d8;
+            const float as_leaf = nd.count <= kMaxLeaf ? area * (float)nd.count : INFINITY;
+            C[0] = std::min(as_leaf, as_node);
+            D[0] = as_leaf <= as_node ? 0 : 1;
+            for (int i = 2; i <= 7; ++i) {
+                float best = C[i - 2];
+                uint8_t ch = 0;
+                for (int k = 1; k < i; ++k) {
+                    const float v = L[k - 1] + R[i - k - 1];
+                    if (v < best) {
+                        best = v;
+                        ch = (uint8_t)k;
+                    }
+                }
+                C[i - 1] = best;
+                D[i - 1] = ch;
+            }
+        }
+    }
+
     // ---- collapse to 8-wide and emit ----------------------------------------------------------
     struct Task {
         uint32_t b2node, cw, depth;
     };
     auto is_inner = [&](uint32_t k) { return !b2[k].leaf && b2[k].count > kMaxLeaf; };
+    // the DP's children of wide node n: the slots of its two children, each slot an inner child
+    // or a leaf
+    auto dp_children = [&](uint32_t n, SmallVec<uint32_t, 8>& ch, bool* inner) {
+        struct Item {
+            uint32_t node;
+            int slots;
+        };
+        SmallVec<Item, 16> st;
+        const int k8 = dp_choice[n][7];
+        st.push_back({b2[n].right, 8 - k8});
+        st.push_back({b2[n].left, k8});
+        while (st.size()) {
+            const Item it = st.v[--st.n];
+            if (it.slots == 1 || b2[it.node].leaf) {
+                inner[ch.size()] = !b2[it.node].leaf && dp_choice[it.node][0] == 1;
+                ch.push_back(it.node);
+                continue;
+            }
+            const int k = dp_choice[it.node][it.slots - 1];
+            if (k == 0) {
+                st.push_back({it.node, it.slots - 1});
+            } else {
+                st.push_back({b2[it.node].right, it.slots - k});
+                st.push_back({b2[it.node].left, k});
+            }
+        }
+    };
     // One CWBVH node from task t into (nodes, tris); its inner children become tasks. Returns
     // false when the tree is deeper than max_depth.
     auto emit = [&](const Task t, std::vector<CwNode>& nodes, std::vector<TriRecord>& tris,
@@ -447,7 +539,11 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
             return false;
         }
         SmallVec<uint32_t, 8> ch;
-        if (is_inner(t.b2node)) {
+        bool inner[8] = {};
+        if (use_dp && !b2[t.b2node].leaf && (t.b2node != 0 || b2[0].count > kMaxLeaf ||
+                                              dp_choice[0][0] == 1)) {
+            dp_children(t.b2node, ch, inner);
+        } else if (is_inner(t.b2node)) {
             ch.push_back(b2[t.b2node].left);
             ch.push_back(b2[t.b2node].right);
             while (ch.size() < 8) {
@@ -480,6 +576,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
                 ch[best] = b2[k].left;
                 ch.push_back(b2[k].right);
             }
+            for (size_t i = 0; i < ch.size(); ++i) inner[i] = is_inner(ch[i]);
         } else {
             ch.push_back(t.b2node); // the whole tree is one leaf
         }
@@ -561,7 +658,7 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
                 qlo[a][s] = (uint8_t)lo;
                 qhi[a][s] = (uint8_t)hi;
             }
-            if (is_inner(ch[i])) {
+            if (inner[i]) {
                 imask |= 1u << s;
                 meta[s] = (uint8_t)((1u << 5) | (24u + (uint32_t)s));
                 push.push_back({ch[i], child_base + n_inner, t.depth + 1});
@@ -602,7 +699,12 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
     };
     // The top of the tree serially until there are enough independent subtrees, then every
     // subtree into its own arrays in parallel, appended in order with rebased node and triangle
-    // indices (the layout is deterministic).
+    // indices (the layout is deterministic). A DP tree deeper than max_depth falls back to the
+    // greedy collapse.
+    auto collapse = [&]() -> bool {
+    out.nodes.clear();
+    out.tris.clear();
+    out.depth = 0;
     out.nodes.reserve(b2.size() / 4 + 1);
     out.tris.reserve(nref);
     out.nodes.emplace_back();
@@ -671,6 +773,11 @@ bool build_cwbvh(const BuildInput& in, CwBvh& out, uint32_t max_depth) {
         }
     }
     return true;
+    };
+    if (collapse()) return true;
+    if (!use_dp) return false;
+    use_dp = false;
+    return collapse();
 }
 
 } // namespace gbpt

@@ -16,7 +16,7 @@ import pytest
 from oracle import binding as O
 
 # sha256 prefix of the soup_small tree (nodes then triangle records), whatever the host
-SOUP_SMALL_BVH = "934d3554852ae135"
+SOUP_SMALL_BVH = "5aa977400ed3122e"
 
 
 def _soup_small():
