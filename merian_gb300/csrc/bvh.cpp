@@ -66,13 +66,16 @@ constexpr float kCostTraverse = GBPT_BVH_TRAVERSE_COST; // relative to one trian
 constexpr uint32_t kMaxLeaf = 3;      // CWBVH leaf children hold up to three triangles
 // The collapse to 8-wide nodes: SAH-optimal by dynamic programming over the binary tree (1), or
 // greedy, opening the largest child until eight slots are taken (0). The DP weighs a visit of a
-// wide node (its eight box tests) against one triangle test; 1.3 is the ratio the traversal
-// kernel's time shows per node visited and per triangle tested.
+// wide node (its eight box tests) against one triangle test. Fitted to the closest-hit
+// traversal's time on the 1M-triangle soup a triangle test costs about three node visits (lanes
+// test triangles one or two at a time while node steps keep most of the warp busy); below about
+// 0.7 the DP reaches the fewest triangle tests the binary leaves allow, and 0.5 measured fastest
+// (1.3: 3 % slower).
 #ifndef GBPT_BVH_DP_COLLAPSE
 #define GBPT_BVH_DP_COLLAPSE 1
 #endif
 #ifndef GBPT_BVH_NODE_COST
-#define GBPT_BVH_NODE_COST 1.3f
+#define GBPT_BVH_NODE_COST 0.5f
 #endif
 constexpr float kWideNodeCost = GBPT_BVH_NODE_COST;
 

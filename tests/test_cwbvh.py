@@ -16,7 +16,7 @@ import pytest
 from oracle import binding as O
 
 # sha256 prefix of the soup_small tree (nodes then triangle records), whatever the host
-SOUP_SMALL_BVH = "5aa977400ed3122e"
+SOUP_SMALL_BVH = "e7c987c5f2a72ad1"
 
 
 def _soup_small():
