@@ -122,44 +122,49 @@ GBPT_DI bool alpha_discard(const DevScene& sc, uint32_t geom, uint32_t prim, flo
 // Explicit round-to-nearest intrinsics (no FMA contraction) so the float result equals the
 // host oracle's bit for bit.
 struct RayPre {
-    int kx, ky, kz;
+    uint32_t k; // the axes kx, ky, kz in bits 0-1, 2-3, 4-5 (one register for the three)
     float Sx, Sy, Sz;
     float ox, oy, oz; // origin permuted to (kx, ky, kz)
+    GBPT_DI int kx() const { return (int)(k & 3u); }
+    GBPT_DI int ky() const { return (int)((k >> 2) & 3u); }
+    GBPT_DI int kz() const { return (int)((k >> 4) & 3u); }
 };
 GBPT_DI float pick(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
 GBPT_DI RayPre ray_pre(float3 o, float3 d) {
     RayPre p;
     const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
-    p.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
-    p.kx = p.kz == 2 ? 0 : p.kz + 1;
-    p.ky = p.kx == 2 ? 0 : p.kx + 1;
-    const float dkz = pick(d.x, d.y, d.z, p.kz);
+    const int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int kx = kz == 2 ? 0 : kz + 1;
+    int ky = kx == 2 ? 0 : kx + 1;
+    const float dkz = pick(d.x, d.y, d.z, kz);
     if (dkz < 0.0f) {
-        const int t = p.kx;
-        p.kx = p.ky;
-        p.ky = t;
+        const int t = kx;
+        kx = ky;
+        ky = t;
     }
-    p.Sx = __fdiv_rn(pick(d.x, d.y, d.z, p.kx), dkz);
-    p.Sy = __fdiv_rn(pick(d.x, d.y, d.z, p.ky), dkz);
+    p.k = (uint32_t)kx | ((uint32_t)ky << 2) | ((uint32_t)kz << 4);
+    p.Sx = __fdiv_rn(pick(d.x, d.y, d.z, kx), dkz);
+    p.Sy = __fdiv_rn(pick(d.x, d.y, d.z, ky), dkz);
     p.Sz = __fdiv_rn(1.0f, dkz);
-    p.ox = pick(o.x, o.y, o.z, p.kx);
-    p.oy = pick(o.x, o.y, o.z, p.ky);
-    p.oz = pick(o.x, o.y, o.z, p.kz);
+    p.ox = pick(o.x, o.y, o.z, kx);
+    p.oy = pick(o.x, o.y, o.z, ky);
+    p.oz = pick(o.x, o.y, o.z, kz);
     return p;
 }
 
 // Returns true with t, u, v when hit within [tmin, tmax] on an accepted face.
 GBPT_DI bool intersect_tri(const RayPre& p, float4 a4, float4 b4, float4 c4, uint32_t tflags,
                            float tmin, float tmax, float& t_out, float& u_out, float& v_out) {
-    const float Akx = __fsub_rn(pick(a4.x, a4.y, a4.z, p.kx), p.ox);
-    const float Aky = __fsub_rn(pick(a4.x, a4.y, a4.z, p.ky), p.oy);
-    const float Akz = __fsub_rn(pick(a4.x, a4.y, a4.z, p.kz), p.oz);
-    const float Bkx = __fsub_rn(pick(b4.x, b4.y, b4.z, p.kx), p.ox);
-    const float Bky = __fsub_rn(pick(b4.x, b4.y, b4.z, p.ky), p.oy);
-    const float Bkz = __fsub_rn(pick(b4.x, b4.y, b4.z, p.kz), p.oz);
-    const float Ckx = __fsub_rn(pick(c4.x, c4.y, c4.z, p.kx), p.ox);
-    const float Cky = __fsub_rn(pick(c4.x, c4.y, c4.z, p.ky), p.oy);
-    const float Ckz = __fsub_rn(pick(c4.x, c4.y, c4.z, p.kz), p.oz);
+    const int kx = p.kx(), ky = p.ky(), kz = p.kz();
+    const float Akx = __fsub_rn(pick(a4.x, a4.y, a4.z, kx), p.ox);
+    const float Aky = __fsub_rn(pick(a4.x, a4.y, a4.z, ky), p.oy);
+    const float Akz = __fsub_rn(pick(a4.x, a4.y, a4.z, kz), p.oz);
+    const float Bkx = __fsub_rn(pick(b4.x, b4.y, b4.z, kx), p.ox);
+    const float Bky = __fsub_rn(pick(b4.x, b4.y, b4.z, ky), p.oy);
+    const float Bkz = __fsub_rn(pick(b4.x, b4.y, b4.z, kz), p.oz);
+    const float Ckx = __fsub_rn(pick(c4.x, c4.y, c4.z, kx), p.ox);
+    const float Cky = __fsub_rn(pick(c4.x, c4.y, c4.z, ky), p.oy);
+    const float Ckz = __fsub_rn(pick(c4.x, c4.y, c4.z, kz), p.oz);
     const float Ax = __fsub_rn(Akx, __fmul_rn(p.Sx, Akz));
     const float Ay = __fsub_rn(Aky, __fmul_rn(p.Sy, Akz));
     const float Bx = __fsub_rn(Bkx, __fmul_rn(p.Sx, Bkz));
@@ -251,9 +256,6 @@ GBPT_DI float3 xform_vector(float4 r0, float4 r1, float4 r2, float3 v) {
 // (t is unchanged: the direction is not renormalised) and continues from the BLAS root; when the
 // stack drops back to the entry depth the world ray is restored. The closest hit and the tie rule
 // (equal t: smallest geometry, primitive, instance) do not depend on the visit order.
-#ifndef GBPT_SMEM_STACK
-#define GBPT_SMEM_STACK 0
-#endif
 
 
 struct TraceState {
@@ -263,13 +265,11 @@ struct TraceState {
     uint32_t mask;       // instance mask of the ray
     float3 o, d, inv;    // the ray in the current space (object space inside an instance)
     float tmin;
-    uint32_t oct_inv, oct_inv4;
-    bool negx, negy, negz;
+    uint32_t oct_inv; // 7 - direction octant (bit a set: axis a positive)
     RayPre pre;
     uint2 ngroup, tgroup;
     int sp;
-    Hit best;
-    bool found;
+    Hit best;          // a hit was found once best.geom != kNoInst
     float3 wo, wd; // the world ray
     uint32_t inst; // instance being traversed, kNoInst at the top level
     int inst_sp;   // stack depth at which it was entered
@@ -282,10 +282,6 @@ GBPT_DI void set_ray(TraceState& s, float3 o, float3 d) {
     const uint32_t oct = (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) |
                          ((__float_as_uint(d.z) >> 31) << 2);
     s.oct_inv = 7u - oct;
-    s.oct_inv4 = s.oct_inv * 0x01010101u;
-    s.negx = (__float_as_uint(d.x) >> 31) != 0u;
-    s.negy = (__float_as_uint(d.y) >> 31) != 0u;
-    s.negz = (__float_as_uint(d.z) >> 31) != 0u;
     s.pre = ray_pre(o, d);
 }
 
@@ -300,7 +296,6 @@ GBPT_DI void trace_init(TraceState& s, float3 o, float3 d, float tmin, float tma
     s.best.t = tmax;
     s.best.u = s.best.v = 0.0f;
     s.best.prim = s.best.geom = s.best.inst = kNoInst;
-    s.found = false;
     s.inst = kNoInst;
     s.inst_sp = -1;
 }
@@ -379,20 +374,24 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
     imask = n0.w >> 24;
     child_base = n1.x;
     tri_base = n1.y;
+    // the direction's signs from the octant (negative axis a: bit a of oct_inv clear)
+    const uint32_t oct_inv4 = s.oct_inv * 0x01010101u;
+    const bool negx = (s.oct_inv & 1u) == 0u, negy = (s.oct_inv & 2u) == 0u;
+    const bool negz = (s.oct_inv & 4u) == 0u;
     uint32_t hitmask = 0;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
         const uint32_t meta4 = half ? n1.w : n1.z;
         const uint32_t is_inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
         const uint32_t inner_mask4 = (is_inner4 >> 4) * 0xFFu;
-        const uint32_t bit_index4 = (meta4 ^ (s.oct_inv4 & inner_mask4)) & 0x1F1F1F1Fu;
+        const uint32_t bit_index4 = (meta4 ^ (oct_inv4 & inner_mask4)) & 0x1F1F1F1Fu;
         const uint32_t child_bits4 = (meta4 >> 5) & 0x07070707u;
         const uint32_t qlx = half ? n2.y : n2.x, qly = half ? n2.w : n2.z;
         const uint32_t qlz = half ? n3.y : n3.x, qhx = half ? n3.w : n3.z;
         const uint32_t qhy = half ? n4.y : n4.x, qhz = half ? n4.w : n4.z;
-        const uint32_t nqx = s.negx ? qhx : qlx, fqx = s.negx ? qlx : qhx;
-        const uint32_t nqy = s.negy ? qhy : qly, fqy = s.negy ? qly : qhy;
-        const uint32_t nqz = s.negz ? qhz : qlz, fqz = s.negz ? qlz : qhz;
+        const uint32_t nqx = negx ? qhx : qlx, fqx = negx ? qlx : qhx;
+        const uint32_t nqy = negy ? qhy : qly, fqy = negy ? qly : qhy;
+        const uint32_t nqz = negz ? qhz : qlz, fqz = negz ? qlz : qhz;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const uint32_t sh = 8u * j;
@@ -497,7 +496,6 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
                 s.best.prim = prim;
                 s.best.geom = geom;
                 s.best.inst = s.inst;
-                s.found = true;
                 if (ANY) {
                     done_any = true;
                     break;
@@ -513,7 +511,6 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
         if (done) break;
         if (WARP && !pool_empty && __popc(__activemask()) < refill_lanes) return false;
     }
-    if (!s.found) s.best.geom = s.best.prim = s.best.inst = kNoInst;
     return true;
 }
 
@@ -548,19 +545,8 @@ __device__ __forceinline__ void trace_persistent(uint32_t n, uint32_t* fetch, Lo
                                                  uint32_t* err, int refill_lanes,
                                                  int postpone_lanes) {
     const uint32_t lane = threadIdx.x & 31u;
-#if GBPT_SMEM_STACK > 0
-    // the first GBPT_SMEM_STACK entries of every thread's stack in shared memory (thread-strided:
-    // no bank conflicts), the rest in local memory; launched with 128-thread blocks
-    __shared__ uint2 smem_stack[GBPT_SMEM_STACK * 128];
-    uint2 stack_local[kStackSize - GBPT_SMEM_STACK];
-    auto st_ref = [&](int i) -> uint2& {
-        return i < GBPT_SMEM_STACK ? smem_stack[i * 128 + threadIdx.x]
-                                   : stack_local[i - GBPT_SMEM_STACK];
-    };
-#else
     uint2 stack[kStackSize];
     auto st_ref = [&](int i) -> uint2& { return stack[i]; };
-#endif
     TraceState s;
     uint32_t ray = 0xFFFFFFFFu;
     bool active = false, exhausted = false;
