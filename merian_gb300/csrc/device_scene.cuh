@@ -9,6 +9,8 @@
 #pragma once
 
 #include "device_math.cuh"
+
+#include <type_traits>
 #include "gbpt.h"
 
 namespace gbpt {
@@ -335,6 +337,29 @@ constexpr float kPlaneBias = 0.0f;
 GBPT_DI float qplane(uint32_t w, int j) { return (float)((w >> (8 * j)) & 0xFFu); }
 #endif
 
+// GBPT_BOX_FMA2: the plane distances of two children with one paired FP32 FMA (fma.rn.f32x2).
+#ifndef GBPT_BOX_FMA2
+#define GBPT_BOX_FMA2 1
+#endif
+GBPT_DI uint64_t pack2(float lo, float hi) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+// the biased planes of children J and J + 1 of word w (as qplane), times a plus o, per lane
+template <int J> GBPT_DI float2 plane_t2(uint32_t w, uint64_t a2, uint64_t o2) {
+    float2 r;
+    asm("{\n\t.reg .b32 q0, q1;\n\t.reg .b64 q, d;\n\t"
+        "prmt.b32 q0, %2, 0x47000000, %3;\n\t"
+        "prmt.b32 q1, %2, 0x47000000, %4;\n\t"
+        "mov.b64 q, {q0, q1};\n\t"
+        "fma.rn.f32x2 d, q, %5, %6;\n\t"
+        "mov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "r"(w), "n"(0x7504 | (J << 4)), "n"(0x7504 | ((J + 1) << 4)), "l"(a2), "l"(o2));
+    return r;
+}
+
 // Intersects the 8 children of node `ni`; returns the hit mask (inner children in bits 24..31 in
 // traversal order, triangles in bits 0..23) and the node's child / triangle bases and imask.
 // The quantised planes are dequantised with a per-axis slack of 2^-20 of the plane distance
@@ -374,6 +399,11 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
     imask = n0.w >> 24;
     child_base = n1.x;
     tri_base = n1.y;
+#if GBPT_BOX_FMA2
+    const uint64_t ax2 = pack2(aix, aix), ay2 = pack2(aiy, aiy), az2 = pack2(aiz, aiz);
+    const uint64_t nox2 = pack2(nox, nox), noy2 = pack2(noy, noy), noz2 = pack2(noz, noz);
+    const uint64_t fox2 = pack2(fox, fox), foy2 = pack2(foy, foy), foz2 = pack2(foz, foz);
+#endif
     // the direction's signs from the octant (negative axis a: bit a of oct_inv clear)
     const uint32_t oct_inv4 = s.oct_inv * 0x01010101u;
     const bool negx = (s.oct_inv & 1u) == 0u, negy = (s.oct_inv & 2u) == 0u;
@@ -392,6 +422,27 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
         const uint32_t nqx = negx ? qhx : qlx, fqx = negx ? qlx : qhx;
         const uint32_t nqy = negy ? qhy : qly, fqy = negy ? qly : qhy;
         const uint32_t nqz = negz ? qhz : qlz, fqz = negz ? qlz : qhz;
+#if GBPT_BOX_FMA2
+        // children j and j + 1 of the half at once: the paired FP32 FMA rounds each lane like
+        // __fmaf_rn, so the decisions are the scalar ones
+        auto pair = [&](auto jc) {
+            constexpr int j = decltype(jc)::value;
+            const float2 tnx = plane_t2<j>(nqx, ax2, nox2), tny = plane_t2<j>(nqy, ay2, noy2);
+            const float2 tnz = plane_t2<j>(nqz, az2, noz2), tfx = plane_t2<j>(fqx, ax2, fox2);
+            const float2 tfy = plane_t2<j>(fqy, ay2, foy2), tfz = plane_t2<j>(fqz, az2, foz2);
+            const float cmin0 = fmaxf(fmaxf(tnx.x, tny.x), fmaxf(tnz.x, s.tmin));
+            const float cmax0 = fminf(fminf(tfx.x, tfy.x), fminf(tfz.x, s.best.t));
+            const float cmin1 = fmaxf(fmaxf(tnx.y, tny.y), fmaxf(tnz.y, s.tmin));
+            const float cmax1 = fminf(fminf(tfx.y, tfy.y), fminf(tfz.y, s.best.t));
+            constexpr uint32_t sh0 = 8u * j, sh1 = 8u * (j + 1);
+            if (cmin0 <= cmax0)
+                hitmask |= ((child_bits4 >> sh0) & 7u) << ((bit_index4 >> sh0) & 31u);
+            if (cmin1 <= cmax1)
+                hitmask |= ((child_bits4 >> sh1) & 7u) << ((bit_index4 >> sh1) & 31u);
+        };
+        pair(std::integral_constant<int, 0>{});
+        pair(std::integral_constant<int, 2>{});
+#else
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const uint32_t sh = 8u * j;
@@ -405,6 +456,7 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
             const float cmax = fminf(fminf(tfx, tfy), fminf(tfz, s.best.t));
             if (cmin <= cmax) hitmask |= ((child_bits4 >> sh) & 7u) << ((bit_index4 >> sh) & 31u);
         }
+#endif
     }
     return hitmask;
 }
