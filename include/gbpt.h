@@ -340,7 +340,9 @@ typedef struct gbpt_tuning {
     int32_t trace_refill_lanes;   /* a warp refills its idle lanes with new rays once fewer than
                                      this many lanes are busy: [1, 32], default 20 */
     int32_t trace_postpone_lanes; /* a lane pushes its triangle group for later when fewer than
-                                     this many lanes have triangles to test: [1, 32], default 6 */
+                                     this many lanes have triangles to test: [1, 32], default 6;
+                                     closest-hit traversal only (a first-hit query tests its
+                                     triangles at once) */
     int32_t trace_blocks_per_sm;  /* 128-thread blocks per SM of the traversal launches: [1, 64],
                                      capped at what is resident; default all resident */
 } gbpt_tuning;

@@ -121,7 +121,7 @@ bool invert_affine(const float* m, double* inv) {
 }
 
 void free_scene(SceneGPU& s) {
-    void* ptrs[] = {s.nodes,    s.tris,     s.verts,      s.idx,       s.geoms,    s.mats,
+    void* ptrs[] = {s.nodes,    s.tris,     s.verts,      s.idx,       s.tri_verts, s.geoms,    s.mats,
                     s.env,      s.env_marg, s.env_cond,   s.env_func,  s.light_tris, s.light_cdf,
                     s.light_guide, s.env_marg_guide, s.env_cond_guide, s.geom_key,
                     s.inst,     s.tex,      s.tex_info,   s.srgb_lut};
@@ -146,6 +146,10 @@ std::vector<uint32_t> cdf_guide(const float* a, uint32_t n, uint32_t& G) {
 // single-level scenes (measured on the 1M-triangle soup: ratio 2 / depth 4 renders 25 % faster
 // than no splitting) and lightly in the BLASes of two-level scenes (instanced meshes: ratio 8 /
 // depth 2 is 5 % faster than none, ratio 2 / depth 4 5 % slower).
+// GBPT_SHADE_TRI_RECORDS: upload the de-indexed per-triangle vertex records read by shading
+#ifndef GBPT_SHADE_TRI_RECORDS
+#define GBPT_SHADE_TRI_RECORDS 1
+#endif
 #ifndef GBPT_BVH_SPLIT_RATIO
 #define GBPT_BVH_SPLIT_RATIO 2.0
 #endif
@@ -564,6 +568,36 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
     if ((rc = upload(&s.tris, bvh.tris.data(), bvh.tris.size() * sizeof(TriRecord), bytes))) return fail(rc);
     if ((rc = upload(&s.verts, d->vertices, d->vertex_count * sizeof(gbpt_packed_vertex), bytes))) return fail(rc);
     if ((rc = upload(&s.idx, d->indices, d->triangle_count * 3 * sizeof(uint32_t), bytes))) return fail(rc);
+#if GBPT_SHADE_TRI_RECORDS
+    // the vertices of each triangle in one record, so shading reads one 80-byte run instead of an
+    // index triple and then three vertices; kept only when every triangle has one first vertex
+    if (d->triangle_count) {
+        constexpr uint32_t kUnset = 0xFFFFFFFFu;
+        std::vector<uint32_t> fv(d->triangle_count, kUnset);
+        bool unique = true;
+        for (uint32_t g = 0; g < d->geometry_count && unique; ++g) {
+            const gbpt_geometry& geo = d->geometries[g];
+            for (uint32_t k = 0; k < geo.triangle_count; ++k) {
+                uint32_t& f = fv[(uint64_t)geo.first_triangle + k];
+                if (f != kUnset && f != geo.first_vertex) {
+                    unique = false;
+                    break;
+                }
+                f = geo.first_vertex;
+            }
+        }
+        if (unique) {
+            std::vector<uint32_t> rec(20ull * d->triangle_count, 0u);
+            for (uint64_t t = 0; t < d->triangle_count; ++t) {
+                if (fv[t] == kUnset) continue;
+                for (int c = 0; c < 3; ++c)
+                    std::memcpy(&rec[20 * t + 6 * c], &d->vertices[(uint64_t)fv[t] + d->indices[3 * t + c]],
+                                sizeof(gbpt_packed_vertex));
+            }
+            if ((rc = upload(&s.tri_verts, rec.data(), rec.size() * sizeof(uint32_t), bytes))) return fail(rc);
+        }
+    }
+#endif
     std::vector<GeomHost> gh(d->geometry_count);
     for (uint32_t g = 0; g < d->geometry_count; ++g)
         gh[g] = {d->geometries[g].first_vertex, d->geometries[g].first_triangle,

@@ -29,6 +29,7 @@ struct DevScene {
     const float4* __restrict__ tris;  // 3 per triangle record
     const uint32_t* __restrict__ verts; // gbpt_packed_vertex as 6 words
     const uint32_t* __restrict__ idx;
+    const uint4* __restrict__ tri_verts; // 5 per triangle (3 vertices, padded) or null
     const GeomGPU* __restrict__ geoms;
     const float4* __restrict__ mats;  // gbpt_material as 5 float4
     uint32_t geom_count;
@@ -107,8 +108,9 @@ GBPT_DI bool alpha_discard(const DevScene& sc, uint32_t geom, uint32_t prim, flo
     float uvx[3], uvy[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const uint32_t vi = g.first_vertex + __ldg(&sc.idx[3 * tri + k]);
-        const uint32_t uv = __ldg(&sc.verts[6ull * vi + 4]);
+        const uint32_t uv =
+            sc.tri_verts ? __ldg((const uint32_t*)(sc.tri_verts + 5ull * tri) + 6 * k + 4)
+                         : __ldg(&sc.verts[6ull * (g.first_vertex + __ldg(&sc.idx[3 * tri + k])) + 4]);
         uvx[k] = __half2float(__ushort_as_half((unsigned short)(uv & 0xFFFFu)));
         uvy[k] = __half2float(__ushort_as_half((unsigned short)(uv >> 16)));
     }
@@ -500,8 +502,9 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
             s.ngroup = make_uint2(0u, 0u);
         }
         bool done_any = false;
-        // only groups followed by node work are postponed (a group popped back is tested)
-        const bool may_postpone = WARP && s.ngroup.y > 0x00FFFFFFu;
+        // only groups followed by node work are postponed (a group popped back is tested), and
+        // never those of a first-hit query, which any of its triangles may end
+        const bool may_postpone = WARP && !ANY && s.ngroup.y > 0x00FFFFFFu;
         while (s.tgroup.y != 0u) {
             if (may_postpone && s.sp < kStackSize && __popc(__activemask()) < postpone_lanes) {
                 st(s.sp++) = s.tgroup;

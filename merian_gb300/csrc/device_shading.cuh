@@ -13,6 +13,7 @@ inline DevScene make_dev_scene(const SceneGPU& s) {
     d.tris = (const float4*)s.tris;
     d.verts = (const uint32_t*)s.verts;
     d.idx = (const uint32_t*)s.idx;
+    d.tri_verts = (const uint4*)s.tri_verts;
     d.geoms = (const GeomGPU*)s.geoms;
     d.mats = (const float4*)s.mats;
     d.geom_count = s.geom_count;
@@ -140,14 +141,23 @@ GBPT_DI SPd surface_sp(const DevScene& sc, float3 o, float3 d, uint32_t geom, ui
     const GeomGPU g = sc.geoms[geom];
     if (g.flags & GBPT_MESH_USE_ENV_MAP) return env_sp(sc, o, d);
     const uint32_t tri = g.first_triangle + prim;
-    const uint32_t i0 = g.first_vertex + __ldg(&sc.idx[3 * tri + 0]);
-    const uint32_t i1 = g.first_vertex + __ldg(&sc.idx[3 * tri + 1]);
-    const uint32_t i2 = g.first_vertex + __ldg(&sc.idx[3 * tri + 2]);
     float3 p0, p1, p2;
     uint32_t n0, n1, n2, uv0, uv1, uv2, t0, t1, t2;
-    load_vertex(sc, i0, p0, n0, uv0, t0);
-    load_vertex(sc, i1, p1, n1, uv1, t1);
-    load_vertex(sc, i2, p2, n2, uv2, t2);
+    if (sc.tri_verts) { // the triangle's record: no index fetch before the vertex loads
+        const uint4* r = sc.tri_verts + 5ull * tri;
+        const uint4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), e = __ldg(r + 3),
+                    f = __ldg(r + 4);
+        p0 = f3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z));
+        n0 = a.w, uv0 = b.x, t0 = b.y;
+        p1 = f3(__uint_as_float(b.z), __uint_as_float(b.w), __uint_as_float(c.x));
+        n1 = c.y, uv1 = c.z, t1 = c.w;
+        p2 = f3(__uint_as_float(e.x), __uint_as_float(e.y), __uint_as_float(e.z));
+        n2 = e.w, uv2 = f.x, t2 = f.y;
+    } else {
+        load_vertex(sc, g.first_vertex + __ldg(&sc.idx[3 * tri + 0]), p0, n0, uv0, t0);
+        load_vertex(sc, g.first_vertex + __ldg(&sc.idx[3 * tri + 1]), p1, n1, uv1, t1);
+        load_vertex(sc, g.first_vertex + __ldg(&sc.idx[3 * tri + 2]), p2, n2, uv2, t2);
+    }
     const float b0 = 1.0f - bu - bv, b1 = bu, b2 = bv;
     const bool xf = inst != kNoInst;
     float4 x0, x1, x2, w0r, w1r, w2r;

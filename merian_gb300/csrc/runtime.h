@@ -18,6 +18,10 @@ struct SceneGPU {
     void* tris = nullptr;       // 48 B per triangle record
     void* verts = nullptr;      // gbpt_packed_vertex
     void* idx = nullptr;        // uint32 x 3 per triangle
+    // the three vertices of each triangle in one 80-byte record (20 words: vertex k at word 6k,
+    // 8 bytes of padding), by triangle index; null when geometries that share a triangle range
+    // disagree on its first vertex
+    void* tri_verts = nullptr;
     void* geoms = nullptr;      // GeomGPU
     void* geom_key = nullptr;   // uint8 material-sort key per geometry
     void* mats = nullptr;       // gbpt_material

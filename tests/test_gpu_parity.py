@@ -261,6 +261,42 @@ def test_render_deterministic_and_subset_consistent(gpu_ctx, cornell):
     assert np.array_equal(c.view(np.uint32), a[pix].view(np.uint32))
 
 
+def test_triangle_records_and_index_path_agree(gpu_ctx, cornell):
+    """Shading reads a triangle's vertices from its 80-byte record when every triangle has one
+    first vertex, and through the index buffer when two geometries over one triangle range
+    disagree on it. The Cornell box plus a geometry that is never hit (instance mask 0) over the
+    range of a diffuse one with its first vertex moved by one takes the index path and renders the
+    same bits."""
+    import dataclasses
+    from merian_gb300 import scene as S
+    sc, sid, osc, cam = cornell
+    geo = sc.geometries
+    mats = sc.materials
+    # a diffuse, non-emissive geometry whose indices stay in range when moved by one vertex
+    g0 = next(g for g in range(len(geo))
+              if mats[geo[g]["material_id"]]["model"] == 0
+              and not np.any(mats[geo[g]["material_id"]]["emission"])
+              and (geo[g]["first_vertex"] + sc.indices[geo[g]["first_triangle"]:
+                   geo[g]["first_triangle"] + geo[g]["triangle_count"]].max() + 1)
+              < len(sc.vertices))
+    extra = geo[g0:g0 + 1].copy()
+    extra["first_vertex"] += 1
+    extra["instance_mask"] = 0
+    sc2 = dataclasses.replace(sc, geometries=np.concatenate([geo, extra]))
+    sid2 = gpu_ctx.upload(sc2)
+    try:
+        b1, b2 = gpu_ctx.scene_stats(sid)["bytes"], gpu_ctx.scene_stats(sid2)["bytes"]
+        # the first scene holds the records (80 B per triangle), the second does not (its tree
+        # is larger by the extra geometry's 128 triangles, far less than the records)
+        assert b1 - b2 > 40 * sc.triangle_count, (b1, b2)
+        p, _ = S.render_params(256, 256, 8, 6, nee=True, rr_depth=3, frame=11)
+        a = gpu_ctx.render(sid, cam, p)
+        b = gpu_ctx.render(sid2, cam, p)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    finally:
+        gpu_ctx.destroy_scene(sid2)
+
+
 def test_render_first_bounce_tracks_fp32_oracle(gpu_ctx, cornell):
     """Same RNG stream and same primary hit: with one bounce (path length 2) the GPU and the FP32
     oracle agree per pixel to float round-off of the BSDF sampling."""
