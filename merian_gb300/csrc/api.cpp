@@ -565,7 +565,29 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
         return code;
     };
     if ((rc = upload(&s.nodes, bvh.nodes.data(), bvh.nodes.size() * sizeof(CwNode), bytes))) return fail(rc);
+#if GBPT_TRI_AXIS_COPIES
+    {
+        // three copies of each record, coordinates in the order (c + 1, c + 2, c) mod 3 for
+        // dominant ray axis c (the traversal's watertight test reads copy kz)
+        std::vector<TriRecord> rec(3 * bvh.tris.size());
+        for (size_t i = 0; i < bvh.tris.size(); ++i) {
+            const TriRecord& r = bvh.tris[i];
+            for (int c = 0; c < 3; ++c) {
+                TriRecord& o = rec[3 * i + c];
+                o = r;
+                for (int a = 0; a < 3; ++a) {
+                    const int src = (c + 1 + a) % 3;
+                    o.v0[a] = r.v0[src];
+                    o.v1[a] = r.v1[src];
+                    o.v2[a] = r.v2[src];
+                }
+            }
+        }
+        if ((rc = upload(&s.tris, rec.data(), rec.size() * sizeof(TriRecord), bytes))) return fail(rc);
+    }
+#else
     if ((rc = upload(&s.tris, bvh.tris.data(), bvh.tris.size() * sizeof(TriRecord), bytes))) return fail(rc);
+#endif
     if ((rc = upload(&s.verts, d->vertices, d->vertex_count * sizeof(gbpt_packed_vertex), bytes))) return fail(rc);
     if ((rc = upload(&s.idx, d->indices, d->triangle_count * 3 * sizeof(uint32_t), bytes))) return fail(rc);
 #if GBPT_SHADE_TRI_RECORDS

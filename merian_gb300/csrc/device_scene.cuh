@@ -12,6 +12,7 @@
 
 #include <type_traits>
 #include "gbpt.h"
+#include "runtime.h"
 
 namespace gbpt {
 
@@ -126,7 +127,7 @@ GBPT_DI bool alpha_discard(const DevScene& sc, uint32_t geom, uint32_t prim, flo
 // Explicit round-to-nearest intrinsics (no FMA contraction) so the float result equals the
 // host oracle's bit for bit.
 struct RayPre {
-    uint32_t k; // the axes kx, ky, kz in bits 0-1, 2-3, 4-5 (one register for the three)
+    uint32_t k; // the axes kx, ky, kz in bits 0-1, 2-3, 4-5; bit 6 when kx, ky were swapped
     float Sx, Sy, Sz;
     float ox, oy, oz; // origin permuted to (kx, ky, kz)
     GBPT_DI int kx() const { return (int)(k & 3u); }
@@ -146,7 +147,7 @@ GBPT_DI RayPre ray_pre(float3 o, float3 d) {
         kx = ky;
         ky = t;
     }
-    p.k = (uint32_t)kx | ((uint32_t)ky << 2) | ((uint32_t)kz << 4);
+    p.k = (uint32_t)kx | ((uint32_t)ky << 2) | ((uint32_t)kz << 4) | (dkz < 0.0f ? 64u : 0u);
     p.Sx = __fdiv_rn(pick(d.x, d.y, d.z, kx), dkz);
     p.Sy = __fdiv_rn(pick(d.x, d.y, d.z, ky), dkz);
     p.Sz = __fdiv_rn(1.0f, dkz);
@@ -159,6 +160,19 @@ GBPT_DI RayPre ray_pre(float3 o, float3 d) {
 // Returns true with t, u, v when hit within [tmin, tmax] on an accepted face.
 GBPT_DI bool intersect_tri(const RayPre& p, float4 a4, float4 b4, float4 c4, uint32_t tflags,
                            float tmin, float tmax, float& t_out, float& u_out, float& v_out) {
+#if GBPT_TRI_AXIS_COPIES
+    // the record copy of axis kz holds (kz + 1, kz + 2, kz); kx = kz + 2 when they are swapped
+    const bool sw = (p.k & 64u) != 0u;
+    const float Akx = __fsub_rn(sw ? a4.y : a4.x, p.ox);
+    const float Aky = __fsub_rn(sw ? a4.x : a4.y, p.oy);
+    const float Akz = __fsub_rn(a4.z, p.oz);
+    const float Bkx = __fsub_rn(sw ? b4.y : b4.x, p.ox);
+    const float Bky = __fsub_rn(sw ? b4.x : b4.y, p.oy);
+    const float Bkz = __fsub_rn(b4.z, p.oz);
+    const float Ckx = __fsub_rn(sw ? c4.y : c4.x, p.ox);
+    const float Cky = __fsub_rn(sw ? c4.x : c4.y, p.oy);
+    const float Ckz = __fsub_rn(c4.z, p.oz);
+#else
     const int kx = p.kx(), ky = p.ky(), kz = p.kz();
     const float Akx = __fsub_rn(pick(a4.x, a4.y, a4.z, kx), p.ox);
     const float Aky = __fsub_rn(pick(a4.x, a4.y, a4.z, ky), p.oy);
@@ -169,6 +183,7 @@ GBPT_DI bool intersect_tri(const RayPre& p, float4 a4, float4 b4, float4 c4, uin
     const float Ckx = __fsub_rn(pick(c4.x, c4.y, c4.z, kx), p.ox);
     const float Cky = __fsub_rn(pick(c4.x, c4.y, c4.z, ky), p.oy);
     const float Ckz = __fsub_rn(pick(c4.x, c4.y, c4.z, kz), p.oz);
+#endif
     const float Ax = __fsub_rn(Akx, __fmul_rn(p.Sx, Akz));
     const float Ay = __fsub_rn(Aky, __fmul_rn(p.Sy, Akz));
     const float Bx = __fsub_rn(Bkx, __fmul_rn(p.Sx, Bkz));
@@ -516,7 +531,7 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
             const uint32_t ti = s.tgroup.x + b;
             if (TWO_LEVEL && s.insts != nullptr && s.inst == kNoInst) {
                 // a top-level leaf: an instance (record: instance index, mask in the flag word)
-                const uint32_t fl = __float_as_uint(__ldg(&s.tris[3 * ti + 2]).w);
+                const uint32_t fl = __float_as_uint(__ldg(&s.tris[3 * kTriCopies * ti + 2]).w);
                 if (((fl & 0xFFu) & s.mask) == 0u) continue;
                 if (s.sp + 2 > kStackSize) {
                     atomicOr(err, 1u);
@@ -526,12 +541,13 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
                 if (s.ngroup.y > 0x00FFFFFFu) st(s.sp++) = s.ngroup;
                 if (s.tgroup.y != 0u) st(s.sp++) = s.tgroup;
                 s.tgroup.y = 0u;
-                enter_instance(s, __float_as_uint(__ldg(&s.tris[3 * ti]).w));
+                enter_instance(s, __float_as_uint(__ldg(&s.tris[3 * kTriCopies * ti]).w));
                 break;
             }
-            const float4 r0 = __ldg(&s.tris[3 * ti + 0]);
-            const float4 r1 = __ldg(&s.tris[3 * ti + 1]);
-            const float4 r2 = __ldg(&s.tris[3 * ti + 2]);
+            const float4* rec = s.tris + 3 * (kTriCopies * ti + (kTriCopies > 1 ? s.pre.kz() : 0));
+            const float4 r0 = __ldg(rec + 0);
+            const float4 r1 = __ldg(rec + 1);
+            const float4 r2 = __ldg(rec + 2);
             const uint32_t tfl = __float_as_uint(r2.w);
             if (((tfl & 0xFFu) & s.mask) == 0u) continue;
             if (COUNT) {
