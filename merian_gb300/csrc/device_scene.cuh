@@ -127,7 +127,11 @@ GBPT_DI bool alpha_discard(const DevScene& sc, uint32_t geom, uint32_t prim, flo
 // Explicit round-to-nearest intrinsics (no FMA contraction) so the float result equals the
 // host oracle's bit for bit.
 struct RayPre {
-    uint32_t k; // the axes kx, ky, kz in bits 0-1, 2-3, 4-5; bit 6 when kx, ky were swapped
+    // the axes kx, ky, kz in bits 0-1, 2-3, 4-5 (kx = kz + 1, ky = kz + 2 mod 3); bit 6 when the
+    // direction is negative along kz. The watertight test's paper swaps kx and ky for that sign
+    // to keep the winding; keeping one frame per kz negates U, V, W, det and T instead, which
+    // leaves t, u and v unchanged and flips the facing.
+    uint32_t k;
     float Sx, Sy, Sz;
     float ox, oy, oz; // origin permuted to (kx, ky, kz)
     GBPT_DI int kx() const { return (int)(k & 3u); }
@@ -139,14 +143,9 @@ GBPT_DI RayPre ray_pre(float3 o, float3 d) {
     RayPre p;
     const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
     const int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
-    int kx = kz == 2 ? 0 : kz + 1;
-    int ky = kx == 2 ? 0 : kx + 1;
+    const int kx = kz == 2 ? 0 : kz + 1;
+    const int ky = kx == 2 ? 0 : kx + 1;
     const float dkz = pick(d.x, d.y, d.z, kz);
-    if (dkz < 0.0f) {
-        const int t = kx;
-        kx = ky;
-        ky = t;
-    }
     p.k = (uint32_t)kx | ((uint32_t)ky << 2) | ((uint32_t)kz << 4) | (dkz < 0.0f ? 64u : 0u);
     p.Sx = __fdiv_rn(pick(d.x, d.y, d.z, kx), dkz);
     p.Sy = __fdiv_rn(pick(d.x, d.y, d.z, ky), dkz);
@@ -161,16 +160,15 @@ GBPT_DI RayPre ray_pre(float3 o, float3 d) {
 GBPT_DI bool intersect_tri(const RayPre& p, float4 a4, float4 b4, float4 c4, uint32_t tflags,
                            float tmin, float tmax, float& t_out, float& u_out, float& v_out) {
 #if GBPT_TRI_AXIS_COPIES
-    // the record copy of axis kz holds (kz + 1, kz + 2, kz); kx = kz + 2 when they are swapped
-    const bool sw = (p.k & 64u) != 0u;
-    const float Akx = __fsub_rn(sw ? a4.y : a4.x, p.ox);
-    const float Aky = __fsub_rn(sw ? a4.x : a4.y, p.oy);
+    // the record copy of axis kz holds the coordinates (kx, ky, kz)
+    const float Akx = __fsub_rn(a4.x, p.ox);
+    const float Aky = __fsub_rn(a4.y, p.oy);
     const float Akz = __fsub_rn(a4.z, p.oz);
-    const float Bkx = __fsub_rn(sw ? b4.y : b4.x, p.ox);
-    const float Bky = __fsub_rn(sw ? b4.x : b4.y, p.oy);
+    const float Bkx = __fsub_rn(b4.x, p.ox);
+    const float Bky = __fsub_rn(b4.y, p.oy);
     const float Bkz = __fsub_rn(b4.z, p.oz);
-    const float Ckx = __fsub_rn(sw ? c4.y : c4.x, p.ox);
-    const float Cky = __fsub_rn(sw ? c4.x : c4.y, p.oy);
+    const float Ckx = __fsub_rn(c4.x, p.ox);
+    const float Cky = __fsub_rn(c4.y, p.oy);
     const float Ckz = __fsub_rn(c4.z, p.oz);
 #else
     const int kx = p.kx(), ky = p.ky(), kz = p.kz();
@@ -202,7 +200,7 @@ GBPT_DI bool intersect_tri(const RayPre& p, float4 a4, float4 b4, float4 c4, uin
     const float det = __fadd_rn(__fadd_rn(U, V), W);
     if (det == 0.0f) return false;
     if (!(tflags & kTriTwoSided)) {
-        const bool front = det > 0.0f;
+        const bool front = (det > 0.0f) != ((p.k & 64u) != 0u);
         if (front == ((tflags & kTriFlip) != 0)) return false;
     }
     const float Az = __fmul_rn(p.Sz, Akz);

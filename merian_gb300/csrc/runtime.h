@@ -12,17 +12,16 @@ namespace gbpt {
 
 struct DevScene; // device_scene.cuh
 
-// A scene resident in HBM. All pointers are device pointers owned by the context.
 // GBPT_TRI_AXIS_COPIES: each traversal triangle record is stored three times, its vertices'
 // coordinates permuted for each dominant ray axis kz to (kz + 1, kz + 2, kz) mod 3, so the
-// watertight test reads the ray's permutation from memory instead of selecting 9 coordinates at
-// run time; a ray whose direction along kz is negative swaps the first two (the only selects
-// left). Copy c of record i is record 3 i + c of the uploaded array.
+// watertight test reads the ray's frame from memory instead of selecting 9 coordinates at run
+// time. Copy c of record i is record 3 i + c of the uploaded array.
 #ifndef GBPT_TRI_AXIS_COPIES
 #define GBPT_TRI_AXIS_COPIES 1
 #endif
 constexpr int kTriCopies = GBPT_TRI_AXIS_COPIES ? 3 : 1;
 
+// A scene resident in HBM. All pointers are device pointers owned by the context.
 struct SceneGPU {
     void* nodes = nullptr;      // CWBVH, 80 B per node
     void* tris = nullptr;       // 48 B per triangle record and copy (kTriCopies)

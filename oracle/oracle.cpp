@@ -196,6 +196,7 @@ static void build_bvh(TriSet& s) {
 // MeshFlags, scene.hpp:39-58, mapped to the TLAS instance flags at scene.cpp:1841-1848).
 template <class R> struct RayPre {
     int kx, ky, kz;
+    bool flip; // direction negative along kz: the 2D frame (kx, ky) sees triangles mirrored
     R Sx, Sy, Sz;
     V3<R> o;
 };
@@ -206,7 +207,9 @@ template <class R> inline RayPre<R> ray_pre(const Ray<R>& r) {
     p.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
     p.kx = (p.kz + 1) % 3;
     p.ky = (p.kx + 1) % 3;
-    if (comp(r.d, p.kz) < R(0)) std::swap(p.kx, p.ky);
+    // the paper swaps kx and ky here to keep the winding; the same frame for both signs negates
+    // U, V, W, det and T instead, so t, u and v are unchanged and only the facing flips
+    p.flip = comp(r.d, p.kz) < R(0);
     p.Sx = comp(r.d, p.kx) / comp(r.d, p.kz);
     p.Sy = comp(r.d, p.ky) / comp(r.d, p.kz);
     p.Sz = R(1) / comp(r.d, p.kz);
@@ -245,7 +248,7 @@ inline bool intersect(const RayPre<R>& p, const float* tv, uint32_t flags, R tmi
     if ((U < R(0) || V < R(0) || W < R(0)) && (U > R(0) || V > R(0) || W > R(0))) return false;
     const R det = U + V + W;
     if (det == R(0)) return false;
-    const bool front = det > R(0);
+    const bool front = (det > R(0)) != p.flip;
     if (!(flags & GBPT_MESH_TWO_SIDED)) {
         const bool want_front = !(flags & GBPT_MESH_FLIP_FACING);
         if (front != want_front) return false;
