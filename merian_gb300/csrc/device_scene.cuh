@@ -157,8 +157,14 @@ GBPT_DI RayPre ray_pre(float3 o, float3 d) {
 }
 
 // Returns true with t, u, v when hit within [tmin, tmax] on an accepted face.
+// With GBPT_DEFER_UV the barycentrics are returned undivided (u_out = V, v_out = W, det_out =
+// det): the caller divides them once for the final hit instead of at every accepted candidate.
+#ifndef GBPT_DEFER_UV
+#define GBPT_DEFER_UV 1
+#endif
 GBPT_DI bool intersect_tri(const RayPre& p, float4 a4, float4 b4, float4 c4, uint32_t tflags,
-                           float tmin, float tmax, float& t_out, float& u_out, float& v_out) {
+                           float tmin, float tmax, float& t_out, float& u_out, float& v_out,
+                           float& det_out) {
 #if GBPT_TRI_AXIS_COPIES
     // the record copy of axis kz holds the coordinates (kx, ky, kz)
     const float Akx = __fsub_rn(a4.x, p.ox);
@@ -210,8 +216,15 @@ GBPT_DI bool intersect_tri(const RayPre& p, float4 a4, float4 b4, float4 c4, uin
     const float t = __fdiv_rn(T, det);
     if (!(t >= tmin && t <= tmax)) return false;
     t_out = t;
+#if GBPT_DEFER_UV
+    u_out = V;
+    v_out = W;
+    det_out = det;
+#else
     u_out = __fdiv_rn(V, det);
     v_out = __fdiv_rn(W, det);
+    det_out = 1.0f;
+#endif
     return true;
 }
 
@@ -287,6 +300,7 @@ struct TraceState {
     uint2 ngroup, tgroup;
     int sp;
     Hit best;          // a hit was found once best.geom != kNoInst
+    float det;         // GBPT_DEFER_UV: best.u, best.v are V, W of the test until divided by it
     float3 wo, wd; // the world ray
     uint32_t inst; // instance being traversed, kNoInst at the top level
     int inst_sp;   // stack depth at which it was entered
@@ -553,12 +567,19 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
                 count_step(ctr->tri_steps, ctr->tri_lanes);
             }
             float t, u, v;
-            if (!intersect_tri(s.pre, r0, r1, r2, tfl, s.tmin, s.best.t, t, u, v)) continue;
+            float det;
+            if (!intersect_tri(s.pre, r0, r1, r2, tfl, s.tmin, s.best.t, t, u, v, det)) continue;
             const uint32_t prim = __float_as_uint(r0.w), geom = __float_as_uint(r1.w);
             if (t < s.best.t || geom < s.best.geom ||
                 (geom == s.best.geom &&
                  (prim < s.best.prim || (prim == s.best.prim && s.inst < s.best.inst)))) {
+#if GBPT_DEFER_UV
+                if ((tfl & kTriAlpha) && alpha(geom, prim, __fdiv_rn(u, det), __fdiv_rn(v, det)))
+                    continue;
+                s.det = det;
+#else
                 if ((tfl & kTriAlpha) && alpha(geom, prim, u, v)) continue;
+#endif
                 s.best.t = t;
                 s.best.u = u;
                 s.best.v = v;
@@ -580,6 +601,12 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
         if (done) break;
         if (WARP && !pool_empty && __popc(__activemask()) < refill_lanes) return false;
     }
+#if GBPT_DEFER_UV
+    if (s.best.geom != kNoInst) {
+        s.best.u = __fdiv_rn(s.best.u, s.det);
+        s.best.v = __fdiv_rn(s.best.v, s.det);
+    }
+#endif
     return true;
 }
 
