@@ -149,7 +149,7 @@ GBPT_DI RayPre ray_pre(float3 o, float3 d) {
     p.k = (uint32_t)kx | ((uint32_t)ky << 2) | ((uint32_t)kz << 4) | (dkz < 0.0f ? 64u : 0u);
     p.Sx = __fdiv_rn(pick(d.x, d.y, d.z, kx), dkz);
     p.Sy = __fdiv_rn(pick(d.x, d.y, d.z, ky), dkz);
-    p.Sz = __fdiv_rn(1.0f, dkz);
+    p.Sz = __frcp_rn(dkz);
     p.ox = pick(o.x, o.y, o.z, kx);
     p.oy = pick(o.x, o.y, o.z, ky);
     p.oz = pick(o.x, o.y, o.z, kz);
@@ -257,7 +257,7 @@ GBPT_DI void count_step(uint32_t& steps, uint32_t& lanes) {
 
 GBPT_DI float safe_rcp(float d) {
     const float m = 1e-20f;
-    return __fdiv_rn(1.0f, fabsf(d) > m ? d : copysignf(m, d));
+    return __frcp_rn(fabsf(d) > m ? d : copysignf(m, d));
 }
 
 // Instance records of two-level scenes, 7 float4 each: object-to-world rows (0..2), world-to-
