@@ -567,13 +567,13 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
     if ((rc = upload(&s.nodes, bvh.nodes.data(), bvh.nodes.size() * sizeof(CwNode), bytes))) return fail(rc);
 #if GBPT_TRI_AXIS_COPIES
     {
-        // three copies of each record, coordinates in the order (c + 1, c + 2, c) mod 3 for
-        // dominant ray axis c (the traversal's watertight test reads copy kz)
+        // three copies of the records, one after the other, coordinates in the order
+        // (c + 1, c + 2, c) mod 3 in copy c (the traversal's watertight test reads copy kz)
         std::vector<TriRecord> rec(3 * bvh.tris.size());
         for (size_t i = 0; i < bvh.tris.size(); ++i) {
             const TriRecord& r = bvh.tris[i];
             for (int c = 0; c < 3; ++c) {
-                TriRecord& o = rec[3 * i + c];
+                TriRecord& o = rec[c * bvh.tris.size() + i];
                 o = r;
                 for (int a = 0; a < 3; ++a) {
                     const int src = (c + 1 + a) % 3;

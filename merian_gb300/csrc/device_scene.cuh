@@ -27,7 +27,8 @@ constexpr uint32_t kTriAlpha = 1u << 10; // non-opaque geometry: candidate hits 
 
 struct DevScene {
     const uint4* __restrict__ nodes;  // 5 per CWBVH node
-    const float4* __restrict__ tris;  // 3 per triangle record
+    const float4* __restrict__ tris;  // 3 per triangle record and copy
+    uint32_t tri_stride;              // float4 from one copy of the records to the next
     const uint32_t* __restrict__ verts; // gbpt_packed_vertex as 6 words
     const uint32_t* __restrict__ idx;
     const uint4* __restrict__ tri_verts; // 5 per triangle (3 vertices, padded) or null
@@ -290,7 +291,9 @@ GBPT_DI float3 xform_vector(float4 r0, float4 r1, float4 r2, float3 v) {
 
 struct TraceState {
     const uint4* nodes;  // the ray's scene (rays of one launch may belong to different scenes)
-    const float4* tris;
+    const float4* tris;  // the records (copy-major layout: the current ray's copy)
+    const float4* tris_base; // copy 0 of the records and the float4 from one copy to the next
+    uint32_t tri_stride;
     const float4* insts; // instance records; nullptr for single-level scenes
     uint32_t mask;       // instance mask of the ray
     float3 o, d, inv;    // the ray in the current space (object space inside an instance)
@@ -314,6 +317,7 @@ GBPT_DI void set_ray(TraceState& s, float3 o, float3 d) {
                          ((__float_as_uint(d.z) >> 31) << 2);
     s.oct_inv = 7u - oct;
     s.pre = ray_pre(o, d);
+    s.tris = kTriCopies > 1 ? s.tris_base + (size_t)s.pre.kz() * s.tri_stride : s.tris_base;
 }
 
 GBPT_DI void trace_init(TraceState& s, float3 o, float3 d, float tmin, float tmax) {
@@ -543,7 +547,7 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
             const uint32_t ti = s.tgroup.x + b;
             if (TWO_LEVEL && s.insts != nullptr && s.inst == kNoInst) {
                 // a top-level leaf: an instance (record: instance index, mask in the flag word)
-                const uint32_t fl = __float_as_uint(__ldg(&s.tris[3 * kTriCopies * ti + 2]).w);
+                const uint32_t fl = __float_as_uint(__ldg(&s.tris[3 * ti + 2]).w);
                 if (((fl & 0xFFu) & s.mask) == 0u) continue;
                 if (s.sp + 2 > kStackSize) {
                     atomicOr(err, 1u);
@@ -553,10 +557,10 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
                 if (s.ngroup.y > 0x00FFFFFFu) st(s.sp++) = s.ngroup;
                 if (s.tgroup.y != 0u) st(s.sp++) = s.tgroup;
                 s.tgroup.y = 0u;
-                enter_instance(s, __float_as_uint(__ldg(&s.tris[3 * kTriCopies * ti]).w));
+                enter_instance(s, __float_as_uint(__ldg(&s.tris[3 * ti]).w));
                 break;
             }
-            const float4* rec = s.tris + 3 * (kTriCopies * ti + (kTriCopies > 1 ? s.pre.kz() : 0));
+            const float4* rec = s.tris + 3 * ti;
             const float4 r0 = __ldg(rec + 0);
             const float4 r1 = __ldg(rec + 1);
             const float4 r2 = __ldg(rec + 2);
@@ -619,7 +623,8 @@ __device__ __forceinline__ Hit trace_ray(const DevScene& sc, float3 o, float3 d,
                                          uint32_t* err) {
     TraceState s;
     s.nodes = sc.nodes;
-    s.tris = sc.tris;
+    s.tris_base = sc.tris;
+    s.tri_stride = sc.tri_stride;
     s.insts = sc.n_inst ? sc.inst : nullptr;
     s.mask = ray_mask;
     trace_init(s, o, d, tmin, tmax);

@@ -11,6 +11,7 @@ inline DevScene make_dev_scene(const SceneGPU& s) {
     DevScene d{};
     d.nodes = (const uint4*)s.nodes;
     d.tris = (const float4*)s.tris;
+    d.tri_stride = (uint32_t)(3u * s.n_tris);
     d.verts = (const uint32_t*)s.verts;
     d.idx = (const uint32_t*)s.idx;
     d.tri_verts = (const uint4*)s.tri_verts;

@@ -42,7 +42,8 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
     auto load = [&](uint32_t i, TraceState& s) {
         const gbpt_ray r = rays[i];
         s.nodes = sc.nodes;
-        s.tris = sc.tris;
+        s.tris_base = sc.tris;
+        s.tri_stride = sc.tri_stride;
         s.insts = sc.n_inst ? sc.inst : nullptr;
         s.mask = mask;
         trace_init(s, f3(r.origin[0], r.origin[1], r.origin[2]),

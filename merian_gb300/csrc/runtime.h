@@ -15,7 +15,8 @@ struct DevScene; // device_scene.cuh
 // GBPT_TRI_AXIS_COPIES: each traversal triangle record is stored three times, its vertices'
 // coordinates permuted for each dominant ray axis kz to (kz + 1, kz + 2, kz) mod 3, so the
 // watertight test reads the ray's frame from memory instead of selecting 9 coordinates at run
-// time. Copy c of record i is record 3 i + c of the uploaded array.
+// time. Copy c of record i is record c n + i of the uploaded array (n records), so a ray reads
+// one contiguous copy. 0: one copy, coordinates selected at run time.
 #ifndef GBPT_TRI_AXIS_COPIES
 #define GBPT_TRI_AXIS_COPIES 1
 #endif

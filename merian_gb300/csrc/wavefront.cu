@@ -72,8 +72,10 @@ struct ChunkGPU {
     const float4* tris;
     const float4* insts; // instance records of a two-level scene, else nullptr
     const uint8_t* geom_key; // material-sort key of each geometry of the scene
+    uint32_t tri_stride;     // float4 from one copy of the triangle records to the next
+    uint32_t pad2;
 };
-static_assert(sizeof(ChunkGPU) == 64, "chunk layout");
+static_assert(sizeof(ChunkGPU) == 72, "chunk layout");
 
 struct TickHeader {
     uint32_t n_chunks, n_pix, n_paths, pad;
@@ -313,7 +315,8 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
         const float4 a = q[2 * i + 0];
         const float4 b = q[2 * i + 1];
         s.nodes = c.nodes;
-        s.tris = c.tris;
+        s.tris_base = c.tris;
+        s.tri_stride = c.tri_stride;
         s.insts = c.insts;
         s.mask = c.mask;
         trace_init(s, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w, b.w);
@@ -506,7 +509,8 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM) k_shadow(TickArgs t) {
         const float4 a = t.w.s_od[2 * i + 0];
         const float4 b = t.w.s_od[2 * i + 1];
         s.nodes = c.nodes;
-        s.tris = c.tris;
+        s.tris_base = c.tris;
+        s.tri_stride = c.tri_stride;
         s.insts = c.insts;
         s.mask = c.mask;
         trace_init(s, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), 0.0f, a.w);
@@ -988,6 +992,7 @@ int tick_enqueue(TickEngine& e, TickItem* const* items, uint32_t n_items, uint64
         c.mask = reqs[ri].mask;
         c.nodes = scenes[si].nodes;
         c.tris = scenes[si].tris;
+        c.tri_stride = scenes[si].tri_stride;
         c.insts = scenes[si].n_inst ? scenes[si].inst : nullptr;
         c.geom_key = (const uint8_t*)it.scene->geom_key;
         tp.two_level |= scenes[si].n_inst != 0u;
@@ -1169,6 +1174,7 @@ int primary_points(const SceneGPU& scene, Work& w, const RenderArgs& args, cudaS
     c.mask = r.mask;
     c.nodes = s.nodes;
     c.tris = s.tris;
+    c.tri_stride = s.tri_stride;
     const TickHeader hdr{1u, P, P, 0u};
     cudaMemcpyAsync(d_reqs, &r, sizeof(r), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(d_scenes, &s, sizeof(s), cudaMemcpyHostToDevice, st);
