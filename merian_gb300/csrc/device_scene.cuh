@@ -110,9 +110,10 @@ GBPT_DI bool alpha_discard(const DevScene& sc, uint32_t geom, uint32_t prim, flo
     float uvx[3], uvy[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const uint32_t uv =
-            sc.tri_verts ? __ldg((const uint32_t*)(sc.tri_verts + 5ull * tri) + 6 * k + 4)
-                         : __ldg(&sc.verts[6ull * (g.first_vertex + __ldg(&sc.idx[3 * tri + k])) + 4]);
+        const uint32_t* v =
+            sc.tri_verts ? (const uint32_t*)(sc.tri_verts + 5ull * tri) + 6 * k
+                         : sc.verts + 6ull * (g.first_vertex + __ldg(&sc.idx[3 * tri + k]));
+        const uint32_t uv = __ldg(v + 4);
         uvx[k] = __half2float(__ushort_as_half((unsigned short)(uv & 0xFFFFu)));
         uvy[k] = __half2float(__ushort_as_half((unsigned short)(uv >> 16)));
     }
@@ -398,7 +399,7 @@ template <int J> GBPT_DI float2 plane_t2(uint32_t w, uint64_t a2, uint64_t o2) {
 // The quantised planes are dequantised with a per-axis slack of 2^-20 of the plane distance
 // magnitude (plus 2^-8 of a quantisation step for the biased planes), so rounding never loses a
 // child the exact box would keep.
-template <bool COUNT>
+template <bool COUNT, bool PAIRED = GBPT_BOX_FMA2 != 0>
 GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& child_base,
                                 uint32_t& tri_base, uint32_t& imask, TraceCounters* ctr) {
     if (COUNT) ctr->nodes++;
@@ -432,11 +433,7 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
     imask = n0.w >> 24;
     child_base = n1.x;
     tri_base = n1.y;
-#if GBPT_BOX_FMA2
-    const uint64_t ax2 = pack2(aix, aix), ay2 = pack2(aiy, aiy), az2 = pack2(aiz, aiz);
-    const uint64_t nox2 = pack2(nox, nox), noy2 = pack2(noy, noy), noz2 = pack2(noz, noz);
-    const uint64_t fox2 = pack2(fox, fox), foy2 = pack2(foy, foy), foz2 = pack2(foz, foz);
-#endif
+
     // the direction's signs from the octant (negative axis a: bit a of oct_inv clear)
     const uint32_t oct_inv4 = s.oct_inv * 0x01010101u;
     const bool negx = (s.oct_inv & 1u) == 0u, negy = (s.oct_inv & 2u) == 0u;
@@ -455,41 +452,45 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
         const uint32_t nqx = negx ? qhx : qlx, fqx = negx ? qlx : qhx;
         const uint32_t nqy = negy ? qhy : qly, fqy = negy ? qly : qhy;
         const uint32_t nqz = negz ? qhz : qlz, fqz = negz ? qlz : qhz;
-#if GBPT_BOX_FMA2
-        // children j and j + 1 of the half at once: the paired FP32 FMA rounds each lane like
-        // __fmaf_rn, so the decisions are the scalar ones
-        auto pair = [&](auto jc) {
-            constexpr int j = decltype(jc)::value;
-            const float2 tnx = plane_t2<j>(nqx, ax2, nox2), tny = plane_t2<j>(nqy, ay2, noy2);
-            const float2 tnz = plane_t2<j>(nqz, az2, noz2), tfx = plane_t2<j>(fqx, ax2, fox2);
-            const float2 tfy = plane_t2<j>(fqy, ay2, foy2), tfz = plane_t2<j>(fqz, az2, foz2);
-            const float cmin0 = fmaxf(fmaxf(tnx.x, tny.x), fmaxf(tnz.x, s.tmin));
-            const float cmax0 = fminf(fminf(tfx.x, tfy.x), fminf(tfz.x, s.best.t));
-            const float cmin1 = fmaxf(fmaxf(tnx.y, tny.y), fmaxf(tnz.y, s.tmin));
-            const float cmax1 = fminf(fminf(tfx.y, tfy.y), fminf(tfz.y, s.best.t));
-            constexpr uint32_t sh0 = 8u * j, sh1 = 8u * (j + 1);
-            if (cmin0 <= cmax0)
-                hitmask |= ((child_bits4 >> sh0) & 7u) << ((bit_index4 >> sh0) & 31u);
-            if (cmin1 <= cmax1)
-                hitmask |= ((child_bits4 >> sh1) & 7u) << ((bit_index4 >> sh1) & 31u);
-        };
-        pair(std::integral_constant<int, 0>{});
-        pair(std::integral_constant<int, 2>{});
-#else
+        if constexpr (PAIRED) {
+            // children j and j + 1 of the half at once: the paired FP32 FMA rounds each lane like
+            // __fmaf_rn, so the decisions are the scalar ones
+            const uint64_t ax2 = pack2(aix, aix), ay2 = pack2(aiy, aiy), az2 = pack2(aiz, aiz);
+            const uint64_t nox2 = pack2(nox, nox), noy2 = pack2(noy, noy), noz2 = pack2(noz, noz);
+            const uint64_t fox2 = pack2(fox, fox), foy2 = pack2(foy, foy), foz2 = pack2(foz, foz);
+            auto pair = [&](auto jc) {
+                constexpr int j = decltype(jc)::value;
+                const float2 tnx = plane_t2<j>(nqx, ax2, nox2), tny = plane_t2<j>(nqy, ay2, noy2);
+                const float2 tnz = plane_t2<j>(nqz, az2, noz2), tfx = plane_t2<j>(fqx, ax2, fox2);
+                const float2 tfy = plane_t2<j>(fqy, ay2, foy2), tfz = plane_t2<j>(fqz, az2, foz2);
+                const float cmin0 = fmaxf(fmaxf(tnx.x, tny.x), fmaxf(tnz.x, s.tmin));
+                const float cmax0 = fminf(fminf(tfx.x, tfy.x), fminf(tfz.x, s.best.t));
+                const float cmin1 = fmaxf(fmaxf(tnx.y, tny.y), fmaxf(tnz.y, s.tmin));
+                const float cmax1 = fminf(fminf(tfx.y, tfy.y), fminf(tfz.y, s.best.t));
+                constexpr uint32_t sh0 = 8u * j, sh1 = 8u * (j + 1);
+                if (cmin0 <= cmax0)
+                    hitmask |= ((child_bits4 >> sh0) & 7u) << ((bit_index4 >> sh0) & 31u);
+                if (cmin1 <= cmax1)
+                    hitmask |= ((child_bits4 >> sh1) & 7u) << ((bit_index4 >> sh1) & 31u);
+            };
+            pair(std::integral_constant<int, 0>{});
+            pair(std::integral_constant<int, 2>{});
+        } else {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t sh = 8u * j;
-            const float tnx = __fmaf_rn(qplane(nqx, j), aix, nox);
-            const float tny = __fmaf_rn(qplane(nqy, j), aiy, noy);
-            const float tnz = __fmaf_rn(qplane(nqz, j), aiz, noz);
-            const float tfx = __fmaf_rn(qplane(fqx, j), aix, fox);
-            const float tfy = __fmaf_rn(qplane(fqy, j), aiy, foy);
-            const float tfz = __fmaf_rn(qplane(fqz, j), aiz, foz);
-            const float cmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, s.tmin));
-            const float cmax = fminf(fminf(tfx, tfy), fminf(tfz, s.best.t));
-            if (cmin <= cmax) hitmask |= ((child_bits4 >> sh) & 7u) << ((bit_index4 >> sh) & 31u);
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t sh = 8u * j;
+                const float tnx = __fmaf_rn(qplane(nqx, j), aix, nox);
+                const float tny = __fmaf_rn(qplane(nqy, j), aiy, noy);
+                const float tnz = __fmaf_rn(qplane(nqz, j), aiz, noz);
+                const float tfx = __fmaf_rn(qplane(fqx, j), aix, fox);
+                const float tfy = __fmaf_rn(qplane(fqy, j), aiy, foy);
+                const float tfz = __fmaf_rn(qplane(fqz, j), aiz, foz);
+                const float cmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, s.tmin));
+                const float cmax = fminf(fminf(tfx, tfy), fminf(tfz, s.best.t));
+                if (cmin <= cmax)
+                    hitmask |= ((child_bits4 >> sh) & 7u) << ((bit_index4 >> sh) & 31u);
+            }
         }
-#endif
     }
     return hitmask;
 }
@@ -523,7 +524,10 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
             const uint32_t ni = s.ngroup.x + __popc((hits & 0xFFu) & ((1u << slot) - 1u));
             uint32_t cb, tb, im;
             if (COUNT) count_step(ctr->node_steps, ctr->node_lanes);
-            const uint32_t hm = intersect_node<COUNT>(s, ni, cb, tb, im, ctr);
+            // the paired planes hold more registers: first-hit traversal, which keeps fewer,
+            // measured faster with the scalar ones
+            const uint32_t hm =
+                intersect_node<COUNT, GBPT_BOX_FMA2 != 0 && !ANY>(s, ni, cb, tb, im, ctr);
             s.ngroup = make_uint2(cb, (hm & 0xFF000000u) | im);
             s.tgroup = make_uint2(tb, hm & 0x00FFFFFFu);
         } else {

@@ -259,8 +259,7 @@ int render_frame_static(const SceneGPU& scene, const RenderArgs& args, const uin
         ptr = (T*)p;
         p += (count * sizeof(T) + 255) & ~255ull;
     };
-    carve(w.thr, N);
-    carve(w.rad, N);
+    carve(w.path, 2 * N);
     carve(w.rng, N);
     carve(w.q_od[0], 2 * N);
     carve(w.q_od[1], 2 * N);

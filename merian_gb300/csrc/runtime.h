@@ -81,8 +81,9 @@ struct Work {
     // or freed, and a wave never exceeds path_cap
     bool fixed = false;
     // path state (SoA, indexed by wave-local path id)
-    float4* thr = nullptr;  // throughput rgb, current IOR
-    float4* rad = nullptr;  // radiance rgb, pdf of the last BSDF sample
+    // 2 float4 per path, one 32-byte sector: (throughput rgb, current IOR), (radiance rgb, pdf
+    // of the last BSDF sample)
+    float4* path = nullptr;
     uint32_t* rng = nullptr;
     // ray queues (two, ping-pong) and hits
     float4* q_od[2] = {nullptr, nullptr}; // 2 float4 per entry: (o, tmin), (d, tmax)

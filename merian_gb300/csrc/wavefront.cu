@@ -275,8 +275,8 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM)
             if (r.max_len > 1)
                 want = scatter(sc, r, 1, sp, d, thr, ior, last_pdf, rng, no, nd, want_shadow,
                                     s_o, s_d, s_c);
-            t.w.thr[p] = make_float4(thr.x, thr.y, thr.z, ior);
-            t.w.rad[p] = make_float4(rad.x, rad.y, rad.z, last_pdf);
+            t.w.path[2 * p + 0] = make_float4(thr.x, thr.y, thr.z, ior);
+            t.w.path[2 * p + 1] = make_float4(rad.x, rad.y, rad.z, last_pdf);
             t.w.rng[p] = rng.state;
         }
         const uint32_t tag = (ci << kPathBits) | p;
@@ -381,12 +381,13 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM)
             const ChunkGPU& c = t.chunks[tag >> kPathBits];
             const ReqGPU& r = t.reqs[c.req];
             const DevScene& sc = t.scenes[c.scene];
-            const float4 qa = t.w.q_od[qi][2 * i + 0];
+            // the ray's direction only: a surface point comes from the hit's vertices, and an
+            // environment point's position is never read here (it does not scatter)
             const float4 qb = t.w.q_od[qi][2 * i + 1];
-            const float3 o = f3(qa.x, qa.y, qa.z), d = f3(qb.x, qb.y, qb.z);
+            const float3 o = f3(0.f, 0.f, 0.f), d = f3(qb.x, qb.y, qb.z);
             const float4 h = t.w.hit_tuv[i];
             const uint32_t geom = t.w.hit_geom[i];
-            const float4 t4 = t.w.thr[p], r4 = t.w.rad[p];
+            const float4 t4 = t.w.path[2 * p + 0], r4 = t.w.path[2 * p + 1];
             float3 thr = f3(t4.x, t4.y, t4.z), rad = f3(r4.x, r4.y, r4.z);
             float ior = t4.w, last_pdf = r4.w;
             Pcg rng{t.w.rng[p]};
@@ -410,8 +411,8 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM)
             if (scatters)
                 want = scatter(sc, r, k, sp, d, thr, ior, last_pdf, rng, no, nd, want_shadow,
                                     s_o, s_d, s_c);
-            t.w.thr[p] = make_float4(thr.x, thr.y, thr.z, ior);
-            t.w.rad[p] = make_float4(rad.x, rad.y, rad.z, last_pdf);
+            t.w.path[2 * p + 0] = make_float4(thr.x, thr.y, thr.z, ior);
+            t.w.path[2 * p + 1] = make_float4(rad.x, rad.y, rad.z, last_pdf);
             t.w.rng[p] = rng.state;
         }
         const uint32_t q = warp_append(t.w.counters + qo, want);
@@ -519,11 +520,11 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM) k_shadow(TickArgs t) {
         if (h.geom == 0xFFFFFFFFu) {
             const uint32_t p = t.w.s_path[i] & kPathMask;
             const float4 c = t.w.s_contrib[i];
-            float4 r = t.w.rad[p];
+            float4 r = t.w.path[2 * p + 1];
             r.x += c.x;
             r.y += c.y;
             r.z += c.z;
-            t.w.rad[p] = r;
+            t.w.path[2 * p + 1] = r;
         }
     };
     auto alpha = [&](uint32_t i, uint32_t g, uint32_t p, float u, float v) {
@@ -555,7 +556,7 @@ __global__ void __launch_bounds__(128) k_finalize(TickArgs t) {
         const float ax = pc[3].w, ay = pc[4].w, az = pc[5].w;
         const bool demod = (r.flags & kReqDemodulate) != 0u;
         for (uint32_t s = lane; s < S; s += 32u) {
-            float4 v = t.w.rad[base + s];
+            float4 v = t.w.path[2 * (base + s) + 1];
             if (demod) {
                 v.x = v.x / ax;
                 v.y = v.y / ay;
@@ -646,7 +647,7 @@ void work_free(Work& w) {
         w = Work{};
         return;
     }
-    void* ptrs[] = {w.thr,     w.rad,       w.rng,    w.q_od[0], w.q_od[1],  w.q_path[0],
+    void* ptrs[] = {w.path,    w.rng,       w.q_od[0], w.q_od[1], w.q_path[0],
                     w.q_path[1], w.hit_tuv, w.hit_geom, w.s_od,  w.s_contrib, w.s_path,
                     w.pix,     w.pix_id,    w.out,    w.counters, w.stats,    w.tables,
                     w.keys,    w.perm,      w.hit_inst};
@@ -673,8 +674,7 @@ int work_reserve(Work& w, uint64_t paths, uint64_t pixels) {
     }
     if (paths > w.path_cap) {
         auto release_paths = [&w]() {
-            release(w.thr);
-            release(w.rad);
+            release(w.path);
             release(w.rng);
             release(w.q_od[0]);
             release(w.q_od[1]);
@@ -693,7 +693,7 @@ int work_reserve(Work& w, uint64_t paths, uint64_t pixels) {
         release_paths();
         new_generation(w);
         uint64_t b = 0;
-        bool ok = alloc(w.thr, paths, b) == cudaSuccess && alloc(w.rad, paths, b) == cudaSuccess &&
+        bool ok = alloc(w.path, 2 * paths, b) == cudaSuccess &&
                   alloc(w.rng, paths, b) == cudaSuccess &&
                   alloc(w.q_od[0], 2 * paths, b) == cudaSuccess &&
                   alloc(w.q_od[1], 2 * paths, b) == cudaSuccess &&
