@@ -197,10 +197,9 @@ static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBy
 namespace {
 constexpr uint64_t kStaticCounterBytes = 256; // 16 counters + 8 stats words, padded
 constexpr uint64_t kStaticPixelBytes = (uint64_t)kStaticMaxPixelList * 4;
-// per path: throughput, radiance (16 + 16), rng (4), two ray queues (2 x 36), hits (24),
-// shadow queue (52); plus a 112-byte primary point per pixel, budgeted as one pixel per path
-constexpr uint64_t kStaticBytesPerPath =
-    16 + 16 + 4 + 2 * (32 + 4) + (16 + 4 + 4) + (32 + 16 + 4) + 16 * kPixFloat4;
+// per path: throughput and radiance (32), two ray queues (2 x 32), hits (32), shadow queue (52);
+// plus a 112-byte primary point per pixel, budgeted as one pixel per path
+constexpr uint64_t kStaticBytesPerPath = 32 + 2 * 32 + 32 + (32 + 16 + 4) + 16 * kPixFloat4;
 // alignment padding of the carved arrays, and the tick tables of a one-request render
 constexpr uint64_t kStaticSlackBytes = 16 * 256 + 1024;
 
@@ -260,14 +259,9 @@ int render_frame_static(const SceneGPU& scene, const RenderArgs& args, const uin
         p += (count * sizeof(T) + 255) & ~255ull;
     };
     carve(w.path, 2 * N);
-    carve(w.rng, N);
     carve(w.q_od[0], 2 * N);
     carve(w.q_od[1], 2 * N);
-    carve(w.q_path[0], N);
-    carve(w.q_path[1], N);
-    carve(w.hit_tuv, N);
-    carve(w.hit_geom, N);
-    carve(w.hit_inst, N);
+    carve(w.hit, 2 * N);
     carve(w.s_od, 2 * N);
     carve(w.s_contrib, N);
     carve(w.s_path, N);

@@ -84,13 +84,13 @@ struct Work {
     // 2 float4 per path, one 32-byte sector: (throughput rgb, current IOR), (radiance rgb, pdf
     // of the last BSDF sample)
     float4* path = nullptr;
-    uint32_t* rng = nullptr;
-    // ray queues (two, ping-pong) and hits
-    float4* q_od[2] = {nullptr, nullptr}; // 2 float4 per entry: (o, tmin), (d, tmax)
-    uint32_t* q_path[2] = {nullptr, nullptr};
-    float4* hit_tuv = nullptr; // t, u, v, primitive bits
-    uint32_t* hit_geom = nullptr;
-    uint32_t* hit_inst = nullptr; // instance of two-level hits, 0xFFFFFFFF otherwise
+    // ray queues (two, ping-pong): 2 float4 per entry, one 32-byte sector: (origin, the path's
+    // RNG state bits), (direction, entry tag bits: chunk << 24 | path); every bounce ray spans
+    // [0, kRayTmax], and the path's RNG state travels with its ray
+    float4* q_od[2] = {nullptr, nullptr};
+    // closest hit per queue entry, 2 uint4 (one sector): (t, u, v, primitive), (geometry,
+    // instance of two-level hits or 0xFFFFFFFF, 0, 0)
+    uint4* hit = nullptr;
     // shadow queue
     float4* s_od = nullptr;     // 2 float4 per entry: (o, tmax), (d, 0)
     float4* s_contrib = nullptr;

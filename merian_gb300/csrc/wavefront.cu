@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM)
         bool want = false, want_shadow = false;
         float3 no, nd;
         float4 s_o, s_d, s_c;
-        uint32_t ci = 0;
+        uint32_t ci = 0, rng_state = 0;
         const uint32_t p = (perm && j < n) ? __ldg(&perm[j]) : j;
         if (j < n) {
             ci = chunk_by_path(t.chunks, nc, p);
@@ -277,14 +277,13 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM)
                                     s_o, s_d, s_c);
             t.w.path[2 * p + 0] = make_float4(thr.x, thr.y, thr.z, ior);
             t.w.path[2 * p + 1] = make_float4(rad.x, rad.y, rad.z, last_pdf);
-            t.w.rng[p] = rng.state;
+            rng_state = rng.state;
         }
         const uint32_t tag = (ci << kPathBits) | p;
         const uint32_t q = warp_append(t.w.counters + 0, want);
         if (want) {
-            t.w.q_od[0][2 * q + 0] = make_float4(no.x, no.y, no.z, 0.f);
-            t.w.q_od[0][2 * q + 1] = make_float4(nd.x, nd.y, nd.z, kRayTmax);
-            t.w.q_path[0][q] = tag;
+            t.w.q_od[0][2 * q + 0] = make_float4(no.x, no.y, no.z, __uint_as_float(rng_state));
+            t.w.q_od[0][2 * q + 1] = make_float4(nd.x, nd.y, nd.z, __uint_as_float(tag));
         }
         {
             const uint32_t sq = warp_append(t.w.counters + 2, want_shadow);
@@ -309,33 +308,34 @@ __global__ void __launch_bounds__(128, kTraceBlocksPerSM)
     if (threadIdx.x < kSortKeys) key_count[threadIdx.x] = 0u;
     __syncthreads();
     const float4* q = t.w.q_od[qi];
-    const uint32_t* qp = t.w.q_path[qi];
+    // the entry's chunk, from the tag in the direction's w
+    auto chunk_of = [&](uint32_t i) -> const ChunkGPU& {
+        return t.chunks[__float_as_uint(__ldg((const float*)&q[2 * i + 1] + 3)) >> kPathBits];
+    };
     auto load = [&](uint32_t i, TraceState& s) {
-        const ChunkGPU& c = t.chunks[__ldg(&qp[i]) >> kPathBits];
         const float4 a = q[2 * i + 0];
         const float4 b = q[2 * i + 1];
+        const ChunkGPU& c = t.chunks[__float_as_uint(b.w) >> kPathBits];
         s.nodes = c.nodes;
         s.tris_base = c.tris;
         s.tri_stride = c.tri_stride;
         s.insts = c.insts;
         s.mask = c.mask;
-        trace_init(s, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w, b.w);
+        trace_init(s, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), 0.0f, kRayTmax);
     };
     auto store = [&](uint32_t i, const Hit& h) {
-        t.w.hit_tuv[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
-        t.w.hit_geom[i] = h.geom;
-        t.w.hit_inst[i] = h.inst;
+        t.w.hit[2 * i + 0] =
+            make_uint4(__float_as_uint(h.t), __float_as_uint(h.u), __float_as_uint(h.v), h.prim);
+        t.w.hit[2 * i + 1] = make_uint4(h.geom, h.inst, 0u, 0u);
         if (sort) {
             uint32_t key = 0u; // misses shade the environment
-            if (h.geom != kNoInst)
-                key = __ldg(&t.chunks[__ldg(&qp[i]) >> kPathBits].geom_key[h.geom]);
+            if (h.geom != kNoInst) key = __ldg(&chunk_of(i).geom_key[h.geom]);
             t.w.keys[i] = (uint8_t)key;
             atomicAdd(&key_count[key], 1u);
         }
     };
     auto alpha = [&](uint32_t i, uint32_t g, uint32_t p, float u, float v) {
-        return ALPHA &&
-               alpha_discard(t.scenes[t.chunks[__ldg(&qp[i]) >> kPathBits].scene], g, p, u, v);
+        return ALPHA && alpha_discard(t.scenes[chunk_of(i).scene], g, p, u, v);
     };
     trace_persistent<false, COUNT, TWO_LEVEL>(n, t.w.counters + 4, load, store, alpha, &ctr,
                                               t.w.counters + 3, t.refill_lanes,
@@ -373,30 +373,33 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM)
         bool want = false, want_shadow = false;
         float3 no, nd;
         float4 s_o, s_d, s_c;
-        uint32_t tag = 0;
+        uint32_t tag = 0, rng_state = 0;
         if (j < n) {
             const uint32_t i = perm ? __ldg(&perm[j]) : j;
-            tag = t.w.q_path[qi][i];
+            // the entry's sector: the path's RNG state and the tag ride in the w components; a
+            // surface point comes from the hit's vertices, and an environment point's position
+            // is never read here (it does not scatter)
+            const float4 qa = t.w.q_od[qi][2 * i + 0];
+            const float4 qb = t.w.q_od[qi][2 * i + 1];
+            tag = __float_as_uint(qb.w);
             const uint32_t p = tag & kPathMask;
             const ChunkGPU& c = t.chunks[tag >> kPathBits];
             const ReqGPU& r = t.reqs[c.req];
             const DevScene& sc = t.scenes[c.scene];
-            // the ray's direction only: a surface point comes from the hit's vertices, and an
-            // environment point's position is never read here (it does not scatter)
-            const float4 qb = t.w.q_od[qi][2 * i + 1];
             const float3 o = f3(0.f, 0.f, 0.f), d = f3(qb.x, qb.y, qb.z);
-            const float4 h = t.w.hit_tuv[i];
-            const uint32_t geom = t.w.hit_geom[i];
+            const uint4 h0 = t.w.hit[2 * i + 0], h1 = t.w.hit[2 * i + 1];
+            const float4 h = make_float4(__uint_as_float(h0.x), __uint_as_float(h0.y),
+                                         __uint_as_float(h0.z), __uint_as_float(h0.w));
+            const uint32_t geom = h1.x;
             const float4 t4 = t.w.path[2 * p + 0], r4 = t.w.path[2 * p + 1];
             float3 thr = f3(t4.x, t4.y, t4.z), rad = f3(r4.x, r4.y, r4.z);
             float ior = t4.w, last_pdf = r4.w;
-            Pcg rng{t.w.rng[p]};
+            Pcg rng{__float_as_uint(qa.w)};
             SPd sp;
             if (geom == 0xFFFFFFFFu || geom >= sc.geom_count) {
                 sp = env_sp(sc, o, d);
             } else {
-                sp = surface_sp(sc, o, d, geom, __float_as_uint(h.w), h.y, h.z,
-                                t.w.hit_inst[i]);
+                sp = surface_sp(sc, o, d, geom, h0.w, h.y, h.z, h1.y);
             }
             const bool scatters = k < (int)r.max_len;
             sp.has_material = sp.has_material && scatters;
@@ -413,13 +416,12 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM)
                                     s_o, s_d, s_c);
             t.w.path[2 * p + 0] = make_float4(thr.x, thr.y, thr.z, ior);
             t.w.path[2 * p + 1] = make_float4(rad.x, rad.y, rad.z, last_pdf);
-            t.w.rng[p] = rng.state;
+            rng_state = rng.state;
         }
         const uint32_t q = warp_append(t.w.counters + qo, want);
         if (want) {
-            t.w.q_od[qo][2 * q + 0] = make_float4(no.x, no.y, no.z, 0.f);
-            t.w.q_od[qo][2 * q + 1] = make_float4(nd.x, nd.y, nd.z, kRayTmax);
-            t.w.q_path[qo][q] = tag;
+            t.w.q_od[qo][2 * q + 0] = make_float4(no.x, no.y, no.z, __uint_as_float(rng_state));
+            t.w.q_od[qo][2 * q + 1] = make_float4(nd.x, nd.y, nd.z, __uint_as_float(tag));
         }
         {
             const uint32_t sq = warp_append(t.w.counters + 2, want_shadow);
@@ -647,10 +649,9 @@ void work_free(Work& w) {
         w = Work{};
         return;
     }
-    void* ptrs[] = {w.path,    w.rng,       w.q_od[0], w.q_od[1], w.q_path[0],
-                    w.q_path[1], w.hit_tuv, w.hit_geom, w.s_od,  w.s_contrib, w.s_path,
+    void* ptrs[] = {w.path,    w.q_od[0],   w.q_od[1], w.hit,     w.s_od,  w.s_contrib, w.s_path,
                     w.pix,     w.pix_id,    w.out,    w.counters, w.stats,    w.tables,
-                    w.keys,    w.perm,      w.hit_inst};
+                    w.keys,    w.perm};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     w = Work{};
@@ -675,14 +676,9 @@ int work_reserve(Work& w, uint64_t paths, uint64_t pixels) {
     if (paths > w.path_cap) {
         auto release_paths = [&w]() {
             release(w.path);
-            release(w.rng);
             release(w.q_od[0]);
             release(w.q_od[1]);
-            release(w.q_path[0]);
-            release(w.q_path[1]);
-            release(w.hit_tuv);
-            release(w.hit_geom);
-            release(w.hit_inst);
+            release(w.hit);
             release(w.s_od);
             release(w.s_contrib);
             release(w.s_path);
@@ -694,14 +690,9 @@ int work_reserve(Work& w, uint64_t paths, uint64_t pixels) {
         new_generation(w);
         uint64_t b = 0;
         bool ok = alloc(w.path, 2 * paths, b) == cudaSuccess &&
-                  alloc(w.rng, paths, b) == cudaSuccess &&
                   alloc(w.q_od[0], 2 * paths, b) == cudaSuccess &&
                   alloc(w.q_od[1], 2 * paths, b) == cudaSuccess &&
-                  alloc(w.q_path[0], paths, b) == cudaSuccess &&
-                  alloc(w.q_path[1], paths, b) == cudaSuccess &&
-                  alloc(w.hit_tuv, paths, b) == cudaSuccess &&
-                  alloc(w.hit_geom, paths, b) == cudaSuccess &&
-                  alloc(w.hit_inst, paths, b) == cudaSuccess &&
+                  alloc(w.hit, 2 * paths, b) == cudaSuccess &&
                   alloc(w.s_od, 2 * paths, b) == cudaSuccess &&
                   alloc(w.s_contrib, paths, b) == cudaSuccess &&
                   alloc(w.s_path, paths, b) == cudaSuccess &&
