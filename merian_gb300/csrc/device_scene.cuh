@@ -139,6 +139,8 @@ struct RayPre {
     GBPT_DI int kx() const { return (int)(k & 3u); }
     GBPT_DI int ky() const { return (int)((k >> 2) & 3u); }
     GBPT_DI int kz() const { return (int)((k >> 4) & 3u); }
+    GBPT_DI uint32_t oct_inv() const { return (k >> 8) & 7u; }
+    GBPT_DI uint32_t mask() const { return (k >> 16) & 0xFFu; }
 };
 GBPT_DI float pick(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
 GBPT_DI RayPre ray_pre(float3 o, float3 d) {
@@ -299,7 +301,6 @@ struct TraceState {
     uint32_t mask;       // instance mask of the ray
     float3 o, d, inv;    // the ray in the current space (object space inside an instance)
     float tmin;
-    uint32_t oct_inv; // 7 - direction octant (bit a set: axis a positive)
     RayPre pre;
     uint2 ngroup, tgroup;
     int sp;
@@ -316,8 +317,8 @@ GBPT_DI void set_ray(TraceState& s, float3 o, float3 d) {
     s.inv = f3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
     const uint32_t oct = (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) |
                          ((__float_as_uint(d.z) >> 31) << 2);
-    s.oct_inv = 7u - oct;
     s.pre = ray_pre(o, d);
+    s.pre.k |= ((7u - oct) << 8) | ((s.mask & 0xFFu) << 16);
     s.tris = kTriCopies > 1 ? s.tris_base + (size_t)s.pre.kz() * s.tri_stride : s.tris_base;
 }
 
@@ -435,9 +436,10 @@ GBPT_DI uint32_t intersect_node(const TraceState& s, uint32_t ni, uint32_t& chil
     tri_base = n1.y;
 
     // the direction's signs from the octant (negative axis a: bit a of oct_inv clear)
-    const uint32_t oct_inv4 = s.oct_inv * 0x01010101u;
-    const bool negx = (s.oct_inv & 1u) == 0u, negy = (s.oct_inv & 2u) == 0u;
-    const bool negz = (s.oct_inv & 4u) == 0u;
+    const uint32_t oct_inv = s.pre.oct_inv();
+    const uint32_t oct_inv4 = oct_inv * 0x01010101u;
+    const bool negx = (oct_inv & 1u) == 0u, negy = (oct_inv & 2u) == 0u;
+    const bool negz = (oct_inv & 4u) == 0u;
     uint32_t hitmask = 0;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
@@ -520,7 +522,7 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
                 }
                 st(s.sp++) = s.ngroup;
             }
-            const uint32_t slot = (bit - 24u) ^ s.oct_inv;
+            const uint32_t slot = (bit - 24u) ^ s.pre.oct_inv();
             const uint32_t ni = s.ngroup.x + __popc((hits & 0xFFu) & ((1u << slot) - 1u));
             uint32_t cb, tb, im;
             if (COUNT) count_step(ctr->node_steps, ctr->node_lanes);
@@ -552,7 +554,7 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
             if (TWO_LEVEL && s.insts != nullptr && s.inst == kNoInst) {
                 // a top-level leaf: an instance (record: instance index, mask in the flag word)
                 const uint32_t fl = __float_as_uint(__ldg(&s.tris[3 * ti + 2]).w);
-                if (((fl & 0xFFu) & s.mask) == 0u) continue;
+                if ((fl & s.pre.mask()) == 0u) continue;
                 if (s.sp + 2 > kStackSize) {
                     atomicOr(err, 1u);
                     s.tgroup.y = 0u;
@@ -569,7 +571,7 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
             const float4 r1 = __ldg(rec + 1);
             const float4 r2 = __ldg(rec + 2);
             const uint32_t tfl = __float_as_uint(r2.w);
-            if (((tfl & 0xFFu) & s.mask) == 0u) continue;
+            if ((tfl & s.pre.mask()) == 0u) continue;
             if (COUNT) {
                 ctr->tris++;
                 count_step(ctr->tri_steps, ctr->tri_lanes);
