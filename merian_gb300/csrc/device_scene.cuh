@@ -303,12 +303,16 @@ struct TraceState {
     float tmin;
     RayPre pre;
     uint2 ngroup, tgroup;
-    int sp;
     Hit best;          // a hit was found once best.geom != kNoInst
     float det;         // GBPT_DEFER_UV: best.u, best.v are V, W of the test until divided by it
     float3 wo, wd; // the world ray
     uint32_t inst; // instance being traversed, kNoInst at the top level
     int inst_sp;   // stack depth at which it was entered
+    // the traversal stack's depth, kept in bits 24..31 of the ray's axis word
+    GBPT_DI int sp() const { return (int)(pre.k >> 24); }
+    GBPT_DI void push_sp() { pre.k += 1u << 24; }
+    GBPT_DI void pop_sp() { pre.k -= 1u << 24; }
+    GBPT_DI void clear_sp() { pre.k &= 0x00FFFFFFu; }
 };
 
 GBPT_DI void set_ray(TraceState& s, float3 o, float3 d) {
@@ -317,19 +321,20 @@ GBPT_DI void set_ray(TraceState& s, float3 o, float3 d) {
     s.inv = f3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
     const uint32_t oct = (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) |
                          ((__float_as_uint(d.z) >> 31) << 2);
+    const uint32_t depth = s.pre.k & 0xFF000000u; // the stack outlives a change of space
     s.pre = ray_pre(o, d);
-    s.pre.k |= ((7u - oct) << 8) | ((s.mask & 0xFFu) << 16);
+    s.pre.k |= ((7u - oct) << 8) | ((s.mask & 0xFFu) << 16) | depth;
     s.tris = kTriCopies > 1 ? s.tris_base + (size_t)s.pre.kz() * s.tri_stride : s.tris_base;
 }
 
 GBPT_DI void trace_init(TraceState& s, float3 o, float3 d, float tmin, float tmax) {
+    s.pre.k = 0u;
     set_ray(s, o, d);
     s.wo = o;
     s.wd = d;
     s.tmin = tmin;
     s.ngroup = make_uint2(0u, 0x80000000u);
     s.tgroup = make_uint2(0u, 0u);
-    s.sp = 0;
     s.best.t = tmax;
     s.best.u = s.best.v = 0.0f;
     s.best.prim = s.best.geom = s.best.inst = kNoInst;
@@ -342,7 +347,7 @@ GBPT_DI void enter_instance(TraceState& s, uint32_t ii) {
     const float4 w0 = __ldg(r + 3), w1 = __ldg(r + 4), w2 = __ldg(r + 5);
     set_ray(s, xform_point(w0, w1, w2, s.wo), xform_vector(w0, w1, w2, s.wd));
     s.inst = ii;
-    s.inst_sp = s.sp;
+    s.inst_sp = s.sp();
     s.ngroup = make_uint2(__float_as_uint(__ldg(r + 6).x), 0x80000000u);
 }
 
@@ -512,15 +517,16 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
             const uint32_t bit = 31u - __clz(hits & 0xFF000000u);
             s.ngroup.y &= ~(1u << bit);
             if (s.ngroup.y > 0x00FFFFFFu) {
-                if (s.sp >= kStackSize) {
+                if (s.sp() >= kStackSize) {
                     atomicOr(err, 1u);
-                    s.sp = 0;
+                    s.clear_sp();
                     s.ngroup.y = 0;
                     s.tgroup.y = 0;
                     s.inst = kNoInst;
                     break;
                 }
-                st(s.sp++) = s.ngroup;
+                st(s.sp()) = s.ngroup;
+                s.push_sp();
             }
             const uint32_t slot = (bit - 24u) ^ s.pre.oct_inv();
             const uint32_t ni = s.ngroup.x + __popc((hits & 0xFFu) & ((1u << slot) - 1u));
@@ -543,8 +549,9 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
         // never those of a first-hit query, which any of its triangles may end
         const bool may_postpone = WARP && !ANY && s.ngroup.y > 0x00FFFFFFu;
         while (s.tgroup.y != 0u) {
-            if (may_postpone && s.sp < kStackSize && __popc(__activemask()) < postpone_lanes) {
-                st(s.sp++) = s.tgroup;
+            if (may_postpone && s.sp() < kStackSize && __popc(__activemask()) < postpone_lanes) {
+                st(s.sp()) = s.tgroup;
+                s.push_sp();
                 s.tgroup.y = 0u;
                 break;
             }
@@ -555,13 +562,19 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
                 // a top-level leaf: an instance (record: instance index, mask in the flag word)
                 const uint32_t fl = __float_as_uint(__ldg(&s.tris[3 * ti + 2]).w);
                 if ((fl & s.pre.mask()) == 0u) continue;
-                if (s.sp + 2 > kStackSize) {
+                if (s.sp() + 2 > kStackSize) {
                     atomicOr(err, 1u);
                     s.tgroup.y = 0u;
                     continue;
                 }
-                if (s.ngroup.y > 0x00FFFFFFu) st(s.sp++) = s.ngroup;
-                if (s.tgroup.y != 0u) st(s.sp++) = s.tgroup;
+                if (s.ngroup.y > 0x00FFFFFFu) {
+                    st(s.sp()) = s.ngroup;
+                    s.push_sp();
+                }
+                if (s.tgroup.y != 0u) {
+                    st(s.sp()) = s.tgroup;
+                    s.push_sp();
+                }
                 s.tgroup.y = 0u;
                 enter_instance(s, __float_as_uint(__ldg(&s.tris[3 * ti]).w));
                 break;
@@ -604,9 +617,13 @@ GBPT_DI bool trace_loop(TraceState& s, StackRef&& st, TraceCounters* ctr, uint32
         }
         bool done = done_any;
         if (!done && s.ngroup.y <= 0x00FFFFFFu) {
-            if (TWO_LEVEL && s.inst != kNoInst && s.sp == s.inst_sp) exit_instance(s);
-            if (s.sp == 0) done = true;
-            else s.ngroup = st(--s.sp);
+            if (TWO_LEVEL && s.inst != kNoInst && s.sp() == s.inst_sp) exit_instance(s);
+            if (s.sp() == 0) {
+                done = true;
+            } else {
+                s.pop_sp();
+                s.ngroup = st(s.sp());
+            }
         }
         if (done) break;
         if (WARP && !pool_empty && __popc(__activemask()) < refill_lanes) return false;
