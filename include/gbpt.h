@@ -286,7 +286,7 @@ GBPT_API int gbpt_render_device(gbpt_ctx* ctx, uint32_t scene, const gbpt_camera
  * fixed 64 MiB device array compiled into the library, held by each GPU that loads the library
  * until the process exits; this call allocates nothing. The scene must already be resident
  * (gbpt_scene_create, an earlier set-up step) and out_rgba_device is caller-owned device memory.
- * Limits: spp at most the paths one pass over the array holds (225,815), a pixel
+ * Limits: spp at most the paths one pass over the array holds (228,908), a pixel
  * subset of at most 65,536 entries; larger requests return GBPT_ERR_INVALID. Every call looks up
  * the array's device address (no allocation; nothing cached, so a device reset between calls is
  * harmless); the first lookup on a device may load the library's module, so make the first call
