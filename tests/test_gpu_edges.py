@@ -195,3 +195,34 @@ def test_bvh_build_modes_find_the_same_hits(gpu_ctx):
         assert nodes[0] < nodes[1] < nodes[2]
     finally:
         gpu_ctx.set_tuning()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("sign", [1.0, -1.0])
+def test_facing_per_axis_matches_oracle(gpu_ctx, axis, sign):
+    """The kernels read each triangle in the order of the ray's dominant axis from one of three
+    stored copies and flip the facing for a negative direction: one-sided, reversed, FlipFacing
+    and TwoSided triangles seen along each axis both ways give the oracle's hits and bits."""
+    import torch
+    from conftest import facing_case
+    from merian_gb300 import _native as N
+    sc, rays, expect, t_expect = facing_case(axis, sign)
+    osc = O.OracleScene(sc)
+    sid = gpu_ctx.upload(sc)
+    try:
+        d_rays = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
+        d_hits = torch.zeros(len(rays) * N.HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        for mask, hit in expect.items():
+            for any_hit in (False, True):
+                gpu_ctx.trace(sid, d_rays.data_ptr(), len(rays), d_hits.data_ptr(), mask=mask,
+                              any_hit=any_hit)
+                gpu_ctx.synchronize()
+                g = d_hits.cpu().numpy().view(N.HIT_DTYPE)
+                assert (g["geometry_index"][0] != 0xFFFFFFFF) == hit, (mask, any_hit)
+            o, _, _ = osc.trace_rays(rays, mask=mask, hit_dtype=N.HIT_DTYPE)
+            assert g["geometry_index"][0] == o["geometry_index"][0]
+            if hit:
+                assert g["t"].view(np.uint32)[0] == o["t"].view(np.uint32)[0]
+    finally:
+        gpu_ctx.destroy_scene(sid)

@@ -195,3 +195,25 @@ def test_oracle_nee_unbiased_on_soup(nee, rr):
     z = (mean - gm)[ok] / se[ok]
     assert np.mean(np.abs(z) > 3) < 0.02, np.sort(np.abs(z))[-10:]
     assert np.mean(z ** 2) < 1.5
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("sign", [1.0, -1.0])
+@pytest.mark.parametrize("fp64", [False, True])
+def test_watertight_facing_per_axis(axis, sign, fp64):
+    """One-sided triangles seen along each dominant axis in both directions: the front face
+    (counter-clockwise, cross(e01, e02) towards the origin) is hit, the back face is culled,
+    FlipFacing swaps them and TwoSided accepts both; the distance is the same either way. The
+    test keeps one 2D frame per dominant axis and flips the facing for a negative direction, so
+    both signs of each axis are pinned here."""
+    from conftest import facing_case
+    from merian_gb300 import _native as N
+    sc, rays, expect, t_expect = facing_case(axis, sign)
+    osc = O.OracleScene(sc)
+    ts = []
+    for mask, hit in expect.items():
+        h, _, _ = osc.trace_rays(rays, mask=mask, fp64=fp64, hit_dtype=N.HIT_DTYPE)
+        assert (h["geometry_index"][0] != 0xFFFFFFFF) == hit, (mask, hit)
+        if hit:
+            ts.append(float(h["t"][0]))
+    assert max(ts) == min(ts) and abs(ts[0] - t_expect) < 1e-5
