@@ -123,7 +123,8 @@ bool invert_affine(const float* m, double* inv) {
 void free_scene(SceneGPU& s) {
     void* ptrs[] = {s.nodes,    s.tris,     s.verts,      s.idx,       s.tri_verts, s.geoms,    s.mats,
                     s.env,      s.env_marg, s.env_cond,   s.env_func,  s.light_tris, s.light_cdf,
-                    s.light_guide, s.env_marg_guide, s.env_cond_guide, s.geom_key,
+                    s.light_guide, s.env_marg_guide, s.env_cond_guide, s.env_rows, s.env_cols,
+                    s.geom_key,
                     s.inst,     s.tex,      s.tex_info,   s.srgb_lut};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -142,14 +143,48 @@ std::vector<uint32_t> cdf_guide(const float* a, uint32_t n, uint32_t& G) {
     return g;
 }
 
-// The build input's reference splitting for a GBPT_BVH_* setting. GBPT_BVH_SPLIT splits hard in
-// single-level scenes (measured on the 1M-triangle soup: ratio 2 / depth 4 renders 25 % faster
-// than no splitting) and lightly in the BLASes of two-level scenes (instanced meshes: ratio 8 /
-// depth 2 is 5 % faster than none, ratio 2 / depth 4 5 % slower).
+// Walker's alias table (Vose's construction) of the discrete distribution w[0, n): entry i is
+// (the probability that bin i keeps i, as float bits; the bin it gives otherwise). Built in
+// double in a fixed order, so every host makes the same table.
+void alias_table(const double* w, uint32_t n, uint32_t* out) {
+    double sum = 0.0;
+    for (uint32_t i = 0; i < n; ++i) sum += w[i];
+    std::vector<double> q(n);
+    std::vector<uint32_t> small, large;
+    for (uint32_t i = 0; i < n; ++i) {
+        q[i] = sum > 0.0 ? w[i] * (double)n / sum : 1.0;
+        (q[i] < 1.0 ? small : large).push_back(i);
+    }
+    while (!small.empty() && !large.empty()) {
+        const uint32_t a = small.back(), b = large.back();
+        small.pop_back();
+        const float pa = (float)q[a];
+        std::memcpy(&out[2 * a], &pa, 4);
+        out[2 * a + 1] = b;
+        q[b] = (q[b] + q[a]) - 1.0;
+        if (q[b] < 1.0) {
+            large.pop_back();
+            small.push_back(b);
+        }
+    }
+    // what rounding leaves on either list keeps its own bin
+    for (const std::vector<uint32_t>* l : {&small, &large})
+        for (uint32_t i : *l) {
+            const float one = 1.0f;
+            std::memcpy(&out[2 * i], &one, 4);
+            out[2 * i + 1] = i;
+        }
+}
+
 // GBPT_SHADE_TRI_RECORDS: upload the de-indexed per-triangle vertex records read by shading
 #ifndef GBPT_SHADE_TRI_RECORDS
 #define GBPT_SHADE_TRI_RECORDS 1
 #endif
+
+// The build input's reference splitting for a GBPT_BVH_* setting. GBPT_BVH_SPLIT splits hard in
+// single-level scenes (measured on the 1M-triangle soup: ratio 2 / depth 4 renders 25 % faster
+// than no splitting) and lightly in the BLASes of two-level scenes (instanced meshes: ratio 8 /
+// depth 2 is 5 % faster than none, ratio 2 / depth 4 5 % slower).
 #ifndef GBPT_BVH_SPLIT_RATIO
 #define GBPT_BVH_SPLIT_RATIO 2.0
 #endif
@@ -772,7 +807,19 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
         marg[h] = 1.0f;
         for (size_t i = 0; i < func.size(); ++i) ffunc[i] = (float)func[i];
         s.env_func_int = (float)(tot / ((double)w * h));
+#if GBPT_ENV_ALIAS
+        {
+            // the same density by alias tables: the row by the row sums, then the column in it
+            std::vector<uint32_t> at(2 * (size_t)h), ct(2 * (size_t)w * h);
+            alias_table(rows.data(), h, at.data());
+            for (uint32_t y = 0; y < h; ++y)
+                alias_table(&func[(size_t)y * w], w, &ct[2 * (size_t)y * w]);
+            if ((rc = upload(&s.env_rows, at.data(), at.size() * 4, bytes))) return fail(rc);
+            if ((rc = upload(&s.env_cols, ct.data(), ct.size() * 4, bytes))) return fail(rc);
+        }
+#endif
         if ((rc = upload(&s.env_func, ffunc.data(), ffunc.size() * sizeof(float), bytes))) return fail(rc);
+#if !GBPT_ENV_ALIAS
         if ((rc = upload(&s.env_cond, cond.data(), cond.size() * sizeof(float), bytes))) return fail(rc);
         if ((rc = upload(&s.env_marg, marg.data(), marg.size() * sizeof(float), bytes))) return fail(rc);
         const std::vector<uint32_t> mg = cdf_guide(marg.data() + 1, h, s.env_marg_g);
@@ -784,6 +831,7 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
         }
         if ((rc = upload(&s.env_marg_guide, mg.data(), mg.size() * 4, bytes))) return fail(rc);
         if ((rc = upload(&s.env_cond_guide, cg.data(), cg.size() * 4, bytes))) return fail(rc);
+#endif
     }
     // RGBA8 textures, concatenated, with (first texel, width, height, sRGB) per texture and the
     // sRGB decoding table (IEC 61966-2-1), evaluated in double and rounded once

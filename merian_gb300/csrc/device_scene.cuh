@@ -53,6 +53,8 @@ struct DevScene {
     // guide tables of the light, marginal and conditional CDFs: entry k is the upper bound of
     // k / G (G a power of two), so the search for u covers [guide[k], guide[k + 1]] only
     const uint32_t* __restrict__ light_guide;
+    const uint2* __restrict__ env_rows; // alias tables (GBPT_ENV_ALIAS): per row, per texel
+    const uint2* __restrict__ env_cols;
     const uint32_t* __restrict__ env_marg_guide;
     const uint32_t* __restrict__ env_cond_guide; // G + 1 per row
     uint32_t light_g, env_marg_g, env_cond_g;

@@ -32,6 +32,8 @@ inline DevScene make_dev_scene(const SceneGPU& s) {
     d.n_lights = s.n_lights;
     d.light_total = s.light_total;
     d.light_guide = (const uint32_t*)s.light_guide;
+    d.env_rows = (const uint2*)s.env_rows;
+    d.env_cols = (const uint2*)s.env_cols;
     d.env_marg_guide = (const uint32_t*)s.env_marg_guide;
     d.env_cond_guide = (const uint32_t*)s.env_cond_guide;
     d.light_g = s.light_g;
@@ -276,6 +278,28 @@ GBPT_DI uint32_t upper_bound_f(const float* a, uint32_t n, float x, const uint32
     return lo;
 }
 
+// Bin (k n) >> 24 of n for the draw u = k 2^-24, and the rest of k n as a fraction in [0, 1):
+// a uniform choice of the bin and, independent of it, a uniform fraction.
+GBPT_DI uint32_t bin_of(float u, uint32_t n, float& frac) {
+    const uint64_t kn = (uint64_t)(uint32_t)(u * 16777216.0f) * n;
+    frac = (float)(uint32_t)(kn & 0xFFFFFFull) * 5.9604644775390625e-08f;
+    return (uint32_t)(kn >> 24);
+}
+
+// Bin i of the alias table t (Walker 1977) keeps i when the uniform d is below its keep
+// probability and gives its alias otherwise; d is rescaled to [0, 1) within the branch taken, a
+// uniform independent of the outcome, for the next decision.
+GBPT_DI uint32_t alias_pick(const uint2* t, uint32_t i, float& d) {
+    const uint2 e = __ldg(&t[i]);
+    const float p = __uint_as_float(e.x);
+    if (d < p) {
+        d = d / p;
+        return i;
+    }
+    d = (d - p) / (1.0f - p);
+    return e.y;
+}
+
 // solid-angle density of the environment strategy (piecewise constant over texels)
 GBPT_DI float env_pdf(const DevScene& sc, float3 dir) {
     if (sc.ew == 0u) return 0.f;
@@ -310,6 +334,14 @@ GBPT_DI LightSample sample_light(const DevScene& sc, float3 pos, Pcg& rng) {
     const float u0 = rng.next_float(), u1 = rng.next_float(), u2 = rng.next_float();
     if (sc.p_env <= 0.f && sc.n_lights == 0u) return ls;
     if (u0 < sc.p_env) {
+#if GBPT_ENV_ALIAS
+        // the row by the row table, then the column by that row's table: u1 and u2 choose the
+        // bins and, by their fractions, the point in the texel; the strategy draw, rescaled
+        // (p_env is 1 or 1/2, so exactly), makes both keep-or-alias decisions
+        float d = u0 / sc.p_env, fy, fx;
+        const uint32_t y = alias_pick(sc.env_rows, bin_of(u1, sc.eh, fy), d);
+        const uint32_t x = alias_pick(sc.env_cols + (size_t)y * sc.ew, bin_of(u2, sc.ew, fx), d);
+#else
         uint32_t y = upper_bound_f(sc.env_marg + 1, sc.eh, u1, sc.env_marg_guide, sc.env_marg_g);
         y = min(y, sc.eh - 1u);
         const float m0 = __ldg(&sc.env_marg[y]), m1 = __ldg(&sc.env_marg[y + 1]);
@@ -321,6 +353,7 @@ GBPT_DI LightSample sample_light(const DevScene& sc, float3 pos, Pcg& rng) {
         const float c0 = __ldg(&c[x]), c1 = __ldg(&c[x + 1]);
         const float fy = fminf(fmaxf((u1 - m0) / (m1 - m0), 0.f), 1.f);
         const float fx = fminf(fmaxf((u2 - c0) / (c1 - c0), 0.f), 1.f);
+#endif
         const float u = ((float)x + fx) / (float)sc.ew, v = ((float)y + fy) / (float)sc.eh;
         const float phi = kPi * (2.0f * u - 1.0f), theta = kPi * v;
         float sp, cp, st, ct;

@@ -22,6 +22,13 @@ struct DevScene; // device_scene.cuh
 #endif
 constexpr int kTriCopies = GBPT_TRI_AXIS_COPIES ? 3 : 1;
 
+// GBPT_ENV_ALIAS: next-event estimation picks the environment texel by alias tables (a row, then
+// a column: two dependent loads) instead of inverting the marginal and conditional CDFs (a
+// guide-table lookup and a short search each)
+#ifndef GBPT_ENV_ALIAS
+#define GBPT_ENV_ALIAS 1
+#endif
+
 // A scene resident in HBM. All pointers are device pointers owned by the context.
 struct SceneGPU {
     void* nodes = nullptr;      // CWBVH, 80 B per node
@@ -45,6 +52,10 @@ struct SceneGPU {
     void* light_guide = nullptr;
     void* env_marg_guide = nullptr;
     void* env_cond_guide = nullptr; // G + 1 entries per row
+    // GBPT_ENV_ALIAS: alias tables of the same density, uint2 (keep probability bits, alias) per
+    // row and per texel
+    void* env_rows = nullptr;
+    void* env_cols = nullptr;
     uint32_t light_g = 0, env_marg_g = 0, env_cond_g = 0;
     uint64_t n_nodes = 0, n_tris = 0, n_verts = 0;
     uint32_t geom_count = 0, mat_count = 0;
