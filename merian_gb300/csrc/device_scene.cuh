@@ -746,11 +746,14 @@ GBPT_DI int wrapi(int i, int n) {
     const int r = i % n;
     return r < 0 ? r + n : r;
 }
-GBPT_DI float3 env_eval(const DevScene& s, float3 dir) {
-    if (s.ew == 0u) return f3(0.f, 0.f, 0.f);
+// The lat-long map coordinates (u, v) of a world direction (its local frame by env_to_local).
+GBPT_DI void env_uv(const DevScene& s, float3 dir, float& u, float& v) {
     const float3 p = normalize(env_to_local(s, dir));
-    const float u = atan2f(p.x, -p.z) * kInv2Pi + 0.5f;
-    const float v = acosf(fminf(fmaxf(p.y, -1.0f), 1.0f)) * kInvPi;
+    u = atan2f(p.x, -p.z) * kInv2Pi + 0.5f;
+    v = acosf(fminf(fmaxf(p.y, -1.0f), 1.0f)) * kInvPi;
+}
+// The environment's radiance at map coordinates (u, v): bilinear, repeating.
+GBPT_DI float3 env_eval_uv(const DevScene& s, float u, float v) {
     if (!(u == u) || !(v == v)) return f3(0.f, 0.f, 0.f);
     const float x = u * (float)s.ew - 0.5f, y = v * (float)s.eh - 0.5f;
     const float fx = floorf(x), fy = floorf(y);
@@ -765,6 +768,12 @@ GBPT_DI float3 env_eval(const DevScene& s, float3 dir) {
     const float3 top = f3(t00.x, t00.y, t00.z) * (1.0f - a) + f3(t10.x, t10.y, t10.z) * a;
     const float3 bot = f3(t01.x, t01.y, t01.z) * (1.0f - a) + f3(t11.x, t11.y, t11.z) * a;
     return (top * (1.0f - b) + bot * b) * s.env_intensity;
+}
+GBPT_DI float3 env_eval(const DevScene& s, float3 dir) {
+    if (s.ew == 0u) return f3(0.f, 0.f, 0.f);
+    float u, v;
+    env_uv(s, dir, u, v);
+    return env_eval_uv(s, u, v);
 }
 
 } // namespace gbpt

@@ -108,12 +108,13 @@ struct SPd {
 };
 
 // _make_environment_map_shading_point (scene.slang:482-498)
-GBPT_DI SPd env_sp(const DevScene& sc, float3 o, float3 d) {
+// the environment seen along d, its map coordinates (u, v) already known
+GBPT_DI SPd env_sp_uv(const DevScene& sc, float3 o, float3 d, float u, float v) {
     SPd sp;
     sp.pos = o + d * kEnvDistance;
     sp.enc_fn = encode_normal(-d);
     sp.fn = -d;
-    sp.emission = env_eval(sc, d);
+    sp.emission = sc.ew ? env_eval_uv(sc, u, v) : f3(0.f, 0.f, 0.f);
     sp.frame = frame_from_normal(-d);
     sp.tex_color = f3(1.f, 1.f, 1.f);
     sp.mat = 0;
@@ -122,6 +123,11 @@ GBPT_DI SPd env_sp(const DevScene& sc, float3 o, float3 d) {
     sp.emissive = false;
     sp.env = true;
     return sp;
+}
+GBPT_DI SPd env_sp(const DevScene& sc, float3 o, float3 d) {
+    float u = 0.f, v = 0.f;
+    if (sc.ew) env_uv(sc, d, u, v);
+    return env_sp_uv(sc, o, d, u, v);
 }
 
 GBPT_DI void load_vertex(const DevScene& sc, uint32_t vi, float3& p, uint32_t& en, uint32_t& uv,
@@ -301,17 +307,19 @@ GBPT_DI uint32_t alias_pick(const uint2* t, uint32_t i, float& d) {
 }
 
 // solid-angle density of the environment strategy (piecewise constant over texels)
-GBPT_DI float env_pdf(const DevScene& sc, float3 dir) {
-    if (sc.ew == 0u) return 0.f;
-    const float3 l = normalize(env_to_local(sc, dir));
-    const float u = atan2f(l.x, -l.z) * kInv2Pi + 0.5f;
-    const float v = acosf(fminf(fmaxf(l.y, -1.f), 1.f)) * kInvPi;
+GBPT_DI float env_pdf_uv(const DevScene& sc, float u, float v) {
     const float st = sinf(v * kPi);
     if (!(st > 0.f)) return 0.f;
     const int x = min(max((int)floorf(u * sc.ew), 0), (int)sc.ew - 1);
     const int y = min(max((int)floorf(v * sc.eh), 0), (int)sc.eh - 1);
     const float pdf_uv = __ldg(&sc.env_func[(size_t)y * sc.ew + x]) / sc.env_func_int;
     return pdf_uv / (2.0f * kPi * kPi * st);
+}
+GBPT_DI float env_pdf(const DevScene& sc, float3 dir) {
+    if (sc.ew == 0u) return 0.f;
+    float u, v;
+    env_uv(sc, dir, u, v);
+    return env_pdf_uv(sc, u, v);
 }
 
 // solid-angle density of reaching an emissive triangle point: selection by power (area x
@@ -366,8 +374,10 @@ GBPT_DI LightSample sample_light(const DevScene& sc, float3 pos, Pcg& rng) {
                              M[2] * dl.x + M[5] * dl.y + M[8] * dl.z);
         ls.dir = normalize(dw);
         ls.dist = kRayTmax;
-        ls.le = env_eval(sc, ls.dir);
-        ls.pdf = sc.p_env * env_pdf(sc, ls.dir);
+        // radiance and density at the sampled map point itself (the direction maps back to it
+        // up to rounding), without the inverse trigonometry of a lookup by direction
+        ls.le = env_eval_uv(sc, u, v);
+        ls.pdf = sc.p_env * env_pdf_uv(sc, u, v);
         ls.valid = ls.pdf > 0.f;
         return ls;
     }

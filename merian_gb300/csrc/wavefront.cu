@@ -396,8 +396,12 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM)
             float ior = t4.w, last_pdf = r4.w;
             Pcg rng{__float_as_uint(qa.w)};
             SPd sp;
-            if (geom == 0xFFFFFFFFu || geom >= sc.geom_count) {
-                sp = env_sp(sc, o, d);
+            // a miss: the map coordinates serve the radiance and, with NEE, the MIS density
+            const bool miss = geom == 0xFFFFFFFFu || geom >= sc.geom_count;
+            float eu = 0.f, ev = 0.f;
+            if (miss) {
+                if (sc.ew) env_uv(sc, d, eu, ev);
+                sp = env_sp_uv(sc, o, d, eu, ev);
             } else {
                 sp = surface_sp(sc, o, d, geom, h0.w, h.y, h.z, h1.y);
             }
@@ -406,7 +410,7 @@ __global__ void __launch_bounds__(128, kShadeBlocksPerSM)
             float3 e = thr * sp.emission;
             if ((r.flags & kReqNee) && !all_zero(e)) {
                 float pl = 0.f;
-                if (sp.env) pl = sc.p_env * env_pdf(sc, d);
+                if (sp.env) pl = sc.p_env * (miss ? env_pdf_uv(sc, eu, ev) : env_pdf(sc, d));
                 else if (sp.emissive) pl = tri_light_pdf(sc, sp.emission, h.x * h.x, dot(d, sp.fn));
                 e = e * power_heuristic(last_pdf, pl);
             }
