@@ -143,39 +143,6 @@ std::vector<uint32_t> cdf_guide(const float* a, uint32_t n, uint32_t& G) {
     return g;
 }
 
-// Walker's alias table (Vose's construction) of the discrete distribution w[0, n): entry i is
-// (the probability that bin i keeps i, as float bits; the bin it gives otherwise). Built in
-// double in a fixed order, so every host makes the same table.
-void alias_table(const double* w, uint32_t n, uint32_t* out) {
-    double sum = 0.0;
-    for (uint32_t i = 0; i < n; ++i) sum += w[i];
-    std::vector<double> q(n);
-    std::vector<uint32_t> small, large;
-    for (uint32_t i = 0; i < n; ++i) {
-        q[i] = sum > 0.0 ? w[i] * (double)n / sum : 1.0;
-        (q[i] < 1.0 ? small : large).push_back(i);
-    }
-    while (!small.empty() && !large.empty()) {
-        const uint32_t a = small.back(), b = large.back();
-        small.pop_back();
-        const float pa = (float)q[a];
-        std::memcpy(&out[2 * a], &pa, 4);
-        out[2 * a + 1] = b;
-        q[b] = (q[b] + q[a]) - 1.0;
-        if (q[b] < 1.0) {
-            large.pop_back();
-            small.push_back(b);
-        }
-    }
-    // what rounding leaves on either list keeps its own bin
-    for (const std::vector<uint32_t>* l : {&small, &large})
-        for (uint32_t i : *l) {
-            const float one = 1.0f;
-            std::memcpy(&out[2 * i], &one, 4);
-            out[2 * i + 1] = i;
-        }
-}
-
 // GBPT_SHADE_TRI_RECORDS: upload the de-indexed per-triangle vertex records read by shading
 #ifndef GBPT_SHADE_TRI_RECORDS
 #define GBPT_SHADE_TRI_RECORDS 1

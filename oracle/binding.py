@@ -50,6 +50,7 @@ def load() -> C.CDLL:
         fp = C.POINTER(C.c_float)
         lib.oracle_camera_look_at.argtypes = [fp, fp, fp, f32, f32, f32, f32, vp]
         lib.oracle_camera_look_at.restype = i32
+        lib.oracle_alias_table.argtypes = [vp, u32, vp]
         # the seeded scene generators, compiled into this library from the package's source
         from merian_gb300 import _native as N
         for name, res, args in N.EXPORTS:
@@ -59,6 +60,14 @@ def load() -> C.CDLL:
                 fn.argtypes = args
         _lib = lib
     return _lib
+
+
+def alias_table(w: np.ndarray) -> np.ndarray:
+    """The package's alias table of weights w: (n, 2) uint32, (keep probability bits, alias)."""
+    w = np.ascontiguousarray(w, np.float64)
+    out = np.zeros((len(w), 2), np.uint32)
+    load().oracle_alias_table(_p(w), len(w), _p(out))
+    return out
 
 
 def _p(a) -> int:

@@ -9,6 +9,7 @@
 // of tests/bsdf/bsdf-checks.slang and the next-event-estimation estimator that the GPU adds
 // (not in the reference; unbiased against it).
 #include "oracle_math.h"
+#include "host_common.h" // the package's alias-table builder (oracle_alias_table)
 
 #include <algorithm>
 #include <array>
@@ -1621,6 +1622,12 @@ static thread_local std::string g_oracle_error;
 void set_error(const std::string& msg) { g_oracle_error = msg; }
 } // namespace gbpt
 ORACLE_API const char* oracle_last_error(void) { return gbpt::g_oracle_error.c_str(); }
+
+// The alias-table builder the package compiles into scene upload (host_common.h), for the tests
+// that check the kernels' environment sampling against the density it encodes.
+ORACLE_API void oracle_alias_table(const double* w, uint32_t n, uint32_t* out) {
+    gbpt::alias_table(w, n, out);
+}
 
 ORACLE_API int oracle_num_threads(void) {
 #ifdef _OPENMP
