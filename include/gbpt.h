@@ -371,7 +371,9 @@ GBPT_API int gbpt_set_tuning(gbpt_ctx* ctx, const gbpt_tuning* tuning);
 GBPT_API int gbpt_get_tuning(gbpt_ctx* ctx, gbpt_tuning* tuning);
 /* Autotuner: renders the frame (camera, params: a whole frame, no pixel list) under candidate
  * schedules and keeps the fastest as the context's tuning, returning it. Stage 1: each tick size
- * (2^21 .. 2^24 paths) with material sorting off and on (8 candidates); then, from the best so far,
+ * (2^24 .. 2^21 paths, largest first; a smaller tick must be at least 2 % faster to be kept, since
+ * larger ticks let more requests share one) with material sorting off and on (8 candidates,
+ * ms_out in ascending tick size); then, from the best so far,
  * one parameter at a time: trace_refill_lanes in {12, 16, 20, 24, 28} (5), trace_postpone_lanes in
  * {2, 4, 6, 8, 12} (5), trace_blocks_per_sm in {6, 7, all resident} (3). ms_out, when non-NULL,
  * receives GBPT_AUTOTUNE_CANDIDATES times in that order (NaN for candidates not run). Results are
