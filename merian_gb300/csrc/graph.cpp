@@ -442,9 +442,9 @@ class AccumulateNode : public Node {
         if (key == "max history" && !(v.n >= 1))
             throw NodeError(type() + ": max history must be at least 1");
         if (key == "firefly filter enable" && v.b)
-            throw NodeError(type() + ": the firefly filter is not implemented in this build");
+            throw NodeError(type() + ": the firefly filter is not implemented in this library");
         if (key == "hard clamp" && std::isfinite(v.n))
-            throw NodeError(type() + ": a finite hard clamp is not implemented in this build");
+            throw NodeError(type() + ": a finite hard clamp is not implemented in this library");
         if (key == "adaptivity" && v.n != 0.0)
             throw NodeError(type() + ": adaptive alpha reduction is not implemented in this "
                                      "build");
@@ -818,7 +818,7 @@ class ImageWriteNode : public Node {
 // ---- Error Plot ----------------------------------------------------------------------------------
 // error_plot.cpp: the per-channel metric of "input" against "reference" ("Metric": MSE, RMSE =
 // sqrt of the MSE, MAE; default RMSE) and its history of "History" values. Outputs (host images,
-// this build's form of the node's plot): "error" (1 x 1 RGBA: the latest metric) and "history"
+// this library's form of the node's plot): "error" (1 x 1 RGBA: the latest metric) and "history"
 // (n x 1 RGBA, oldest first).
 class ErrorPlotNode : public Node {
   public:
@@ -1082,7 +1082,7 @@ GBPT_API int gbpt_graph_create(gbpt_ctx* ctx, const char* graph_json, gbpt_graph
             auto f = registry().find(type);
             if (f == registry().end())
                 throw NodeError("node \"" + kv.first + "\": type \"" + type +
-                                "\" is not available in this build");
+                                "\" is not available in this library");
             if (g->nodes.count(kv.first)) throw NodeError("node \"" + kv.first + "\" twice");
             std::unique_ptr<Node> node = f->second();
             if (const Json* props = spec.get("properties"))

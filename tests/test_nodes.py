@@ -90,7 +90,7 @@ def test_graph_json_and_properties(native):
     assert d.set_property("a", "max history", 16) == 0 and d.properties("a", "max history") == 16
     d.set_property("a", "inf history", True)
     assert d.properties("a", "max history") is None and d.properties("a", "inf history") is False
-    # values this build cannot honour are refused, as merian's node_error
+    # values this library cannot honour are refused, as merian's node_error
     for node_name, key, value in [("a", "firefly filter enable", True), ("a", "hard clamp", 10),
                                   ("a", "adaptivity", 0.5), ("w", "format", "PNG"),
                                   ("w", "trigger", "frametime"), ("w", "advanced/scale", 0.5)]:
