@@ -307,13 +307,16 @@ GBPT_DI uint32_t alias_pick(const uint2* t, uint32_t i, float& d) {
 }
 
 // solid-angle density of the environment strategy (piecewise constant over texels)
-GBPT_DI float env_pdf_uv(const DevScene& sc, float u, float v) {
-    const float st = sinf(v * kPi);
+// the density at map point (u, v) given sin(pi v)
+GBPT_DI float env_pdf_st(const DevScene& sc, float u, float v, float st) {
     if (!(st > 0.f)) return 0.f;
     const int x = min(max((int)floorf(u * sc.ew), 0), (int)sc.ew - 1);
     const int y = min(max((int)floorf(v * sc.eh), 0), (int)sc.eh - 1);
     const float pdf_uv = __ldg(&sc.env_func[(size_t)y * sc.ew + x]) / sc.env_func_int;
     return pdf_uv / (2.0f * kPi * kPi * st);
+}
+GBPT_DI float env_pdf_uv(const DevScene& sc, float u, float v) {
+    return env_pdf_st(sc, u, v, sinf(v * kPi));
 }
 GBPT_DI float env_pdf(const DevScene& sc, float3 dir) {
     if (sc.ew == 0u) return 0.f;
@@ -363,10 +366,10 @@ GBPT_DI LightSample sample_light(const DevScene& sc, float3 pos, Pcg& rng) {
         const float fx = fminf(fmaxf((u2 - c0) / (c1 - c0), 0.f), 1.f);
 #endif
         const float u = ((float)x + fx) / (float)sc.ew, v = ((float)y + fy) / (float)sc.eh;
-        const float phi = kPi * (2.0f * u - 1.0f), theta = kPi * v;
+        // phi = pi (2u - 1), theta = pi v: sine and cosine of pi times an argument in [-1, 1]
         float sp, cp, st, ct;
-        sincosf(phi, &sp, &cp);
-        sincosf(theta, &st, &ct);
+        sincospif(2.0f * u - 1.0f, &sp, &cp);
+        sincospif(v, &st, &ct);
         const float3 dl = f3(st * sp, ct, -st * cp);
         const float* M = sc.env_m;
         const float3 dw = f3(M[0] * dl.x + M[3] * dl.y + M[6] * dl.z,
@@ -377,7 +380,7 @@ GBPT_DI LightSample sample_light(const DevScene& sc, float3 pos, Pcg& rng) {
         // radiance and density at the sampled map point itself (the direction maps back to it
         // up to rounding), without the inverse trigonometry of a lookup by direction
         ls.le = env_eval_uv(sc, u, v);
-        ls.pdf = sc.p_env * env_pdf_uv(sc, u, v);
+        ls.pdf = sc.p_env * env_pdf_st(sc, u, v, st);
         ls.valid = ls.pdf > 0.f;
         return ls;
     }
