@@ -134,7 +134,9 @@ struct RayPre {
     // the axes kx, ky, kz in bits 0-1, 2-3, 4-5 (kx = kz + 1, ky = kz + 2 mod 3); bit 6 when the
     // direction is negative along kz. The watertight test's paper swaps kx and ky for that sign
     // to keep the winding; keeping one frame per kz negates U, V, W, det and T instead, which
-    // leaves t, u and v unchanged and flips the facing.
+    // leaves t, u and v unchanged and flips the facing. The traversal keeps more of the ray in
+    // the same register (set_ray, TraceState): 7 - the direction octant in bits 8-10, the ray's
+    // instance mask in bits 16-23 and the stack depth in bits 24-31.
     uint32_t k;
     float Sx, Sy, Sz;
     float ox, oy, oz; // origin permuted to (kx, ky, kz)
