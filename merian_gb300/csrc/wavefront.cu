@@ -39,6 +39,14 @@ static_assert(kWavePaths <= kMaxWavePaths, "path ids must fit the packed queue e
 #define GBPT_SHADE_BLOCKS_PER_SM 5
 #endif
 constexpr int kShadeBlocksPerSM = GBPT_SHADE_BLOCKS_PER_SM;
+// the primary-hit kernel's budget (it traces one camera ray per thread, then shades the hit):
+// 64 registers and some spills beat the 164 registers it takes unbounded (3 blocks per SM) on
+// the 640x360 frame (primary + finalize 0.58 against 0.68 ms; 4 / 6 / 10 / 12 blocks: 0.65 /
+// 0.63 / 0.64 / 0.57)
+#ifndef GBPT_PRIMARY_BLOCKS_PER_SM
+#define GBPT_PRIMARY_BLOCKS_PER_SM 8
+#endif
+constexpr int kPrimaryBlocksPerSM = GBPT_PRIMARY_BLOCKS_PER_SM;
 
 constexpr uint32_t kReqEmission = 1u, kReqNee = 2u, kReqDemodulate = 4u;
 
@@ -113,7 +121,7 @@ GBPT_DI uint32_t chunk_by_path(const ChunkGPU* c, uint32_t n, uint32_t p) {
 GBPT_DI uint32_t pixel_id(const ReqGPU& r, uint32_t li) { return r.pixels ? __ldg(&r.pixels[li]) : li; }
 
 // Primary hit + shading point per pixel slot (gbuffer_rt.slang:18-58, render_pt.slang:98-103)
-__global__ void __launch_bounds__(128) k_primary(TickArgs t, int sort) {
+__global__ void __launch_bounds__(128, kPrimaryBlocksPerSM) k_primary(TickArgs t, int sort) {
     const uint32_t n = t.hdr->n_pix, nc = t.hdr->n_chunks;
     const uint32_t stride = gridDim.x * blockDim.x;
     // with material-sorted shading: the key of each pixel's primary hit for all its paths
