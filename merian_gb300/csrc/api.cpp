@@ -614,9 +614,13 @@ GBPT_API int gbpt_scene_create(gbpt_ctx* ctx, const gbpt_scene_desc* d, uint32_t
             std::vector<uint32_t> rec(20ull * d->triangle_count, 0u);
             for (uint64_t t = 0; t < d->triangle_count; ++t) {
                 if (fv[t] == kUnset) continue;
-                for (int c = 0; c < 3; ++c)
-                    std::memcpy(&rec[20 * t + 6 * c], &d->vertices[(uint64_t)fv[t] + d->indices[3 * t + c]],
-                                sizeof(gbpt_packed_vertex));
+                for (int c = 0; c < 3; ++c) {
+                    // a geometry outside every BLAS of a two-level scene is never traversed and
+                    // its indices were not checked: such a vertex stays zero
+                    const uint64_t vi = (uint64_t)fv[t] + d->indices[3 * t + c];
+                    if (vi < d->vertex_count)
+                        std::memcpy(&rec[20 * t + 6 * c], &d->vertices[vi], sizeof(gbpt_packed_vertex));
+                }
             }
             if ((rc = upload(&s.tri_verts, rec.data(), rec.size() * sizeof(uint32_t), bytes))) return fail(rc);
         }
